@@ -1,0 +1,674 @@
+// C ABI of the solver hot path: validation, packing into device-resident SoA, handles,
+// CUDA-graph time loops, batches.  Declared in include/neurite_gb300.h.
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "nrt_internal.h"
+#include "nrt_solver.h"
+
+namespace nrt {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int cuda_fail(cudaError_t e, const char *what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? NRT_ENOMEM : NRT_EDEVICE;
+}
+
+static int fail(int code, const std::string &msg) {
+  set_error(msg);
+  return code;
+}
+
+// ------------------------------------------------------------------ validation
+
+// Checks one tree.  strict = the numbering convention that the reference's implicit
+// assembly relies on (src/solverIm-cpu.cpp:86-145 detects terminals through
+// element[j+1].DR == j+1 and takes mother as the only lower column).
+static int validate_problem(const nrt_problem *p, bool strict, std::string &why) {
+  if (!p) return (why = "null problem", NRT_EINVAL);
+  const int32_t n = p->num_elem;
+  if (n < 4) return (why = "num_elem must be >= 4", NRT_EINVAL);
+  if (!p->mother || !p->dr || !p->dl || !p->branching || !p->terminals || !p->dx || !p->c_m ||
+      !p->r_a || !p->W || !p->K || !p->input || !p->V0)
+    return (why = "null element array", NRT_EINVAL);
+  if (p->num_term < 1) return (why = "num_term must be >= 1", NRT_EINVAL);
+  if (!(p->dT > 0)) return (why = "dT must be > 0", NRT_EINVAL);
+  if (p->num_hh < 0 || p->num_hh > n) return (why = "bad num_hh", NRT_EINVAL);
+  if (p->num_hh > 0 && (!p->hh_elem || !p->m || !p->h || !p->n || !p->g_Na || !p->g_K ||
+                        !p->G_L || !p->E_Na || !p->E_K || !p->E_L || !p->ls_Na || !p->ls_K ||
+                        !p->rest))
+    return (why = "null HH array", NRT_EINVAL);
+  std::vector<char> is_term(n, 0);
+  for (int32_t q = 0; q < p->num_term; q++) {
+    int32_t t = p->terminals[q];
+    if (t < 0 || t >= n) return (why = "terminal index out of range", NRT_ETOPOLOGY);
+    is_term[t] = 1;
+  }
+  if (p->terminals[0] + 1 >= n) return (why = "terminals[0] + 1 out of range", NRT_ETOPOLOGY);
+  for (int32_t j = 0; j < n; j++) {
+    const int32_t m = p->mother[j], r = p->dr[j], l = p->dl[j];
+    if (r < 0 || r >= n || l < 0 || l >= n) return (why = "DR/DL out of range", NRT_ETOPOLOGY);
+    if (j > 0 && (m < 0 || m >= n)) return (why = "mother out of range", NRT_ETOPOLOGY);
+    if (j == 0 && m != -1 && (m < 0 || m >= n)) return (why = "mother out of range", NRT_ETOPOLOGY);
+    if (p->branching[j] != 0 && p->branching[j] != 1) return (why = "branching must be 0/1", NRT_EINVAL);
+  }
+  for (int32_t q = 1; q < p->num_term; q++) {
+    const int32_t t = p->terminals[q];
+    if (t == 0 || p->mother[t] < 0) return (why = "terminal without a mother", NRT_ETOPOLOGY);
+    if (is_term[p->mother[t]]) return (why = "terminal whose mother is a terminal", NRT_ETOPOLOGY);
+  }
+  if (is_term[p->terminals[0] + 1]) return (why = "terminals[0] + 1 is a terminal", NRT_ETOPOLOGY);
+  int32_t prev = -1;
+  for (int32_t k = 0; k < p->num_hh; k++) {
+    const int32_t e = p->hh_elem[k];
+    if (e < 0 || e >= n || e <= prev) return (why = "hh_elem must be ascending and in range", NRT_EINVAL);
+    prev = e;
+  }
+  if (strict) {
+    if (p->terminals[0] != 0 || p->mother[0] != -1) return (why = "element 0 must be the fictitious root", NRT_ETOPOLOGY);
+    if (!is_term[n - 1]) return (why = "the last element must be a terminal", NRT_ETOPOLOGY);
+    for (int32_t j = 1; j < n; j++) {
+      const int32_t m = p->mother[j];
+      if (m >= j) return (why = "a mother must precede its child", NRT_ETOPOLOGY);
+      if (is_term[j]) {
+        if (p->dr[j] != j) return (why = "a terminal must have DR == itself", NRT_ETOPOLOGY);
+        if (m != j - 1 && !(p->branching[m] && p->dl[m] == j))
+          return (why = "a terminal's mother must be the previous element", NRT_ETOPOLOGY);
+      } else {
+        if (p->dr[j] != j + 1 || p->mother[j + 1] != j)
+          return (why = "non-terminal elements need DR == j + 1 with mother j", NRT_ETOPOLOGY);
+      }
+      if (p->branching[j]) {
+        const int32_t l = p->dl[j];
+        if (l <= j || p->mother[l] != j) return (why = "DL must be a later element whose mother is the branch point", NRT_ETOPOLOGY);
+      } else if (p->dl[j] != 0) {
+        return (why = "DL must be 0 off branch points", NRT_ETOPOLOGY);
+      }
+      if (m != j - 1 && !(p->branching[m] && p->dl[m] == j))
+        return (why = "an element's mother must be j-1 unless it is a DL child", NRT_ETOPOLOGY);
+    }
+    if (is_term[1] || is_term[2] || p->branching[1])
+      return (why = "the root branch needs at least two plain compartments", NRT_ETOPOLOGY);
+  }
+  return NRT_OK;
+}
+
+// ------------------------------------------------------------------ packing
+
+int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
+  hp.ninst = count;
+  hp.off.assign(count + 1, 0);
+  for (int32_t i = 0; i < count; i++) hp.off[i + 1] = hp.off[i] + probs[i].num_elem;
+  const int64_t N = hp.ntot = hp.off[count];
+  if (N >= ((int64_t)1 << 31)) return fail(NRT_EINVAL, "total elements exceed 2^31");
+  if (count >= (1 << (32 - INST_SHIFT))) return fail(NRT_EINVAL, "too many instances");
+  hp.topo.resize(N);
+  hp.cdt.resize(N); hp.gax.resize(N); hp.wdx.resize(N); hp.kdx.resize(N); hp.inp.resize(N);
+  hp.V0.resize(N); hp.V1.resize(N);
+  hp.c_m_dx.resize(N); hp.radx.resize(N); hp.Wfull.resize(N); hp.Kfull.resize(N);
+  hp.gate.assign(3 * N, 0.0);
+  hp.hp.assign((size_t)HP_ROWS * N, 0.0);
+  hp.inst.resize(count);
+  hp.num_elem.resize(count);
+  hp.hh_off.assign(count + 1, 0);
+  hp.hh_local.clear();
+  hp.terms.clear();
+  hp.fusable = true;
+  for (int32_t i = 0; i < count; i++) {
+    const nrt_problem &p = probs[i];
+    const int64_t o = hp.off[i];
+    const int32_t n = p.num_elem;
+    hp.num_elem[i] = n;
+    std::vector<char> is_term(n, 0);
+    for (int32_t q = 0; q < p.num_term; q++) is_term[p.terminals[q]] = 1;
+    std::vector<char> is_hh(n, 0);
+    for (int32_t k = 0; k < p.num_hh; k++) is_hh[p.hh_elem[k]] = 1;
+    for (int32_t j = 0; j < n; j++) {
+      Topo t;
+      t.mother = (int32_t)(o + (p.mother[j] >= 0 ? p.mother[j] : j));
+      t.dr = (int32_t)(o + p.dr[j]);
+      t.dl = (int32_t)(o + (p.branching[j] ? p.dl[j] : j));
+      uint32_t f = 0;
+      if (is_hh[j]) f |= F_HH;
+      if (p.branching[j]) f |= F_BRANCH;
+      if (is_term[j]) f |= F_TERM;
+      if (j == p.terminals[0]) f |= F_ROOT;
+      // Flux through a terminal neighbour is zero when that terminal copies this element.
+      auto src_of = [&](int32_t t_) { return t_ == p.terminals[0] ? t_ + 1 : p.mother[t_]; };
+      if (!is_term[j]) {
+        if (p.branching[j] && is_term[p.dl[j]]) {
+          if (src_of(p.dl[j]) == j) f |= F_DL_TERM; else hp.fusable = false;
+        }
+        if (is_term[p.dr[j]]) {
+          if (src_of(p.dr[j]) == j) f |= F_DR_TERM; else hp.fusable = false;
+        }
+        if (p.mother[j] >= 0 && is_term[p.mother[j]]) {
+          if (src_of(p.mother[j]) == j) f |= F_MO_TERM; else hp.fusable = false;
+        }
+      }
+      t.flags = f | ((uint32_t)i << INST_SHIFT);
+      hp.topo[o + j] = t;
+      const double dx = p.dx[j], c_m = p.c_m[j], r_a = p.r_a[j];
+      hp.cdt[o + j] = p.dT / (c_m * dx);     // dT/(c_m dX), src/solverEx-cpu.cpp:141
+      hp.gax[o + j] = 1.0 / (r_a * dx);      // 1/(r_a dX)
+      hp.wdx[o + j] = p.W[j] * dx;
+      hp.kdx[o + j] = p.K[j] * dx;
+      hp.inp[o + j] = p.input[j];
+      hp.V0[o + j] = p.V0[j];
+      hp.V1[o + j] = p.V1 ? p.V1[j] : p.V0[j];
+      hp.c_m_dx[o + j] = c_m * dx;
+      hp.radx[o + j] = r_a * dx;
+      hp.Wfull[o + j] = p.W[j];
+      hp.Kfull[o + j] = p.K[j];
+    }
+    for (int32_t q = 0; q < p.num_term; q++) {
+      const int32_t t = p.terminals[q];
+      hp.terms.push_back(o + t);
+      const int32_t src = (q == 0 || t == p.terminals[0]) ? t + 1 : p.mother[t];
+      if (p.V0[t] != p.V0[src]) hp.invariant = false;
+    }
+    for (int32_t k = 0; k < p.num_hh; k++) {
+      const int64_t e = o + p.hh_elem[k];
+      hp.hh_local.push_back(p.hh_elem[k]);
+      hp.gate[e] = p.m[k];
+      hp.gate[N + e] = p.h[k];
+      hp.gate[2 * N + e] = p.n[k];
+      hp.hp[HP_GNA * N + e] = p.g_Na[k];
+      hp.hp[HP_GK * N + e] = p.g_K[k];
+      hp.hp[HP_GL * N + e] = p.G_L[k];
+      hp.hp[HP_ENA * N + e] = p.E_Na[k];
+      hp.hp[HP_EK * N + e] = p.E_K[k];
+      hp.hp[HP_EL * N + e] = p.E_L[k];
+      hp.hp[HP_LSNA * N + e] = p.ls_Na[k];
+      hp.hp[HP_LSK * N + e] = p.ls_K[k];
+      hp.hp[HP_REST * N + e] = p.rest[k];
+      hp.hp[HP_DX * N + e] = p.dx[p.hh_elem[k]];
+      hp.hp[HP_DTMS * N + e] = p.dT * 1000;  // src/solverEx-cpu.cpp:96
+    }
+    hp.hh_off[i + 1] = (int64_t)hp.hh_local.size();
+    InstDev in;
+    in.base = 0;
+    in.iend = INT64_MAX;
+    in.dT = p.dT;
+    in.t0 = 0;
+    in.t1 = -1;
+    hp.inst[i] = in;
+  }
+  return NRT_OK;
+}
+
+// ------------------------------------------------------------------ device arena
+
+int Arena::reserve(size_t bytes) {
+  if (base) return NRT_EINVAL;
+  NRT_CUDA(cudaMalloc(&base, bytes));
+  cap = bytes;
+  used = 0;
+  return NRT_OK;
+}
+
+void *Arena::take(size_t bytes) {
+  size_t o = (used + 255) & ~(size_t)255;
+  if (o + bytes > cap) return nullptr;
+  used = o + bytes;
+  return (char *)base + o;
+}
+
+void Arena::release() {
+  if (base) cudaFree(base);
+  base = nullptr;
+  cap = used = 0;
+}
+
+static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+
+template <typename T>
+static int upload(Arena &a, T *&dst, const T *src, size_t count, cudaStream_t st) {
+  dst = (T *)a.take(sizeof(T) * count);
+  if (!dst) return fail(NRT_ENOMEM, "arena exhausted");
+  if (src) NRT_CUDA(cudaMemcpyAsync(dst, src, sizeof(T) * count, cudaMemcpyHostToDevice, st));
+  return NRT_OK;
+}
+
+#define TRY(x)                 \
+  do {                         \
+    int _rc = (x);             \
+    if (_rc != NRT_OK) return _rc; \
+  } while (0)
+
+int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) {
+  opt = *o;
+  if (opt.device >= 0) NRT_CUDA(cudaSetDevice(opt.device));
+  NRT_CUDA(cudaGetDevice(&device));
+  NRT_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  TRY(build_host_pack(probs, count, host));
+  const int64_t N = host.ntot;
+  const bool mixed = opt.precision == NRT_MIXED;
+  // Sizes: V x2, topo, coefficient rows, gates, HH rows, instances, terminals, implicit.
+  size_t bytes = 2 * al(8 * N) + al(sizeof(Topo) * N) + al(sizeof(InstDev) * count) +
+                 al(8 * host.terms.size() + 8);
+  if (mixed)
+    bytes += 5 * al(4 * N) + al(4 * 3 * N) + al(4 * (size_t)HP_ROWS * N);
+  else
+    bytes += 5 * al(8 * N) + al(8 * 3 * N) + al(8 * (size_t)HP_ROWS * N);
+  if (opt.mode == NRT_IMPLICIT_BE) bytes += implicit_bytes();
+  TRY(arena.reserve(bytes + 4096));
+  cudaStream_t st = stream;
+  TRY(upload(arena, V[0], host.V0.data(), N, st));
+  TRY(upload(arena, V[1], host.V1.data(), N, st));
+  Topo *topo = nullptr;
+  TRY(upload(arena, topo, host.topo.data(), N, st));
+  InstDev *inst = nullptr;
+  TRY(upload(arena, inst, host.inst.data(), count, st));
+  TRY(upload(arena, terms, host.terms.data(), host.terms.size(), st));
+  pv.ntot = N;
+  pv.ninst = count;
+  pv.topo = topo;
+  pv.inst = inst;
+  if (mixed) {
+    auto f32 = [&](const std::vector<double> &v) {
+      hostf.emplace_back(v.begin(), v.end());
+      return hostf.back().data();
+    };
+    hostf.reserve(8);
+    float *p;
+    TRY(upload(arena, p, f32(host.cdt), N, st)); pv.cdtf = p;
+    TRY(upload(arena, p, f32(host.gax), N, st)); pv.gaxf = p;
+    TRY(upload(arena, p, f32(host.wdx), N, st)); pv.wdxf = p;
+    TRY(upload(arena, p, f32(host.kdx), N, st)); pv.kdxf = p;
+    TRY(upload(arena, p, f32(host.inp), N, st)); pv.inpf = p;
+    TRY(upload(arena, p, f32(host.gate), 3 * N, st)); pv.gatef = p;
+    TRY(upload(arena, p, f32(host.hp), (size_t)HP_ROWS * N, st)); pv.hpf = p;
+  } else {
+    double *p;
+    TRY(upload(arena, p, host.cdt.data(), N, st)); pv.cdt = p;
+    TRY(upload(arena, p, host.gax.data(), N, st)); pv.gax = p;
+    TRY(upload(arena, p, host.wdx.data(), N, st)); pv.wdx = p;
+    TRY(upload(arena, p, host.kdx.data(), N, st)); pv.kdx = p;
+    TRY(upload(arena, p, host.inp.data(), N, st)); pv.inp = p;
+    TRY(upload(arena, p, host.gate.data(), 3 * N, st)); pv.gate = p;
+    TRY(upload(arena, p, host.hp.data(), (size_t)HP_ROWS * N, st)); pv.hp = p;
+  }
+  if (opt.mode == NRT_IMPLICIT_BE) TRY(implicit_init());
+  NRT_CUDA(cudaStreamSynchronize(st));
+  hostf.clear();
+  hostf.shrink_to_fit();
+  return NRT_OK;
+}
+
+Engine::~Engine() {
+  if (device >= 0) cudaSetDevice(device);
+  for (int q = 0; q < 2; q++)
+    if (graph_exec[q]) cudaGraphExecDestroy(graph_exec[q]);
+  if (stream) cudaStreamSynchronize(stream);
+  implicit_release();
+  arena.release();
+  if (stream) cudaStreamDestroy(stream);
+}
+
+// One loop iteration (update + calculate) for every instance, reading V[cur].
+int Engine::step(int k, int force) {
+  const bool general = !host.invariant && steps_done == 0;
+  if (opt.mode == NRT_IMPLICIT_BE) {
+    TRY(implicit_step(k, force));
+  } else {
+    TRY(launch_explicit_step(pv, opt.precision, general || !host.fusable, k, force, V[cur],
+                             V[cur ^ 1], stream));
+    if (general || !host.fusable)
+      TRY(launch_terminal_fixup(pv.topo, terms, (int64_t)host.terms.size(), V[cur ^ 1], stream));
+  }
+  cur ^= 1;
+  steps_done++;
+  terminals_dirty = opt.mode == NRT_EXPLICIT;
+  return NRT_OK;
+}
+
+int Engine::fixup() {
+  if (!terminals_dirty) return NRT_OK;
+  TRY(launch_terminal_fixup(pv.topo, terms, (int64_t)host.terms.size(), V[cur], stream));
+  terminals_dirty = false;
+  return NRT_OK;
+}
+
+// Runs `steps` loop iterations from every instance's current base (device-side loop
+// indices), replaying a captured graph of kChunk steps where possible.
+int Engine::advance(int64_t steps) {
+  int64_t left = steps;
+  while (left > 0 && (steps_done == 0 && !host.invariant)) {  // exact first step
+    TRY(step(0, -1));
+    TRY(launch_advance_base(pv.inst, pv.ninst, 1, stream));
+    left--;
+  }
+  const bool graphs = opt.use_graphs != 0 && opt.mode == NRT_EXPLICIT && host.fusable;
+  if (graphs && left >= kChunk) {
+    if (!graph_exec[cur]) {
+      cudaGraph_t g;
+      NRT_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      int rc = NRT_OK;
+      for (int k = 0; k < kChunk && rc == NRT_OK; k++)
+        rc = launch_explicit_step(pv, opt.precision, false, k, -1, V[(cur + k) & 1],
+                                  V[(cur + k + 1) & 1], stream);
+      if (rc == NRT_OK) rc = launch_advance_base(pv.inst, pv.ninst, kChunk, stream);
+      cudaError_t e = cudaStreamEndCapture(stream, &g);
+      if (rc != NRT_OK) return rc;
+      NRT_CUDA(e);
+      e = cudaGraphInstantiate(&graph_exec[cur], g, 0);
+      cudaGraphDestroy(g);
+      NRT_CUDA(e);
+    }
+    while (left >= kChunk) {
+      NRT_CUDA(cudaGraphLaunch(graph_exec[cur], stream));
+      steps_done += kChunk;  // kChunk is even: cur is unchanged
+      left -= kChunk;
+      terminals_dirty = true;
+    }
+  }
+  while (left > 0) {
+    TRY(step(0, -1));
+    TRY(launch_advance_base(pv.inst, pv.ninst, 1, stream));
+    left--;
+  }
+  return NRT_OK;
+}
+
+}  // namespace nrt
+
+using nrt::Engine;
+
+struct nrt_solver {
+  Engine eng;
+  int pending_input = 0;
+  bool have_update = false;
+};
+
+struct nrt_batch {
+  Engine eng;
+  std::vector<nrt_instance_run> runs;
+};
+
+extern "C" {
+
+const char *nrt_status_string(int s) {
+  switch (s) {
+    case NRT_OK: return "ok";
+    case NRT_EINVAL: return "invalid argument";
+    case NRT_ETOPOLOGY: return "invalid tree topology";
+    case NRT_ENOMEM: return "out of memory";
+    case NRT_ENOCONV: return "Krylov solve did not converge within its iteration budget";
+    case NRT_EDEVICE: return "CUDA device error";
+    case NRT_EBUDGET: return "request exceeds the memory budget";
+    case NRT_ESTATE: return "call out of order";
+    case NRT_ENOTREADY: return "result not ready";
+    default: return "unknown status";
+  }
+}
+
+const char *nrt_last_error(void) { return nrt::g_last_error.c_str(); }
+
+int nrt_options_default(nrt_options *o) {
+  if (!o) return NRT_EINVAL;
+  memset(o, 0, sizeof(*o));
+  o->mode = NRT_EXPLICIT;
+  o->precision = NRT_FP64;
+  o->krylov = NRT_GMRES;
+  o->precond = NRT_PRECOND_SEGMENT;
+  o->restart = 30;
+  o->tol_mode = NRT_TOL_ABS;
+  o->tol = 1e-14;  // RANGE_ERROR, inc/configuration.h:16
+  o->max_iter = 0;
+  o->device = -1;
+  o->use_graphs = 1;
+  return NRT_OK;
+}
+
+static int check_options(const nrt_options *o, std::string &why) {
+  if (o->mode != NRT_EXPLICIT && o->mode != NRT_IMPLICIT_BE) return (why = "bad mode", NRT_EINVAL);
+  if (o->precision != NRT_FP64 && o->precision != NRT_MIXED) return (why = "bad precision", NRT_EINVAL);
+  if (o->krylov != NRT_GMRES && o->krylov != NRT_BICGSTAB) return (why = "bad krylov", NRT_EINVAL);
+  if (o->precond < NRT_PRECOND_NONE || o->precond > NRT_PRECOND_SEGMENT) return (why = "bad precond", NRT_EINVAL);
+  if (o->restart < 1 || o->restart > nrt::kMaxRestart) return (why = "restart must be in [1, 64]", NRT_EINVAL);
+  if (!(o->tol > 0)) return (why = "tol must be > 0", NRT_EINVAL);
+  if (o->max_iter < 0) return (why = "max_iter must be >= 0", NRT_EINVAL);
+  return NRT_OK;
+}
+
+int nrt_create(const nrt_problem *p, const nrt_options *opt, nrt_solver **out) {
+  if (!p || !out) return nrt::fail(NRT_EINVAL, "null argument");
+  *out = nullptr;
+  nrt_options o;
+  if (opt) o = *opt; else nrt_options_default(&o);
+  std::string why;
+  int rc = check_options(&o, why);
+  if (rc) return nrt::fail(rc, why);
+  rc = nrt::validate_problem(p, o.mode == NRT_IMPLICIT_BE, why);
+  if (rc) return nrt::fail(rc, why);
+  nrt_solver *s = new (std::nothrow) nrt_solver();
+  if (!s) return nrt::fail(NRT_ENOMEM, "host allocation");
+  rc = s->eng.init(p, 1, &o);
+  if (rc) {
+    delete s;
+    return rc;
+  }
+  *out = s;
+  return NRT_OK;
+}
+
+int nrt_update(nrt_solver *s, int input_active) {
+  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+  s->pending_input = input_active ? 1 : 0;
+  s->have_update = true;
+  return NRT_OK;
+}
+
+int nrt_calculate(nrt_solver *s) {
+  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+  if (!s->have_update) return nrt::fail(NRT_ESTATE, "calculate() without a preceding update()");
+  NRT_CUDA(cudaSetDevice(s->eng.device));
+  int rc = s->eng.step(0, s->pending_input);
+  s->have_update = false;
+  return rc;
+}
+
+int nrt_snapshot(nrt_solver *s, double *potential) {
+  if (!s || !potential) return nrt::fail(NRT_EINVAL, "null argument");
+  nrt::Engine &e = s->eng;
+  NRT_CUDA(cudaSetDevice(e.device));
+  int rc = e.fixup();
+  if (rc) return rc;
+  NRT_CUDA(cudaMemcpyAsync(potential, e.V[e.cur], sizeof(double) * e.host.ntot,
+                           cudaMemcpyDeviceToHost, e.stream));
+  NRT_CUDA(cudaStreamSynchronize(e.stream));
+  return NRT_OK;
+}
+
+int nrt_run(nrt_solver *s, int64_t i_begin, int64_t i_end, double init_time, double end_input) {
+  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+  if (i_end < i_begin) return nrt::fail(NRT_EINVAL, "i_end < i_begin");
+  nrt::Engine &e = s->eng;
+  NRT_CUDA(cudaSetDevice(e.device));
+  nrt::InstDev in = e.host.inst[0];
+  in.base = i_begin;
+  in.iend = i_end;
+  in.t0 = init_time;
+  in.t1 = end_input;
+  e.host.inst[0] = in;
+  NRT_CUDA(cudaMemcpyAsync(e.pv.inst, &e.host.inst[0], sizeof(in), cudaMemcpyHostToDevice, e.stream));
+  int rc = e.advance(i_end - i_begin);
+  if (rc) return rc;
+  // leave the drop-in path's device loop range open again
+  e.host.inst[0].base = 0;
+  e.host.inst[0].iend = INT64_MAX;
+  NRT_CUDA(cudaMemcpyAsync(e.pv.inst, &e.host.inst[0], sizeof(in), cudaMemcpyHostToDevice, e.stream));
+  NRT_CUDA(cudaStreamSynchronize(e.stream));
+  return NRT_OK;
+}
+
+int nrt_synchronize(nrt_solver *s) {
+  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+  NRT_CUDA(cudaSetDevice(s->eng.device));
+  NRT_CUDA(cudaStreamSynchronize(s->eng.stream));
+  return NRT_OK;
+}
+
+int nrt_get_stream(nrt_solver *s, void **stream) {
+  if (!s || !stream) return nrt::fail(NRT_EINVAL, "null argument");
+  *stream = (void *)s->eng.stream;
+  return NRT_OK;
+}
+
+int nrt_batch_get_stream(nrt_batch *b, void **stream) {
+  if (!b || !stream) return nrt::fail(NRT_EINVAL, "null argument");
+  *stream = (void *)b->eng.stream;
+  return NRT_OK;
+}
+
+int nrt_potential_device(nrt_solver *s, const double **dev_ptr) {
+  if (!s || !dev_ptr) return nrt::fail(NRT_EINVAL, "null argument");
+  NRT_CUDA(cudaSetDevice(s->eng.device));
+  int rc = s->eng.fixup();
+  if (rc) return rc;
+  *dev_ptr = s->eng.V[s->eng.cur];
+  return NRT_OK;
+}
+
+int nrt_get_gates(nrt_solver *s, double *m, double *h, double *n) {
+  if (!s || !m || !h || !n) return nrt::fail(NRT_EINVAL, "null argument");
+  nrt::Engine &e = s->eng;
+  NRT_CUDA(cudaSetDevice(e.device));
+  const int64_t N = e.host.ntot;
+  std::vector<double> g(3 * N);
+  if (e.opt.precision == NRT_MIXED) {
+    std::vector<float> gf(3 * N);
+    NRT_CUDA(cudaMemcpyAsync(gf.data(), e.pv.gatef, sizeof(float) * 3 * N, cudaMemcpyDeviceToHost, e.stream));
+    NRT_CUDA(cudaStreamSynchronize(e.stream));
+    for (int64_t q = 0; q < 3 * N; q++) g[q] = gf[q];
+  } else {
+    NRT_CUDA(cudaMemcpyAsync(g.data(), e.pv.gate, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, e.stream));
+    NRT_CUDA(cudaStreamSynchronize(e.stream));
+  }
+  const int64_t nh = e.host.hh_off[1];
+  for (int64_t k = 0; k < nh; k++) {
+    const int64_t el = e.host.hh_local[k];
+    m[k] = g[el];
+    h[k] = g[N + el];
+    n[k] = g[2 * N + el];
+  }
+  return NRT_OK;
+}
+
+int nrt_get_stats(nrt_solver *s, nrt_stats *st) {
+  if (!s || !st) return nrt::fail(NRT_EINVAL, "null argument");
+  return s->eng.get_stats(st);
+}
+
+int nrt_destroy(nrt_solver *s) {
+  delete s;
+  return NRT_OK;
+}
+
+// ------------------------------------------------------------------ batches
+
+int nrt_batch_create(const nrt_problem *problems, int32_t count, const nrt_options *opt,
+                     nrt_batch **out) {
+  if (!problems || count < 1 || !out) return nrt::fail(NRT_EINVAL, "bad arguments");
+  *out = nullptr;
+  nrt_options o;
+  if (opt) o = *opt; else nrt_options_default(&o);
+  std::string why;
+  int rc = check_options(&o, why);
+  if (rc) return nrt::fail(rc, why);
+  for (int32_t i = 0; i < count; i++) {
+    rc = nrt::validate_problem(&problems[i], o.mode == NRT_IMPLICIT_BE, why);
+    if (rc) return nrt::fail(rc, "instance " + std::to_string(i) + ": " + why);
+  }
+  nrt_batch *b = new (std::nothrow) nrt_batch();
+  if (!b) return nrt::fail(NRT_ENOMEM, "host allocation");
+  rc = b->eng.init(problems, count, &o);
+  if (rc) {
+    delete b;
+    return rc;
+  }
+  b->runs.assign(count, nrt_instance_run{0, 0, 0.0, -1.0});
+  *out = b;
+  return NRT_OK;
+}
+
+int nrt_batch_set_runs(nrt_batch *b, const nrt_instance_run *runs) {
+  if (!b || !runs) return nrt::fail(NRT_EINVAL, "null argument");
+  nrt::Engine &e = b->eng;
+  NRT_CUDA(cudaSetDevice(e.device));
+  for (int32_t i = 0; i < e.pv.ninst; i++) {
+    if (runs[i].i_end < runs[i].i_begin) return nrt::fail(NRT_EINVAL, "i_end < i_begin");
+    b->runs[i] = runs[i];
+    e.host.inst[i].base = runs[i].i_begin;
+    e.host.inst[i].iend = runs[i].i_end;
+    e.host.inst[i].t0 = runs[i].init_time;
+    e.host.inst[i].t1 = runs[i].end_input;
+  }
+  NRT_CUDA(cudaMemcpyAsync(e.pv.inst, e.host.inst.data(), sizeof(nrt::InstDev) * e.pv.ninst,
+                           cudaMemcpyHostToDevice, e.stream));
+  NRT_CUDA(cudaStreamSynchronize(e.stream));
+  return NRT_OK;
+}
+
+int nrt_batch_advance(nrt_batch *b, int64_t steps) {
+  if (!b || steps < 0) return nrt::fail(NRT_EINVAL, "bad arguments");
+  NRT_CUDA(cudaSetDevice(b->eng.device));
+  return b->eng.advance(steps);
+}
+
+int nrt_batch_synchronize(nrt_batch *b) {
+  if (!b) return nrt::fail(NRT_EINVAL, "null batch");
+  NRT_CUDA(cudaSetDevice(b->eng.device));
+  NRT_CUDA(cudaStreamSynchronize(b->eng.stream));
+  return NRT_OK;
+}
+
+int nrt_batch_snapshot(nrt_batch *b, int32_t instance, double *potential) {
+  if (!b || !potential) return nrt::fail(NRT_EINVAL, "null argument");
+  nrt::Engine &e = b->eng;
+  if (instance < 0 || instance >= e.pv.ninst) return nrt::fail(NRT_EINVAL, "instance out of range");
+  NRT_CUDA(cudaSetDevice(e.device));
+  int rc = e.fixup();
+  if (rc) return rc;
+  const int64_t o = e.host.off[instance];
+  NRT_CUDA(cudaMemcpyAsync(potential, e.V[e.cur] + o, sizeof(double) * e.host.num_elem[instance],
+                           cudaMemcpyDeviceToHost, e.stream));
+  NRT_CUDA(cudaStreamSynchronize(e.stream));
+  return NRT_OK;
+}
+
+int nrt_batch_remaining(nrt_batch *b, int64_t *remaining) {
+  if (!b || !remaining) return nrt::fail(NRT_EINVAL, "null argument");
+  nrt::Engine &e = b->eng;
+  NRT_CUDA(cudaSetDevice(e.device));
+  std::vector<nrt::InstDev> in(e.pv.ninst);
+  NRT_CUDA(cudaMemcpyAsync(in.data(), e.pv.inst, sizeof(nrt::InstDev) * e.pv.ninst,
+                           cudaMemcpyDeviceToHost, e.stream));
+  NRT_CUDA(cudaStreamSynchronize(e.stream));
+  for (int32_t i = 0; i < e.pv.ninst; i++) remaining[i] = in[i].iend - in[i].base;
+  return NRT_OK;
+}
+
+int nrt_batch_get_stats(nrt_batch *b, nrt_stats *st) {
+  if (!b || !st) return nrt::fail(NRT_EINVAL, "null argument");
+  return b->eng.get_stats(st);
+}
+
+int nrt_batch_destroy(nrt_batch *b) {
+  delete b;
+  return NRT_OK;
+}
+
+}  // extern "C"

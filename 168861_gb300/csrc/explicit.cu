@@ -1,0 +1,201 @@
+// Explicit (forward Euler) step: one fused kernel per time step.
+//
+// Replaces the reference's four launches per step -- Update_HH, explicit_solver_normal,
+// explicit_solver_branch, explicit_solver_terminal (src/solverEx-gpu.cpp:87-194) -- and
+// computes what SolverExCPU::update + ::calculate compute (src/solverEx-cpu.cpp:90-168):
+//
+//   gates_j   <- gates_j + dt (alpha (1 - gate) - beta gate)            (HH elements)
+//   V'_j      =  V_j + dT/(c_m dX)_j [ b_j (V_DL - V_j) g_DL + (V_DR - V_j) g_DR
+//                                      + (V_mo - V_j) g_j + W_j dX_j V_j + K_j dX_j + I_j ]
+//   V'_t      =  V'_mother(t) for terminals, V'_0 = V'_1             (sealed ends)
+//
+// with g_x = 1/(r_a dX)_x.
+//
+// Sealed ends without a second launch: after every step a terminal holds an exact copy of
+// its source element, so the flux a neighbour sees through it, (V_t - V_j) g_t, is
+// exactly zero at the next step.  The kernel therefore skips flux terms through terminals
+// (flag bits F_*_TERM, bit-identical to the reference's subtraction of equal values) and
+// never writes terminal voltages during a run; `terminal_fixup` copies them into place
+// before anything reads V (snapshot, export, device pointer).  A terminal that is itself
+// a Hodgkin_Huxley element still advances its gates from its source's voltage, which is
+// what the reference's update() reads for it.  When the caller's initial potential breaks
+// the copy invariant, the first step runs in the general form (terminal terms evaluated,
+// then the copy launch), exactly as the reference does.
+//
+// Instances: elements of many trees are packed back to back (global indices); the
+// instance id in the flags selects dT, the stimulus window and the loop index, so one
+// launch advances every tree.  An instance whose loop range is exhausted copies V.
+#include "hh.cuh"
+#include "nrt_internal.h"
+
+namespace nrt {
+
+namespace {
+
+__device__ __forceinline__ bool input_on(const InstDev &in, int64_t i, int force) {
+  if (force >= 0) return force != 0;
+  const double t = (double)i * in.dT;   // time_run = i * dT, src/neurite.cpp:227
+  return (t >= in.t0) && (t <= in.t1);  // src/neurite.cpp:230
+}
+
+__device__ __forceinline__ int64_t ghost_source(const Topo &t, int64_t j) {
+  return (t.flags & F_ROOT) ? j + 1 : (int64_t)t.mother;
+}
+
+template <bool kGeneral>
+__global__ void __launch_bounds__(256) explicit_step_f64(PackView p, int k, int force,
+                                                         const double *__restrict__ Vin,
+                                                         double *__restrict__ Vout) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.ntot) return;
+  const Topo tj = p.topo[j];
+  const InstDev in = p.inst[tj.flags >> INST_SHIFT];
+  const int64_t i = in.base + k;
+  if (i >= in.iend) {  // this instance is done: carry V over to the other buffer
+    Vout[j] = Vin[j];
+    return;
+  }
+  const int64_t N = p.ntot;
+  const double *hp = p.hp;
+  const bool term = (tj.flags & F_TERM) != 0;
+  if (term && !(tj.flags & F_HH)) return;
+  const double v = Vin[(kGeneral || !term) ? j : ghost_source(tj, j)];
+  double wdx = 0, kdx = 0;
+  if (tj.flags & F_HH) {
+    GateStep64 g = hh_step64(v, p.gate[j], p.gate[N + j], p.gate[2 * N + j],
+                             hp[HP_LSNA * N + j], hp[HP_LSK * N + j], hp[HP_REST * N + j],
+                             hp[HP_DTMS * N + j], hp[HP_GNA * N + j], hp[HP_GK * N + j],
+                             hp[HP_GL * N + j], hp[HP_ENA * N + j], hp[HP_EK * N + j],
+                             hp[HP_EL * N + j]);
+    p.gate[j] = g.m;
+    p.gate[N + j] = g.h;
+    p.gate[2 * N + j] = g.n;
+    if (term) return;  // ghost: only its gates move
+    const double dx = hp[HP_DX * N + j];
+    wdx = g.W * dx;
+    kdx = g.K * dx;
+  } else {
+    wdx = p.wdx[j];
+    kdx = p.kdx[j];
+  }
+  const bool active = input_on(in, i, force);
+  // src/solverEx-cpu.cpp:141-152, same summation order
+  double acc = 0.0;
+  const bool skip_dl = !kGeneral && (tj.flags & F_DL_TERM);
+  const bool skip_dr = !kGeneral && (tj.flags & F_DR_TERM);
+  const bool skip_mo = !kGeneral && (tj.flags & F_MO_TERM);
+  if ((tj.flags & F_BRANCH) && !skip_dl) acc = (Vin[tj.dl] - v) * p.gax[tj.dl];
+  if (!skip_dr) acc = acc + (Vin[tj.dr] - v) * p.gax[tj.dr];
+  if (!skip_mo) acc = acc + (Vin[tj.mother] - v) * p.gax[j];
+  acc = acc + wdx * v;
+  acc = acc + kdx;
+  if (active) acc = acc + p.inp[j];
+  Vout[j] = v + p.cdt[j] * acc;
+}
+
+// Mixed precision: gates, rates, conductances and currents in FP32; V stays FP64 and the
+// neighbour differences are formed in FP64 before rounding, so the accumulator keeps
+// full precision over long horizons.
+template <bool kGeneral>
+__global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, int force,
+                                                           const double *__restrict__ Vin,
+                                                           double *__restrict__ Vout) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.ntot) return;
+  const Topo tj = p.topo[j];
+  const InstDev in = p.inst[tj.flags >> INST_SHIFT];
+  const int64_t i = in.base + k;
+  if (i >= in.iend) {
+    Vout[j] = Vin[j];
+    return;
+  }
+  const int64_t N = p.ntot;
+  const float *hp = p.hpf;
+  const bool term = (tj.flags & F_TERM) != 0;
+  if (term && !(tj.flags & F_HH)) return;
+  const double v = Vin[(kGeneral || !term) ? j : ghost_source(tj, j)];
+  float wdx, kdx;
+  if (tj.flags & F_HH) {
+    const double rest = (double)hp[HP_REST * N + j];
+    const float dvna = (float)((v + (double)hp[HP_LSNA * N + j]) - rest);
+    const float dvk = (float)((v + (double)hp[HP_LSK * N + j]) - rest);
+    GateStep32 g = hh_step32(dvna, dvk, p.gatef[j], p.gatef[N + j], p.gatef[2 * N + j],
+                             hp[HP_DTMS * N + j], hp[HP_GNA * N + j], hp[HP_GK * N + j],
+                             hp[HP_GL * N + j], hp[HP_ENA * N + j], hp[HP_EK * N + j],
+                             hp[HP_EL * N + j]);
+    p.gatef[j] = g.m;
+    p.gatef[N + j] = g.h;
+    p.gatef[2 * N + j] = g.n;
+    if (term) return;
+    const float dx = hp[HP_DX * N + j];
+    wdx = g.W * dx;
+    kdx = g.K * dx;
+  } else {
+    wdx = p.wdxf[j];
+    kdx = p.kdxf[j];
+  }
+  const bool active = input_on(in, i, force);
+  float acc = 0.0f;
+  if ((tj.flags & F_BRANCH) && (kGeneral || !(tj.flags & F_DL_TERM)))
+    acc = (float)(Vin[tj.dl] - v) * p.gaxf[tj.dl];
+  if (kGeneral || !(tj.flags & F_DR_TERM))
+    acc = fmaf((float)(Vin[tj.dr] - v), p.gaxf[tj.dr], acc);
+  if (kGeneral || !(tj.flags & F_MO_TERM))
+    acc = fmaf((float)(Vin[tj.mother] - v), p.gaxf[j], acc);
+  acc = fmaf(wdx, (float)v, acc) + kdx;
+  if (active) acc += p.inpf[j];
+  Vout[j] = v + (double)(p.cdtf[j] * acc);
+}
+
+// V_t = V_source(t) for every terminal (src/solverEx-cpu.cpp:155-161).
+__global__ void terminal_fixup(const Topo *__restrict__ topo, const int64_t *__restrict__ terms,
+                               int64_t nterm, double *__restrict__ V) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nterm) return;
+  const int64_t t = terms[q];
+  V[t] = V[ghost_source(topo[t], t)];
+}
+
+__global__ void advance_base(InstDev *inst, int32_t ninst, int64_t steps) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ninst) return;
+  int64_t b = inst[i].base + steps;
+  inst[i].base = b < inst[i].iend ? b : inst[i].iend;
+}
+
+}  // namespace
+
+int launch_explicit_step(const PackView &pv, int precision, bool general, int k, int force,
+                         const double *Vin, double *Vout, cudaStream_t st) {
+  const int threads = 256;
+  const unsigned blocks = (unsigned)((pv.ntot + threads - 1) / threads);
+  if (precision == NRT_MIXED) {
+    if (general)
+      explicit_step_mixed<true><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout);
+    else
+      explicit_step_mixed<false><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout);
+  } else {
+    if (general)
+      explicit_step_f64<true><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout);
+    else
+      explicit_step_f64<false><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout);
+  }
+  NRT_CUDA(cudaGetLastError());
+  return NRT_OK;
+}
+
+int launch_terminal_fixup(const Topo *topo, const int64_t *terms, int64_t nterm, double *V,
+                          cudaStream_t st) {
+  if (nterm <= 0) return NRT_OK;
+  terminal_fixup<<<(unsigned)((nterm + 255) / 256), 256, 0, st>>>(topo, terms, nterm, V);
+  NRT_CUDA(cudaGetLastError());
+  return NRT_OK;
+}
+
+int launch_advance_base(InstDev *inst, int32_t ninst, int64_t steps, cudaStream_t st) {
+  advance_base<<<(ninst + 255) / 256, 256, 0, st>>>(inst, ninst, steps);
+  NRT_CUDA(cudaGetLastError());
+  return NRT_OK;
+}
+
+}  // namespace nrt

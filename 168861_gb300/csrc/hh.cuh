@@ -1,0 +1,81 @@
+// Hodgkin-Huxley rate functions and the forward-Euler gate step, FP64 and FP32 forms.
+//
+// Model: src/coupling.cpp:25-48 (hhRate_Const), gate and conductance update
+// src/solverEx-cpu.cpp:106-127, W and K src/discretization.cpp:99-104.  Voltages enter in
+// mV relative to rest (SCALE 0.001, inc/configuration.h:36) and dt in ms.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace nrt {
+
+struct GateStep64 {
+  double m, h, n;   // gates after the step
+  double W, K;      // membrane coefficients with the new gates
+};
+
+// FP64: the reference's expressions with constant divisions turned into products.
+__device__ __forceinline__ GateStep64 hh_step64(double v, double m0, double h0, double n0,
+                                                double ls_na, double ls_k, double rest,
+                                                double dt_ms, double gNa, double gK, double GL,
+                                                double ENa, double EK, double EL) {
+  const double vna = ((v + ls_na) - rest) * 1000.0;
+  const double vk = ((v + ls_k) - rest) * 1000.0;
+  const double xm = 2.5 - 0.1 * vna;
+  const double am = xm / (exp(xm) - 1.0);
+  const double bm = 4.0 * exp(vna * (-1.0 / 18.0));
+  const double ah = 0.07 * exp(vna * (-1.0 / 20.0));
+  const double bh = 1.0 / (exp(3.0 - 0.1 * vna) + 1.0);
+  const double xn = 1.0 - 0.1 * vk;
+  const double an = (0.1 - 0.01 * vk) / (exp(xn) - 1.0);
+  const double bn = 0.125 * exp(vk * (-1.0 / 80.0));
+  GateStep64 r;
+  r.m = m0 + dt_ms * (am * (1.0 - m0) - bm * m0);
+  r.h = h0 + dt_ms * (ah * (1.0 - h0) - bh * h0);
+  r.n = n0 + dt_ms * (an * (1.0 - n0) - bn * n0);
+  const double G_Na = gNa * r.m * r.m * r.m * r.h;
+  const double G_K = gK * r.n * r.n * r.n * r.n;
+  r.W = -(G_Na + G_K + GL);
+  r.K = G_Na * ENa + G_K * EK + GL * EL;
+  return r;
+}
+
+// x / (e^x - 1), the shape of alpha_m and alpha_n, with its removable singularity at 0
+// handled by the series 1 / (1 + x/2 + x^2/6) for |x| < 1e-3.
+__device__ __forceinline__ float xexpm1_ratio(float x, float ex) {
+  return fabsf(x) < 1e-3f ? __frcp_rn(fmaf(x, fmaf(x, 1.0f / 6.0f, 0.5f), 1.0f))
+                          : __fdividef(x, ex - 1.0f);
+}
+
+struct GateStep32 {
+  float m, h, n, W, K;
+};
+
+// FP32 form for the mixed-precision path.  dv_na / dv_k are (V + LS - rest) in volts,
+// formed in FP64 by the caller and rounded once.  exp(3 - 0.1 v) is e^0.5 * exp(2.5 - 0.1 v).
+__device__ __forceinline__ GateStep32 hh_step32(float dv_na, float dv_k, float m0, float h0,
+                                                float n0, float dt_ms, float gNa, float gK,
+                                                float GL, float ENa, float EK, float EL) {
+  const float vna = dv_na * 1000.0f;
+  const float vk = dv_k * 1000.0f;
+  const float xm = fmaf(-0.1f, vna, 2.5f);
+  const float exm = __expf(xm);
+  const float am = xexpm1_ratio(xm, exm);
+  const float bm = 4.0f * __expf(vna * (-1.0f / 18.0f));
+  const float ah = 0.07f * __expf(vna * (-1.0f / 20.0f));
+  const float bh = __frcp_rn(fmaf(exm, 1.6487212707001282f, 1.0f));
+  const float xn = fmaf(-0.1f, vk, 1.0f);
+  const float an = 0.1f * xexpm1_ratio(xn, __expf(xn));
+  const float bn = 0.125f * __expf(vk * (-1.0f / 80.0f));
+  GateStep32 r;
+  r.m = fmaf(dt_ms, am * (1.0f - m0) - bm * m0, m0);
+  r.h = fmaf(dt_ms, ah * (1.0f - h0) - bh * h0, h0);
+  r.n = fmaf(dt_ms, an * (1.0f - n0) - bn * n0, n0);
+  const float G_Na = gNa * r.m * r.m * r.m * r.h;
+  const float n2 = r.n * r.n;
+  const float G_K = gK * n2 * n2;
+  r.W = -(G_Na + G_K + GL);
+  r.K = fmaf(G_Na, ENa, fmaf(G_K, EK, GL * EL));
+  return r;
+}
+
+}  // namespace nrt

@@ -1,0 +1,109 @@
+// Internal definitions shared by the host runtime (api.cu, pack.cu) and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "neurite_gb300.h"
+
+namespace nrt {
+
+// Per-element flag bits (low 12 bits of Topo::flags; the instance id sits above).
+enum : uint32_t {
+  F_HH = 1u,        // Hodgkin_Huxley element (gates evolve)
+  F_BRANCH = 2u,    // branching point: has a DL child
+  F_TERM = 4u,      // terminal: copies a neighbour after the step (explicit)
+  F_ROOT = 8u,      // terminals[0]: copies element root+1 (src/solverEx-cpu.cpp:157)
+  F_UP = 16u,       // implicit row has a column at its mother
+  F_DOWNR = 32u,    // implicit row has a column at DR (== j + 1)
+  F_IDENT = 64u,    // implicit identity row (left untouched by the reference)
+  F_DL_TERM = 128u, // explicit: the DL neighbour is a terminal (zero flux)
+  F_MO_TERM = 256u, // explicit: the mother is a terminal (element 1 next to the root)
+  F_DR_TERM = 512u, // explicit: the DR neighbour is a terminal (zero flux)
+  F_DOWNL = 1024u,  // implicit row has a column at DL
+};
+constexpr int INST_SHIFT = 12;
+
+// Topology of one element, global (packed) indices.  16 bytes, loaded as one int4.
+struct __align__(16) Topo {
+  int32_t mother;   // explicit: neighbour for the mother term; -1 at the root
+  int32_t dr;       // DR (== self for terminals)
+  int32_t dl;       // DL (branch points only; else the element itself)
+  uint32_t flags;   // F_* | instance << INST_SHIFT
+};
+
+// HH parameters per element, SoA rows of Pack::hp (FP64) / Pack::hpf (FP32).
+enum { HP_GNA, HP_GK, HP_GL, HP_ENA, HP_EK, HP_EL, HP_LSNA, HP_LSK, HP_REST, HP_DX, HP_DTMS, HP_ROWS };
+
+// Per-instance run state kept on the device.
+struct InstDev {
+  int64_t base;     // loop index of the next step
+  int64_t iend;     // one past the last loop index
+  double dT;
+  double t0, t1;    // stimulus window
+};
+
+// Device-side view passed by value to the kernels.
+struct PackView {
+  int64_t ntot;
+  int32_t ninst;
+  const Topo *topo;
+  const double *cdt;   // dT / (c_m dX)
+  const double *gax;   // 1 / (r_a dX): conductance to the mother
+  const double *wdx;   // W dX (cables)
+  const double *kdx;   // K dX (cables)
+  const double *inp;   // injected current
+  double *gate;        // [3][ntot] m, h, n (FP64 path)
+  float *gatef;        // [3][ntot] (mixed path)
+  const double *hp;    // [HP_ROWS][ntot]
+  const float *hpf;    // [HP_ROWS][ntot]
+  const float *cdtf, *gaxf, *wdxf, *kdxf, *inpf;  // FP32 copies (mixed path)
+  InstDev *inst;
+};
+
+struct DeviceBuffer {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+};
+
+// Host-side error helper: records the message in a thread-local slot.
+void set_error(const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+#define NRT_CUDA(call)                                        \
+  do {                                                        \
+    cudaError_t _e = (call);                                  \
+    if (_e != cudaSuccess) return ::nrt::cuda_fail(_e, #call); \
+  } while (0)
+
+// Host mirror of the packed trees: built from nrt_problem arrays.
+struct HostPack {
+  int64_t ntot = 0;
+  int32_t ninst = 0;
+  std::vector<int64_t> off;         // element offset per instance (ninst + 1)
+  std::vector<Topo> topo;
+  std::vector<double> cdt, gax, wdx, kdx, inp, V0, V1;
+  std::vector<double> gate;         // [3][ntot]
+  std::vector<double> hp;           // [HP_ROWS][ntot]
+  std::vector<double> c_m_dx, radx; // c_m dX and r_a dX per element (implicit assembly)
+  std::vector<double> Wfull, Kfull; // W, K per element as given
+  std::vector<InstDev> inst;
+  std::vector<int32_t> hh_local;    // per instance: HH element indices (local), concatenated
+  std::vector<int64_t> hh_off;      // per instance offsets into hh_local (ninst + 1)
+  std::vector<int32_t> num_elem;    // per instance
+  std::vector<int64_t> terms;       // global indices of all terminals
+  bool fusable = true;              // every terminal neighbour copies its reader
+  bool invariant = true;            // initial V already has terminals equal to their sources
+};
+
+int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp);
+
+// Kernel launchers (explicit.cu).
+int launch_explicit_step(const PackView &pv, int precision, bool general, int k, int force,
+                         const double *Vin, double *Vout, cudaStream_t st);
+int launch_terminal_fixup(const Topo *topo, const int64_t *terms, int64_t nterm, double *V,
+                          cudaStream_t st);
+int launch_advance_base(InstDev *inst, int32_t ninst, int64_t steps, cudaStream_t st);
+
+}  // namespace nrt

@@ -1,0 +1,50 @@
+// The engine behind a solver handle or a batch: one device arena holding the packed
+// trees, the two potential buffers, and (implicit mode) the Krylov workspace.
+#pragma once
+#include "nrt_internal.h"
+
+namespace nrt {
+
+constexpr int kChunk = 64;        // steps per captured graph (even: buffer parity returns)
+constexpr int kMaxRestart = 64;   // GMRES restart limit (Hessenberg kept in shared memory)
+
+struct Arena {
+  void *base = nullptr;
+  size_t cap = 0, used = 0;
+  int reserve(size_t bytes);
+  void *take(size_t bytes);
+  void release();
+};
+
+struct ImplicitState;  // implicit.cu
+
+struct Engine {
+  nrt_options opt{};
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  HostPack host;
+  Arena arena;
+  PackView pv{};
+  double *V[2] = {nullptr, nullptr};
+  int cur = 0;
+  int64_t *terms = nullptr;
+  int64_t steps_done = 0;
+  bool terminals_dirty = false;
+  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};  // one per starting buffer parity
+  std::vector<std::vector<float>> hostf;  // staging for FP32 uploads
+  ImplicitState *im = nullptr;
+
+  int init(const nrt_problem *probs, int32_t count, const nrt_options *o);
+  int step(int k, int force);
+  int advance(int64_t steps);
+  int fixup();
+  int get_stats(nrt_stats *st);
+  // implicit.cu
+  size_t implicit_bytes() const;
+  int implicit_init();
+  int implicit_step(int k, int force);
+  void implicit_release();
+  ~Engine();
+};
+
+}  // namespace nrt

@@ -1,0 +1,305 @@
+"""Host-side mirror of the reference's solver interface over the C ABI.
+
+`SolverEx` / `SolverIm` follow `class Solver` (inc/solver.h:12-24): update(input_active),
+calculate(), snapshot().  They are built from the same inputs as the reference solver
+constructors (src/solverEx-gpu.cpp:204-439, src/solverIm-gpu.cpp:381-682): the tree and
+the per-element values produced by the parameter pipeline (src/init.cpp:235-298), which
+`derive()` computes on the host with the library's nrt_derive.
+
+`Batch` packs many trees into one device-resident set of arrays and advances them with
+one launch per step (no reference counterpart).
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+_PREC = {"fp64": _lib.NRT_FP64, "mixed": _lib.NRT_MIXED}
+_KRY = {"gmres": _lib.NRT_GMRES, "bicgstab": _lib.NRT_BICGSTAB}
+_PC = {"none": _lib.NRT_PRECOND_NONE, "jacobi": _lib.NRT_PRECOND_JACOBI,
+       "segment": _lib.NRT_PRECOND_SEGMENT}
+
+
+@dataclasses.dataclass
+class Derived:
+    """Output of the parameter pipeline: eparam [6][n] = (c_m, r_a, dX, W, K, critical dT),
+    hh_elem [num_hh], hparam [12][num_hh] = (m, h, n, g_Na, g_K, G_L, E_Na, E_K, E_L,
+    LS_Na, LS_K, rest), dT_crit."""
+    eparam: np.ndarray
+    hh_elem: np.ndarray
+    hparam: np.ndarray
+    dT_crit: float
+
+    @property
+    def num_hh(self) -> int:
+        return int(self.hh_elem.shape[0])
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(ctypes.POINTER(ct))
+
+
+def derive(spec) -> Derived:
+    """Runs the reference's parameter pipeline (nrt_derive) for a model.TreeSpec."""
+    lib = _lib.load()
+    n = spec.n
+    nh = int(np.count_nonzero(spec.kind == 1))
+    isp = spec.ispec()
+    dsp = spec.dspec()
+    ep = np.zeros((6, n))
+    he = np.zeros(max(nh, 1), np.int32)
+    hpar = np.zeros((12, max(nh, 1)))
+    nho = ctypes.c_int32(0)
+    crit = ctypes.c_double(0)
+    check(lib.nrt_derive(n, _p(isp, ctypes.c_int32), _p(dsp, ctypes.c_double), int(spec.myelin),
+                         spec.e_max, _p(ep, ctypes.c_double), _p(he, ctypes.c_int32),
+                         _p(hpar, ctypes.c_double), ctypes.byref(nho), ctypes.byref(crit)),
+          "nrt_derive")
+    hparam = np.ascontiguousarray(hpar.reshape(12, max(nh, 1))[:, :nh]) if nh else np.zeros((12, 0))
+    return Derived(ep, he[:nh].copy(), hparam, crit.value)
+
+
+def step_size(spec, d: Derived) -> float:
+    """dT = dtf * critical dT, or the spec's absolute step (src/neurite.cpp:171-173)."""
+    return spec.dt_abs if spec.dt_abs > 0 else d.dT_crit * spec.dtf
+
+
+class ProblemArrays:
+    """Keeps the numpy arrays of one nrt_problem alive and exposes the C struct."""
+
+    def __init__(self, *, mother, dr, dl, branching, terminals, dx, c_m, r_a, W, K, input,
+                 hh_elem, m, h, n, g_Na, g_K, G_L, E_Na, E_K, E_L, ls_Na, ls_K, rest, V0,
+                 V1=None, dT):
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        self.arrays = dict(mother=i32(mother), dr=i32(dr), dl=i32(dl), branching=i32(branching),
+                           terminals=i32(terminals), dx=f64(dx), c_m=f64(c_m), r_a=f64(r_a),
+                           W=f64(W), K=f64(K), input=f64(input), hh_elem=i32(hh_elem), m=f64(m),
+                           h=f64(h), n=f64(n), g_Na=f64(g_Na), g_K=f64(g_K), G_L=f64(G_L),
+                           E_Na=f64(E_Na), E_K=f64(E_K), E_L=f64(E_L), ls_Na=f64(ls_Na),
+                           ls_K=f64(ls_K), rest=f64(rest), V0=f64(V0))
+        if V1 is not None:
+            self.arrays["V1"] = f64(V1)
+        a = self.arrays
+        s = _lib.Problem()
+        s.num_elem = len(a["mother"])
+        s.num_term = len(a["terminals"])
+        s.num_hh = len(a["hh_elem"])
+        s.dT = float(dT)
+        for k, v in a.items():
+            setattr(s, k, _p(v, ctypes.c_int32 if v.dtype == np.int32 else ctypes.c_double))
+        self.struct = s
+        self.dT = float(dT)
+
+    @property
+    def num_elem(self) -> int:
+        return int(self.struct.num_elem)
+
+    @classmethod
+    def from_spec(cls, spec, d: Derived, dT: float | None = None, V0=None, V1=None,
+                  hparam=None):
+        """Inputs of the reference solver constructors for a spec after derivation."""
+        dT = step_size(spec, d) if dT is None else dT
+        hp = d.hparam if hparam is None else hparam
+        V0 = spec.rest_pot.copy() if V0 is None else V0  # setting_rest_pot, src/init.cpp:260-267
+        e = d.eparam
+        return cls(mother=spec.mother, dr=spec.dr, dl=spec.dl, branching=spec.branching,
+                   terminals=spec.terminals, dx=e[2], c_m=e[0], r_a=e[1], W=e[3], K=e[4],
+                   input=spec.input_current, hh_elem=d.hh_elem, m=hp[0], h=hp[1], n=hp[2],
+                   g_Na=hp[3], g_K=hp[4], G_L=hp[5], E_Na=hp[6], E_K=hp[7], E_L=hp[8],
+                   ls_Na=hp[9], ls_K=hp[10], rest=hp[11], V0=V0, V1=V1, dT=dT)
+
+
+def make_options(mode: int, precision: str = "fp64", krylov: str = "gmres",
+                 precond: str = "segment", restart: int = 30, tol: float = 1e-14,
+                 tol_mode: str = "abs", max_iter: int = 0, use_graphs: bool = True,
+                 device: int = -1) -> _lib.Options:
+    lib = _lib.load()
+    o = _lib.Options()
+    check(lib.nrt_options_default(ctypes.byref(o)), "nrt_options_default")
+    o.mode = mode
+    o.precision = _PREC[precision]
+    o.krylov = _KRY[krylov]
+    o.precond = _PC[precond]
+    o.restart = restart
+    o.tol = tol
+    o.tol_mode = _lib.NRT_TOL_ABS if tol_mode == "abs" else _lib.NRT_TOL_REL
+    o.max_iter = max_iter
+    o.use_graphs = int(use_graphs)
+    o.device = device
+    return o
+
+
+class Solver:
+    """inc/solver.h:12-24 over the C ABI."""
+
+    mode = _lib.NRT_EXPLICIT
+
+    def __init__(self, problem: ProblemArrays, **opts):
+        self.lib = _lib.load()
+        self.problem = problem
+        self.options = make_options(self.mode, **opts)
+        h = ctypes.c_void_p()
+        check(self.lib.nrt_create(ctypes.byref(problem.struct), ctypes.byref(self.options),
+                                  ctypes.byref(h)), "nrt_create")
+        self.h = h
+        self.n = problem.num_elem
+        self.num_hh = int(problem.struct.num_hh)
+
+    def update(self, input_active: bool) -> None:
+        check(self.lib.nrt_update(self.h, int(bool(input_active))), "nrt_update")
+
+    def calculate(self) -> None:
+        check(self.lib.nrt_calculate(self.h), "nrt_calculate")
+
+    def snapshot(self, out: np.ndarray | None = None) -> np.ndarray:
+        out = np.empty(self.n) if out is None else out
+        check(self.lib.nrt_snapshot(self.h, _p(out, ctypes.c_double)), "nrt_snapshot")
+        return out
+
+    def run(self, i_begin: int, i_end: int, init_time: float, end_input: float) -> None:
+        """The driver loop of src/neurite.cpp:224-236 for i in [i_begin, i_end)."""
+        check(self.lib.nrt_run(self.h, int(i_begin), int(i_end), float(init_time),
+                               float(end_input)), "nrt_run")
+
+    def synchronize(self) -> None:
+        check(self.lib.nrt_synchronize(self.h), "nrt_synchronize")
+
+    def stream(self) -> int:
+        """The handle's cudaStream_t as an integer (for timing events on it)."""
+        v = ctypes.c_void_p()
+        check(self.lib.nrt_get_stream(self.h, ctypes.byref(v)), "nrt_get_stream")
+        return int(v.value or 0)
+
+    def gates(self):
+        nh = self.num_hh
+        m, h, n = np.empty(nh), np.empty(nh), np.empty(nh)
+        if nh:
+            check(self.lib.nrt_get_gates(self.h, _p(m, ctypes.c_double), _p(h, ctypes.c_double),
+                                         _p(n, ctypes.c_double)), "nrt_get_gates")
+        return m, h, n
+
+    def stats(self) -> _lib.Stats:
+        st = _lib.Stats()
+        check(self.lib.nrt_get_stats(self.h, ctypes.byref(st)), "nrt_get_stats")
+        return st
+
+    def export_system(self, input_active: bool):
+        n = self.n
+        cap = 4 * n + 2
+        rp = np.zeros(n + 1, np.int32)
+        col = np.zeros(cap, np.int32)
+        val = np.zeros(cap)
+        rhs = np.zeros(n)
+        nnz = ctypes.c_int32(0)
+        check(self.lib.nrt_export_system(self.h, int(bool(input_active)), _p(rp, ctypes.c_int32),
+                                         _p(col, ctypes.c_int32), _p(val, ctypes.c_double),
+                                         _p(rhs, ctypes.c_double), ctypes.byref(nnz)),
+              "nrt_export_system")
+        k = nnz.value
+        return rp, col[:k].copy(), val[:k].copy(), rhs
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.nrt_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class SolverEx(Solver):
+    """Replaces SolverExGPU / SolverExCPU (explicit forward Euler)."""
+    mode = _lib.NRT_EXPLICIT
+
+
+class SolverIm(Solver):
+    """Replaces SolverImGPU / SolverImCPU (implicit backward Euler)."""
+    mode = _lib.NRT_IMPLICIT_BE
+
+
+class Batch:
+    """Many independent trees advanced together (one launch per step for all of them)."""
+
+    def __init__(self, problems: list[ProblemArrays], mode: int = _lib.NRT_EXPLICIT, **opts):
+        self.lib = _lib.load()
+        self.problems = problems
+        arr = (_lib.Problem * len(problems))(*[p.struct for p in problems])
+        self._arr = arr
+        self.options = make_options(mode, **opts)
+        h = ctypes.c_void_p()
+        check(self.lib.nrt_batch_create(arr, len(problems), ctypes.byref(self.options),
+                                        ctypes.byref(h)), "nrt_batch_create")
+        self.h = h
+        self.count = len(problems)
+
+    def set_runs(self, runs) -> None:
+        """runs: iterable of (i_begin, i_end, init_time, end_input)."""
+        arr = (_lib.InstanceRun * self.count)(*[_lib.InstanceRun(int(a), int(b), float(c), float(d))
+                                                  for a, b, c, d in runs])
+        check(self.lib.nrt_batch_set_runs(self.h, arr), "nrt_batch_set_runs")
+
+    def advance(self, steps: int) -> None:
+        check(self.lib.nrt_batch_advance(self.h, int(steps)), "nrt_batch_advance")
+
+    def synchronize(self) -> None:
+        check(self.lib.nrt_batch_synchronize(self.h), "nrt_batch_synchronize")
+
+    def stream(self) -> int:
+        v = ctypes.c_void_p()
+        check(self.lib.nrt_batch_get_stream(self.h, ctypes.byref(v)), "nrt_batch_get_stream")
+        return int(v.value or 0)
+
+    def snapshot(self, i: int) -> np.ndarray:
+        out = np.empty(self.problems[i].num_elem)
+        check(self.lib.nrt_batch_snapshot(self.h, i, _p(out, ctypes.c_double)), "nrt_batch_snapshot")
+        return out
+
+    def remaining(self) -> np.ndarray:
+        out = np.zeros(self.count, np.int64)
+        check(self.lib.nrt_batch_remaining(self.h, _p(out, ctypes.c_int64)), "nrt_batch_remaining")
+        return out
+
+    def stats(self) -> _lib.Stats:
+        st = _lib.Stats()
+        check(self.lib.nrt_batch_get_stats(self.h, ctypes.byref(st)), "nrt_batch_get_stats")
+        return st
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.nrt_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def simulate(spec, mode: str = "explicit", steps: int | None = None, **opts):
+    """Runs the reference driver loop (src/neurite.cpp:171-236) for a spec; returns
+    (final V, solver).  steps limits the loop to i in [1, 1 + steps)."""
+    d = derive(spec)
+    dT = step_size(spec, d)
+    prob = ProblemArrays.from_spec(spec, d, dT)
+    cls = SolverEx if mode == "explicit" else SolverIm
+    s = cls(prob, **opts)
+    ns = spec.num_steps(dT)
+    i_end = ns - 1 if steps is None else min(ns - 1, 1 + steps)
+    s.run(1, i_end, spec.init_time, spec.end_input)
+    return s.snapshot(), s

@@ -1,0 +1,372 @@
+"""Benchmark of the solver hot path: compartment-steps/s on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
+
+A "step" is one loop iteration of the reference driver (src/neurite.cpp:224-236:
+update + calculate) applied to every tree of the workload.  `value` is whole-job
+throughput with the trees resident in HBM (CUDA events on the library's stream around K
+steps); `e2e` is the same metric through the public C ABI from host buffers (create =
+H2D of every tree, K steps, snapshot of every tree = D2H).  Inputs are larger than L2.
+
+Workloads (synthetic, seeded; see model.py):
+  batch-implicit-mixed  4096 random trees, 1e3-1e5 elements log-uniform, implicit backward
+                        Euler, FP32 GMRES(20) inner + FP64 refinement to 1e-10 (relative),
+                        dt 0.025 ms, stimulus U(0.5, 3) nA, strain U(0, 0.15)
+  batch-explicit-mixed  the same tree population, explicit, mixed precision, dt 0.8 dT_crit
+  batch-explicit-fp64   as above in plain FP64
+  axon-explicit-fp64    the 1 cm squid axon (1002 elements), plain FP64 (single tree)
+
+--impl reference times the oracle port of the reference's CPU solver (no GPU) on the box's
+host cores over a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import math
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "compartment-steps/s"
+WORKLOADS = ("batch-implicit-mixed", "batch-explicit-mixed", "batch-explicit-fp64",
+             "axon-explicit-fp64")
+DEFAULT_WORKLOAD = "batch-explicit-mixed"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=0)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--workload", choices=WORKLOADS, default=DEFAULT_WORKLOAD)
+    ap.add_argument("--trees", type=int, default=0, help="override the tree count (probes only)")
+    ap.add_argument("--seed", type=int, default=20261203)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ workloads
+
+def tree_population(count: int, seed: int):
+    model = importlib.import_module("168861_gb300.model")
+    sizes = model.log_uniform_sizes(count, 1e3, 1e5, seed)
+    return [(seed * 7919 + i, int(sizes[i])) for i in range(count)]
+
+
+def build_batch_problems(workload: str, count: int, seed: int, rank: int, world: int):
+    pkg = importlib.import_module("168861_gb300")
+    model = pkg.model
+    pop = tree_population(count, seed)[rank::world]
+    probs, runs = [], []
+    n_elem = 0
+    for tseed, size in pop:
+        spec = model.random_tree(seed=tseed, n_target=size)
+        d = pkg.derive(spec)
+        if workload.startswith("batch-explicit"):
+            dT = 0.8 * d.dT_crit
+        else:
+            dT = spec.dt_abs
+        p = pkg.ProblemArrays.from_spec(spec, d, dT)
+        probs.append(p)
+        runs.append((1, spec.num_steps(dT) - 1, spec.init_time, spec.end_input))
+        n_elem += spec.n
+        del spec, d
+    return probs, runs, n_elem
+
+
+def workload_config(workload: str, count: int):
+    if workload == "axon-explicit-fp64":
+        return {"workload": "axon-explicit-fp64", "trees": 1, "elements_per_tree": 1002,
+                "mode": "explicit", "precision": "fp64", "dt": "0.8 dT_crit = 8e-4 ms"}
+    cfg = {"workload": workload, "trees": count, "elements_per_tree": "log-uniform 1e3-1e5",
+           "depth": "4-12", "branching_prob": "0.6-0.9", "stimulus_nA": "U(0.5,3)",
+           "strain": "U(0,0.15)"}
+    if workload == "batch-implicit-mixed":
+        cfg.update(mode="implicit backward Euler", precision="FP32 GMRES(20) + FP64 refinement",
+                   tol="1e-10 relative", dt_ms=0.025, preconditioner="segment tridiagonal")
+    else:
+        cfg.update(mode="explicit", precision=workload.rsplit("-", 1)[1], dt="0.8 dT_crit")
+    cfg["l2"] = "inputs larger than L2 (129 MB)"
+    return cfg
+
+
+# ------------------------------------------------------------------ measurement helpers
+
+class ClockSampler:
+    """nvidia-smi clocks during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        if not self.proc or not self.path:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9 and f[1].replace(".", "").isdigit():
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(rows[0][2]),
+                "samples": len(rows), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes_explicit(probs, precision: str) -> float:
+    """Bytes per step that the explicit step must move (the per-compartment figures of the
+    design notes): V read+write, gates read+write, parent index, the per-compartment
+    coefficients dT/(c_m dX) and 1/(r_a dX), and the channel parameters that vary per
+    compartment (g_Na, g_K, G_L, E_Na, E_K, E_L, LS_Na, LS_K).  Passive compartments move
+    V, index, both coefficients and W dX, K dX."""
+    fb = 8 if precision == "fp64" else 4
+    n_hh = sum(int(p.struct.num_hh) for p in probs)
+    n = sum(p.num_elem for p in probs)
+    hh = 16 + 6 * fb + 4 + 2 * fb + 8 * fb
+    pas = 16 + 4 + 2 * fb + 2 * fb
+    return n_hh * hh + (n - n_hh) * pas
+
+
+# ------------------------------------------------------------------ our arm
+
+def run_ours(args, rank: int, world: int):
+    import torch
+    pkg = importlib.import_module("168861_gb300")
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    wl = args.workload
+    count = args.trees or (4096 if wl.startswith("batch") else 1)
+    precision = "fp64" if wl.endswith("fp64") else "mixed"
+    implicit = wl.startswith("batch-implicit")
+    K = args.steps or (40 if implicit else 2048)
+    W = max(3, args.warmup)
+
+    t_build = time.time()
+    if wl == "axon-explicit-fp64":
+        spec = pkg.model.straight_axon(dtf=0.8)
+        d = pkg.derive(spec)
+        dT = pkg.step_size(spec, d)
+        probs = [pkg.ProblemArrays.from_spec(spec, d, dT)]
+        runs = [(1, spec.num_steps(dT) - 1, spec.init_time, spec.end_input)]
+        n_elem = spec.n
+    else:
+        probs, runs, n_elem = build_batch_problems(wl, count, args.seed, rank, world)
+    t_build = time.time() - t_build
+    opts = dict(precision=precision)
+    if implicit:
+        opts.update(krylov="gmres", restart=20, tol=1e-10, tol_mode="rel", precond="segment")
+    mode = pkg._lib.NRT_IMPLICIT_BE if implicit else pkg._lib.NRT_EXPLICIT
+    # loop ranges long enough for warm-up + timed steps
+    runs = [(a, max(b, a + W + K + 1), c, d_) for a, b, c, d_ in runs]
+
+    # ---- end to end through the public API (host buffers in, host buffers out)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    b = pkg.Batch(probs, mode=mode, **opts)
+    b.set_runs(runs)
+    b.advance(K)
+    outs = [b.snapshot(i) for i in range(b.count)]
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    h2d = sum(sum(a.nbytes for a in p.arrays.values()) for p in probs)
+    d2h = sum(o.nbytes for o in outs)
+    b.close()
+    del outs
+
+    # ---- device-resident throughput
+    b = pkg.Batch(probs, mode=mode, **opts)
+    b.set_runs(runs)
+    stream = torch.cuda.ExternalStream(b.stream())
+    b.advance(W)
+    b.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        b.advance(K)
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    st = b.stats()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        tot = torch.tensor([float(n_elem)], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tot)
+        n_all = float(tot.item())
+    else:
+        n_all = float(n_elem)
+    value = n_all * K / (ms / 1e3)
+    e2e_value = n_all * K / e2e_s
+    alg = algorithmic_bytes_explicit(probs, precision) if not implicit else None
+    peak, peak_kind = measured_peaks()
+    roof = None
+    if alg is not None:
+        achieved = alg * K / (ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                "algorithmic_bytes_per_step": alg}
+    launches = K + math.ceil(K / 64) if not implicit else None
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": ms / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if precision == "fp64" else "f32+f64",
+        "data": "synthetic (seeded random trees)",
+        "config": workload_config(wl, count), "elements": n_all,
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d / K,
+                "d2h_bytes_per_step": d2h / K, "seconds": e2e_s},
+        "roofline": roof, "gpu_launches": launches, "clocks": clk.summary(),
+        "build_seconds": t_build,
+        "krylov_iters": int(st.krylov_iters) if implicit else None,
+    }
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline(wl, args.seed, count)
+        print(json.dumps(line), flush=True)
+    b.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------ CPU (reference) arm
+
+def _oracle_job(job):
+    """One oracle run in a worker process (spawned; no CUDA here)."""
+    wl, tseed, size, steps = job
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    model = importlib.import_module("168861_gb300.model")
+    if wl == "axon-explicit-fp64":
+        spec = model.straight_axon(dtf=0.8)
+    else:
+        spec = model.random_tree(seed=tseed, n_target=size)
+    orc = O.Oracle()
+    d = orc.derive(spec)
+    t0 = time.perf_counter()
+    if wl.startswith("batch-implicit"):
+        orc.implicit_run(spec, d, spec.dt_abs, 1, 1 + steps, linsolve=1)
+    else:
+        dT = O.spec_dT(spec, d.dT_crit) if wl == "axon-explicit-fp64" else 0.8 * d.dT_crit
+        orc.explicit_run(spec, d, dT, 1, 1 + steps)
+    return spec.n * steps, time.perf_counter() - t0
+
+
+def _sample_jobs(wl: str, seed: int, count: int, budget_s: float, cores: int):
+    if wl == "axon-explicit-fp64":
+        return [(wl, 0, 1002, 2000)] * cores, "1002-element axon, 2000 steps per process"
+    pop = tree_population(count, seed)
+    per = 2 if wl.startswith("batch-implicit") else 200
+    jobs = [(wl, s, n, per) for s, n in pop[: max(cores, 8)]]
+    return jobs, f"first {len(jobs)} trees of the workload, {per} steps each"
+
+
+def cpu_baseline(wl: str, seed: int, count: int, budget_s: float = 20.0):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    jobs, sample = _sample_jobs(wl, seed, count, budget_s, cores)
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_oracle_job, jobs)
+    wall = time.perf_counter() - t0
+    work = sum(r[0] for r in res)
+    return {"value": work / wall, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": sample, "seconds": wall}
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    wl = args.workload
+    count = args.trees or (4096 if wl.startswith("batch") else 1)
+    K = args.steps or 3
+    W = max(3, args.warmup)
+    vals = []
+    cb = None
+    for it in range(W + K):
+        cb = cpu_baseline(wl, args.seed, count)
+        if it >= W:
+            vals.append(cb["value"])
+    v = float(np.mean(vals))
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world,
+            "steps": K, "warmup": W, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random trees)",
+            "config": workload_config(wl, count), "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", args.gpus))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,222 @@
+/* neurite_gb300.h -- C ABI of the GB300-native Neurite solver hot path.
+ *
+ * This is the drop-in boundary for the reference's `Solver` objects (inc/solver.h:12-24):
+ * explicit forward Euler (src/solverEx-cpu.cpp, src/solverEx-gpu.cpp) and implicit
+ * backward Euler (src/solverIm-cpu.cpp, src/solverIm-gpu.cpp).  Plain pointers and
+ * sizes only; every function returns an nrt_status.  The C++ adapter classes with the
+ * reference's constructor signature live in neurite_gb300_solver.hpp.
+ *
+ * Units are the reference's: SI (V, m, s, A, S, F); HH rates use mV relative to rest
+ * and dt in ms internally, as src/coupling.cpp:25-48 and src/solverEx-cpu.cpp:96 do.
+ *
+ * Threading: a handle is not thread-safe; distinct handles are independent.  All work of
+ * a handle runs on its own CUDA stream on the device that was current (or named in
+ * nrt_options.device) when it was created.
+ */
+#ifndef NEURITE_GB300_H
+#define NEURITE_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference throws cudaException from throw() methods
+ * (inc/cudaException.h:81-191, inc/solverEx-gpu.h:83-85) or calls exit(0) on solver
+ * failure (src/solverIm-cpu.cpp:247-250); here every failure is a returned code. */
+typedef enum nrt_status {
+  NRT_OK = 0,
+  NRT_EINVAL = 1,         /* null pointer, bad size or option */
+  NRT_ETOPOLOGY = 2,      /* tree violates the numbering convention */
+  NRT_ENOMEM = 3,         /* device or host allocation failed */
+  NRT_ENOCONV = 4,        /* Krylov solve hit its iteration budget (state still advanced) */
+  NRT_EDEVICE = 5,        /* CUDA error; see nrt_last_error() */
+  NRT_EBUDGET = 6,        /* serving: request exceeds the HBM budget */
+  NRT_ESTATE = 7,         /* call out of order (e.g. unknown request id) */
+  NRT_ENOTREADY = 8       /* serving: result not finished yet */
+} nrt_status;
+
+typedef enum nrt_mode {
+  NRT_EXPLICIT = 0,       /* forward Euler, src/solverEx-cpu.cpp:90-168 */
+  NRT_IMPLICIT_BE = 1     /* backward Euler, src/solverIm-cpu.cpp:29-370 */
+} nrt_mode;
+
+typedef enum nrt_precision {
+  NRT_FP64 = 0,           /* plain double everywhere (the drop-in) */
+  NRT_MIXED = 1           /* FP32 gates/stencil/inner Krylov; FP64 V accumulator, outer
+                             residual and Krylov inner products */
+} nrt_precision;
+
+typedef enum nrt_krylov {
+  NRT_GMRES = 0,          /* restarted GMRES(m), classical Gram-Schmidt */
+  NRT_BICGSTAB = 1        /* unpreconditioned-form BiCGSTAB, src/solverIm-gpu.cpp:725-843 */
+} nrt_krylov;
+
+typedef enum nrt_precond {
+  NRT_PRECOND_NONE = 0,
+  NRT_PRECOND_JACOBI = 1,    /* diagonal scaling */
+  NRT_PRECOND_SEGMENT = 2    /* exact tridiagonal solve of every unbranched segment
+                                (block Jacobi with the branch-point couplings cut) */
+} nrt_precond;
+
+typedef enum nrt_tol_mode {
+  NRT_TOL_ABS = 0,        /* ||b - A x||_2 <= tol (the reference's test, RANGE_ERROR 1e-14) */
+  NRT_TOL_REL = 1         /* ||b - A x||_2 <= tol * ||b||_2 over the physical rows */
+} nrt_tol_mode;
+
+/* One tree, after the reference's parameter pipeline (src/init.cpp:235-298), i.e. what
+ * the reference solver constructors read from their `discretization` and
+ * `Hodgkin_Huxley` objects (src/solverEx-gpu.cpp:266-434, src/solverIm-gpu.cpp:514-672).
+ * Element arrays have num_elem entries, HH arrays num_hh entries.  Nothing is retained:
+ * nrt_create copies what it needs. */
+typedef struct nrt_problem {
+  int32_t num_elem;              /* numStepsX */
+  const int32_t *mother;         /* get_mother(); -1 for element 0 */
+  const int32_t *dr;             /* get_DR(); == itself for terminals */
+  const int32_t *dl;             /* get_DL(); 0 where not branching */
+  const int32_t *branching;      /* get_branching() (0/1) */
+  int32_t num_term;
+  const int32_t *terminals;      /* terminals[0] == 0 is the fictitious root */
+  const double *dx, *c_m, *r_a;  /* get_dX(), get_c_m(), get_r_a() */
+  const double *W, *K;           /* get_W(), get_K() (HH entries are recomputed) */
+  const double *input;           /* get_input_current() */
+  int32_t num_hh;
+  const int32_t *hh_elem;        /* HH_elements[i]->get_element(), ascending */
+  const double *m, *h, *n;       /* gates */
+  const double *g_Na, *g_K, *G_L;
+  const double *E_Na, *E_K, *E_L;
+  const double *ls_Na, *ls_K;    /* get_Left_Shift_Na/K() */
+  const double *rest;            /* get_rest_pot() */
+  const double *V0;              /* potential[0] (the reference's prevT); NULL -> rest */
+  const double *V1;              /* potential[1] (currT); NULL -> V0 */
+  double dT;                     /* time step, s */
+} nrt_problem;
+
+typedef struct nrt_options {
+  int32_t mode;                  /* nrt_mode */
+  int32_t precision;             /* nrt_precision */
+  int32_t krylov;                /* nrt_krylov */
+  int32_t precond;               /* nrt_precond */
+  int32_t restart;               /* GMRES restart length (<= 64) */
+  int32_t tol_mode;              /* nrt_tol_mode */
+  double tol;                    /* residual tolerance per step */
+  int32_t max_iter;              /* Krylov iterations per step; 0 -> num_elem */
+  int32_t device;                /* CUDA device ordinal; -1 -> current device */
+  int32_t use_graphs;            /* capture nrt_run time loops in CUDA graphs (default 1) */
+  int32_t reserved[7];
+} nrt_options;
+
+typedef struct nrt_stats {
+  int64_t steps;                 /* calculate() calls so far */
+  int64_t krylov_iters;          /* total Krylov iterations (implicit) */
+  int32_t last_iters;            /* iterations of the last step */
+  int32_t nonconverged_steps;    /* steps that hit max_iter */
+  double last_residual;          /* ||b - A x||_2 of the last step (FP64) */
+  int64_t device_bytes;          /* device memory held by the handle */
+} nrt_stats;
+
+typedef struct nrt_solver nrt_solver;
+
+/* Fills the defaults: explicit, FP64, GMRES(30), segment preconditioner, absolute
+ * tolerance 1e-14 (RANGE_ERROR, inc/configuration.h:16), max_iter 0, device -1. */
+int nrt_options_default(nrt_options *opt);
+
+/* Replaces `new SolverExGPU(...)` / `new SolverImGPU(...)`
+ * (src/solverEx-gpu.cpp:204-439, src/solverIm-gpu.cpp:381-682): validates the tree,
+ * copies every array to device-resident SoA buffers and returns a handle. */
+int nrt_create(const nrt_problem *p, const nrt_options *opt, nrt_solver **out);
+
+/* Solver::update(bool input_active), inc/solver.h:16; src/solverEx-gpu.cpp:443-476.
+ * Selects the stimulus for the next calculate(); the gating update itself is fused into
+ * calculate() (the reference's separate Update_HH launch), so an update() must precede
+ * every calculate(), as the reference's driver loop does (src/neurite.cpp:230-236). */
+int nrt_update(nrt_solver *s, int input_active);
+
+/* Solver::calculate(), inc/solver.h:18; src/solverEx-gpu.cpp:481-530 and
+ * src/solverIm-gpu.cpp:725-843: advances V (and the gates) by one step. */
+int nrt_calculate(nrt_solver *s);
+
+/* Solver::snapshot(TYPE *potential), inc/solver.h:21; src/solverEx-gpu.cpp:534-541:
+ * copies the latest potential (num_elem doubles) to host memory; synchronous. */
+int nrt_snapshot(nrt_solver *s, double *potential);
+
+/* The driver loop of src/neurite.cpp:224-236 on the device: for i in [i_begin, i_end):
+ * t = i*dT; update(init_time <= t <= end_input); calculate().  Runs as CUDA-graph
+ * replays when use_graphs is set.  Asynchronous on the handle's stream. */
+int nrt_run(nrt_solver *s, int64_t i_begin, int64_t i_end, double init_time, double end_input);
+
+/* Waits for the handle's stream. */
+int nrt_synchronize(nrt_solver *s);
+
+/* The handle's CUDA stream (a cudaStream_t), e.g. to record timing events on it. */
+int nrt_get_stream(nrt_solver *s, void **stream);
+
+/* Device pointer of the latest potential (valid until the next calculate/run). */
+int nrt_potential_device(nrt_solver *s, const double **dev_ptr);
+
+/* Exports the gate state (num_hh each, HH order) to host memory; synchronous.  The
+ * reference has no such export (snapshot copies V only). */
+int nrt_get_gates(nrt_solver *s, double *m, double *h, double *n);
+
+/* Exports the implicit system assembled for the next step in the reference's CSR layout
+ * (src/solverIm-cpu.cpp:29-183): row_ptr[num_elem+1], col/val[capacity >= 4*num_elem+2],
+ * rhs[num_elem] (rows the reference leaves untouched hold the stale second buffer).
+ * Runs the assembly phase for the given stimulus flag without advancing the state. */
+int nrt_export_system(nrt_solver *s, int input_active, int32_t *row_ptr, int32_t *col,
+                      double *val, double *rhs, int32_t *nnz_out);
+
+int nrt_get_stats(nrt_solver *s, nrt_stats *st);
+
+/* The reference's destructor (src/solverEx-gpu.cpp:546-582): frees everything. */
+int nrt_destroy(nrt_solver *s);
+
+/* Human-readable text for a status code, and the last error recorded on this thread. */
+const char *nrt_status_string(int status);
+const char *nrt_last_error(void);
+
+/* ----------------------------------------------------------------------------------
+ * Parameter pipeline on the host: the reference's src/init.cpp:320-333 (strain on dX),
+ * :235-254 (electrical_properties), :273-298 (hhIconds), :180-198
+ * (cable_init_constants), :138-174 (critical time step) for a tree description.
+ *   ispec [5][n]  int32: kind (1 HH / 0 cable), mother, DR, DL, branching
+ *   dspec [12][n] double: dX, diameter, epsilon, input_current, ro_a, ro_m, per_m,
+ *                         thickness, rest_pot, sigma_Na, sigma_K, sigma_L
+ * Outputs: eparam [6][n] (c_m, r_a, dX, W, K, critical dT), hh_elem [num_hh],
+ * hparam [12][num_hh] (m, h, n, g_Na, g_K, G_L, E_Na, E_K, E_L, LS_Na, LS_K, rest). */
+int nrt_derive(int32_t n, const int32_t *ispec, const double *dspec, int32_t myelin,
+               double e_max, double *eparam, int32_t *hh_elem, double *hparam,
+               int32_t *num_hh_out, double *dT_crit_out);
+
+/* ----------------------------------------------------------------------------------
+ * Batches: many independent trees of uneven size advanced together, one persistent
+ * block-per-instance launch per chunk of steps.  Each instance keeps its own dT,
+ * stimulus window and step counter.  No reference counterpart (the reference runs one
+ * tree per process, src/neurite.cpp:84-291). */
+typedef struct nrt_batch nrt_batch;
+
+typedef struct nrt_instance_run {
+  int64_t i_begin;               /* first loop index (the reference starts at 1) */
+  int64_t i_end;                 /* one past the last loop index (numStepsT - 1) */
+  double init_time, end_input;   /* stimulus window, s */
+} nrt_instance_run;
+
+int nrt_batch_create(const nrt_problem *problems, int32_t count, const nrt_options *opt,
+                     nrt_batch **out);
+/* Sets every instance's loop range and stimulus window. */
+int nrt_batch_set_runs(nrt_batch *b, const nrt_instance_run *runs);
+/* Advances every unfinished instance by up to `steps` loop iterations. */
+int nrt_batch_advance(nrt_batch *b, int64_t steps);
+int nrt_batch_synchronize(nrt_batch *b);
+int nrt_batch_get_stream(nrt_batch *b, void **stream);
+/* Latest potential of one instance (its num_elem doubles) to host memory. */
+int nrt_batch_snapshot(nrt_batch *b, int32_t instance, double *potential);
+/* Number of loop iterations still to run per instance (count entries). */
+int nrt_batch_remaining(nrt_batch *b, int64_t *remaining);
+int nrt_batch_get_stats(nrt_batch *b, nrt_stats *st);
+int nrt_batch_destroy(nrt_batch *b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NEURITE_GB300_H */

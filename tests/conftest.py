@@ -1,0 +1,68 @@
+import glob
+import importlib
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the sm_103a library)")
+
+
+def golden_names(mode=None):
+    names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    if mode is None:
+        return names
+    return [n for n in names if str(np.load(os.path.join(GOLDEN, n + ".npz"))["mode"]) == mode]
+
+
+def load_golden(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d = {k: z[k] for k in z.files}
+    model = importlib.import_module("168861_gb300.model")
+    d["spec"] = model.TreeSpec.from_arrays(d)
+    return d
+
+
+@pytest.fixture(scope="session")
+def pkg():
+    return importlib.import_module("168861_gb300")
+
+
+@pytest.fixture(scope="session")
+def model():
+    return importlib.import_module("168861_gb300.model")
+
+
+@pytest.fixture(scope="session")
+def orc():
+    import oracle
+    oracle.build()
+    return oracle.Oracle()
+
+
+@pytest.fixture(scope="session")
+def lib(pkg):
+    """The CUDA library (built on demand; host-only entry points work without a GPU)."""
+    build = importlib.import_module("168861_gb300.build")
+    if not os.path.exists(build.LIB):
+        build.build()
+    return pkg.load()
+
+
+@pytest.fixture(scope="session")
+def gpu(lib):
+    """Requires a visible CUDA device; the GPU tests have no fallback."""
+    import ctypes
+    cudart = ctypes.CDLL("libcudart.so", mode=ctypes.RTLD_GLOBAL) if False else None  # noqa: F841
+    import torch
+    if not torch.cuda.is_available():
+        pytest.fail("the -m gpu tests need a CUDA device")
+    return lib
