@@ -83,8 +83,9 @@ static int validate_problem(const nrt_problem *p, bool strict, std::string &why)
       if (m >= j) return (why = "a mother must precede its child", NRT_ETOPOLOGY);
       if (is_term[j]) {
         if (p->dr[j] != j) return (why = "a terminal must have DR == itself", NRT_ETOPOLOGY);
-        if (m != j - 1 && !(p->branching[m] && p->dl[m] == j))
-          return (why = "a terminal's mother must be the previous element", NRT_ETOPOLOGY);
+        // the reference's assembly turns the row after a terminal's mother into the
+        // identity row, so a terminal must directly follow its mother
+        if (m != j - 1) return (why = "a terminal's mother must be the previous element", NRT_ETOPOLOGY);
       } else {
         if (p->dr[j] != j + 1 || p->mother[j + 1] != j)
           return (why = "non-terminal elements need DR == j + 1 with mother j", NRT_ETOPOLOGY);
@@ -92,6 +93,8 @@ static int validate_problem(const nrt_problem *p, bool strict, std::string &why)
       if (p->branching[j]) {
         const int32_t l = p->dl[j];
         if (l <= j || p->mother[l] != j) return (why = "DL must be a later element whose mother is the branch point", NRT_ETOPOLOGY);
+        if (is_term[j + 1] || is_term[l])
+          return (why = "a branch point's children must not be terminals", NRT_ETOPOLOGY);
       } else if (p->dl[j] != 0) {
         return (why = "DL must be 0 off branch points", NRT_ETOPOLOGY);
       }
@@ -344,6 +347,7 @@ int Engine::fixup() {
 // Runs `steps` loop iterations from every instance's current base (device-side loop
 // indices), replaying a captured graph of kChunk steps where possible.
 int Engine::advance(int64_t steps) {
+  if (opt.mode == NRT_IMPLICIT_BE) return implicit_advance(*this, steps);
   int64_t left = steps;
   while (left > 0 && (steps_done == 0 && !host.invariant)) {  // exact first step
     TRY(step(0, -1));
@@ -475,9 +479,23 @@ int nrt_calculate(nrt_solver *s) {
   if (!s) return nrt::fail(NRT_EINVAL, "null solver");
   if (!s->have_update) return nrt::fail(NRT_ESTATE, "calculate() without a preceding update()");
   NRT_CUDA(cudaSetDevice(s->eng.device));
+  const int64_t before = s->eng.opt.mode == NRT_IMPLICIT_BE ? nrt::nonconverged_total(s->eng) : 0;
   int rc = s->eng.step(0, s->pending_input);
   s->have_update = false;
+  if (rc == NRT_OK && s->eng.opt.mode == NRT_IMPLICIT_BE) {
+    const int64_t after = nrt::nonconverged_total(s->eng);
+    if (after < 0) return NRT_EDEVICE;
+    if (after > before)
+      return nrt::fail(NRT_ENOCONV, "implicit step hit its Krylov iteration budget");
+  }
   return rc;
+}
+
+int nrt_export_system(nrt_solver *s, int input_active, int32_t *row_ptr, int32_t *col, double *val,
+                      double *rhs, int32_t *nnz_out) {
+  if (!s || !row_ptr || !col || !val || !rhs || !nnz_out) return nrt::fail(NRT_EINVAL, "null argument");
+  NRT_CUDA(cudaSetDevice(s->eng.device));
+  return nrt::export_system(s->eng, input_active, row_ptr, col, val, rhs, nnz_out);
 }
 
 int nrt_snapshot(nrt_solver *s, double *potential) {
@@ -504,14 +522,18 @@ int nrt_run(nrt_solver *s, int64_t i_begin, int64_t i_end, double init_time, dou
   in.t1 = end_input;
   e.host.inst[0] = in;
   NRT_CUDA(cudaMemcpyAsync(e.pv.inst, &e.host.inst[0], sizeof(in), cudaMemcpyHostToDevice, e.stream));
+  const bool implicit = e.opt.mode == NRT_IMPLICIT_BE;
+  const int64_t before = implicit ? nrt::nonconverged_total(e) : 0;
   int rc = e.advance(i_end - i_begin);
   if (rc) return rc;
+  if (implicit && nrt::nonconverged_total(e) > before)
+    rc = nrt::fail(NRT_ENOCONV, "an implicit step hit its Krylov iteration budget");
   // leave the drop-in path's device loop range open again
   e.host.inst[0].base = 0;
   e.host.inst[0].iend = INT64_MAX;
   NRT_CUDA(cudaMemcpyAsync(e.pv.inst, &e.host.inst[0], sizeof(in), cudaMemcpyHostToDevice, e.stream));
   NRT_CUDA(cudaStreamSynchronize(e.stream));
-  return NRT_OK;
+  return rc;
 }
 
 int nrt_synchronize(nrt_solver *s) {

@@ -167,7 +167,10 @@ __global__ void advance_base(InstDev *inst, int32_t ninst, int64_t steps) {
 
 int launch_explicit_step(const PackView &pv, int precision, bool general, int k, int force,
                          const double *Vin, double *Vout, cudaStream_t st) {
-  const int threads = 256;
+  // Small trees: spread the elements over as many SMs as possible (the FP64 pipe of one
+  // SM, not memory, bounds a small block); large packs: 256-thread blocks.
+  int threads = 256;
+  while (threads > 32 && pv.ntot < (int64_t)threads * 2 * 152) threads >>= 1;
   const unsigned blocks = (unsigned)((pv.ntot + threads - 1) / threads);
   if (precision == NRT_MIXED) {
     if (general)

@@ -47,4 +47,10 @@ struct Engine {
   ~Engine();
 };
 
+// implicit.cu
+int implicit_advance(Engine &e, int64_t steps);
+int export_system(Engine &e, int input_active, int32_t *row_ptr, int32_t *col, double *val,
+                  double *rhs, int32_t *nnz_out);
+int64_t nonconverged_total(Engine &e);
+
 }  // namespace nrt

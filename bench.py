@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--workload", choices=WORKLOADS, default=DEFAULT_WORKLOAD)
     ap.add_argument("--trees", type=int, default=0, help="override the tree count (probes only)")
     ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the CPU baseline leg (profiling runs)")
     return ap.parse_args()
 
 
@@ -280,7 +282,8 @@ def run_ours(args, rank: int, world: int):
         "krylov_iters": int(st.krylov_iters) if implicit else None,
     }
     if rank == 0:
-        line["cpu_baseline"] = cpu_baseline(wl, args.seed, count)
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(wl, args.seed, count)
         print(json.dumps(line), flush=True)
     b.close()
     if dist:
@@ -310,26 +313,37 @@ def _oracle_job(job):
     return spec.n * steps, time.perf_counter() - t0
 
 
-def _sample_jobs(wl: str, seed: int, count: int, budget_s: float, cores: int):
+def _sample_jobs(wl: str, seed: int, count: int, cores: int):
+    """About 10-20 s of CPU work spread over `cores` processes."""
     if wl == "axon-explicit-fp64":
-        return [(wl, 0, 1002, 2000)] * cores, "1002-element axon, 2000 steps per process"
+        return [(wl, 0, 1002, 12000)] * cores, "1002-element axon, 12000 steps per process"
     pop = tree_population(count, seed)
-    per = 2 if wl.startswith("batch-implicit") else 200
-    jobs = [(wl, s, n, per) for s, n in pop[: max(cores, 8)]]
+    per = 2 if wl.startswith("batch-implicit") else 600
+    jobs = [(wl, s, n, per) for s, n in pop[: 2 * cores]]
     return jobs, f"first {len(jobs)} trees of the workload, {per} steps each"
 
 
-def cpu_baseline(wl: str, seed: int, count: int, budget_s: float = 20.0):
+def _warm(_):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.Oracle()
+    importlib.import_module("168861_gb300.model")
+    return os.getpid()
+
+
+def cpu_baseline(wl: str, seed: int, count: int):
+    """The oracle port timed on the host cores (one process per core, spawned, warmed)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
     cores = os.cpu_count() or 1
-    jobs, sample = _sample_jobs(wl, seed, count, budget_s, cores)
+    jobs, sample = _sample_jobs(wl, seed, count, cores)
     ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
-        res = pool.map(_oracle_job, jobs)
-    wall = time.perf_counter() - t0
+        pool.map(_warm, range(cores))
+        t0 = time.perf_counter()
+        res = pool.map(_oracle_job, jobs, chunksize=1)
+        wall = time.perf_counter() - t0
     work = sum(r[0] for r in res)
     return {"value": work / wall, "unit": METRIC, "cores": cores, "kind": "port",
             "sample": sample, "seconds": wall}

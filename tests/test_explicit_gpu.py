@@ -58,7 +58,8 @@ def test_explicit_fp64_matches_reference(gpu, pkg, name):
     assert trace.shape == g["trace"].shape
     assert np.abs(trace - g["trace"]).max() < TOL_FP64
     m, h, n = s.gates()
-    assert np.abs(np.stack([m, h, n]) - g["final_gates"]).max() < 1e-9
+    if len(m):
+        assert np.abs(np.stack([m, h, n]) - g["final_gates"]).max() < 1e-9
     s.close()
 
 

@@ -1,0 +1,162 @@
+"""Implicit (backward Euler) path on the GPU.
+
+Plain FP64 is held to 1e-6 mV (1e-9 V) against the exact backward-Euler solution of the
+reference's own system (the oracle's tree solve of the restated createMatrix, which is
+pinned to the reference's src/solverIm-cpu.cpp through its FGMRES run at 1e-12 V); against
+the reference's FGMRES output directly, the bound is that solver's own error (1e-5 V, see
+test_oracle_golden.py).  Mixed precision is held to 0.1 mV.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-9
+TOL_MIXED = 1e-4
+
+
+def problem(pkg, g):
+    d = pkg.Derived(g["eparam"], g["hh_elem"], g["hparam"], float(g["dT_crit"]))
+    return pkg.ProblemArrays.from_spec(g["spec"], d, float(g["dT"]))
+
+
+def tight(**kw):
+    o = dict(tol=1e-13, tol_mode="rel", restart=30, precond="segment")
+    o.update(kw)
+    return o
+
+
+@pytest.mark.parametrize("name", golden_names("i"))
+@pytest.mark.parametrize("precond", ["segment", "jacobi"])
+def test_implicit_fp64_matches_exact_solution(gpu, pkg, orc, name, precond):
+    g = load_golden(name)
+    spec = g["spec"]
+    steps = int(g["numStepsT"]) - 2
+    s = pkg.SolverIm(problem(pkg, g), **tight(precond=precond))
+    s.run(1, 1 + steps, spec.init_time, spec.end_input)
+    V = s.snapshot()
+    d = orc.derive(spec)
+    Vo, _, _, _ = orc.implicit_run(spec, d, float(g["dT"]), 1, 1 + steps, linsolve=0)
+    assert np.abs(V - Vo).max() < TOL_FP64
+    # and the reference's own FGMRES output, within that solver's error
+    assert np.abs(V - g["final_V"]).max() < 1e-5
+    st = s.stats()
+    assert st.nonconverged_steps == 0 and st.krylov_iters > 0
+    s.close()
+
+
+def test_implicit_system_matches_reference_assembly(gpu, pkg, orc):
+    """nrt_export_system reproduces createMatrix (src/solverIm-cpu.cpp:29-183)."""
+    g = load_golden("im_ytree_d3")
+    spec = g["spec"]
+    s = pkg.SolverIm(problem(pkg, g), **tight())
+    rp, col, val, rhs = s.export_system(True)
+    d = orc.derive(spec)
+    # the oracle's W, K after the first update() (gates from V^n = rest)
+    W = d.eparam[3].copy()
+    K = d.eparam[4].copy()
+    hp = d.hparam.copy()
+    dt = float(g["dT"]) * 1000
+    V = spec.rest_pot.copy()
+    vna = (V[d.hh_elem] + hp[9] - hp[11]) / 1e-3
+    vk = (V[d.hh_elem] + hp[10] - hp[11]) / 1e-3
+    am = (2.5 - 0.1 * vna) / (np.exp(2.5 - 0.1 * vna) - 1); bm = 4 * np.exp(-vna / 18)
+    ah = 0.07 * np.exp(-vna / 20); bh = 1 / (np.exp(3 - 0.1 * vna) + 1)
+    an = (0.1 - 0.01 * vk) / (np.exp(1 - 0.1 * vk) - 1); bn = 0.125 * np.exp(-vk / 80)
+    m = hp[0] + dt * (am * (1 - hp[0]) - bm * hp[0])
+    h = hp[1] + dt * (ah * (1 - hp[1]) - bh * hp[1])
+    n = hp[2] + dt * (an * (1 - hp[2]) - bn * hp[2])
+    GNa = hp[3] * m ** 3 * h
+    GK = hp[4] * n ** 4
+    W[d.hh_elem] = -(GNa + GK + hp[5])
+    K[d.hh_elem] = GNa * hp[6] + GK * hp[7] + hp[5] * hp[8]
+    rp_o, col_o, val_o, rhs_o = orc.implicit_matrix(spec, d, W, K, spec.input_current,
+                                                    float(g["dT"]), V, rhs_in=V.copy())
+    np.testing.assert_array_equal(rp, rp_o)
+    np.testing.assert_array_equal(col, col_o)
+    np.testing.assert_allclose(val, val_o, rtol=1e-13, atol=0)
+    np.testing.assert_allclose(rhs, rhs_o, rtol=1e-13, atol=0)
+    s.close()
+
+
+def test_implicit_dropin_loop_equals_device_loop(gpu, pkg):
+    g = load_golden("im_axon300")
+    spec = g["spec"]
+    dT = float(g["dT"])
+    a = pkg.SolverIm(problem(pkg, g), **tight())
+    b = pkg.SolverIm(problem(pkg, g), **tight())
+    steps = 40
+    for i in range(1, 1 + steps):
+        t = i * dT
+        a.update(spec.init_time <= t <= spec.end_input)
+        a.calculate()
+    b.run(1, 1 + steps, spec.init_time, spec.end_input)
+    np.testing.assert_array_equal(a.snapshot(), b.snapshot())
+
+
+def test_implicit_large_tree_cooperative(gpu, pkg, orc, model):
+    """~6.5e4-element tree on the whole-GPU cooperative kernel vs the exact solution."""
+    spec = model.random_binary_tree(depth=8, seed=5, dt=2.5e-5, tspan=5e-3)
+    steps = 20
+    s = pkg.SolverIm(pkg.ProblemArrays.from_spec(spec, pkg.derive(spec)), **tight())
+    s.run(1, 1 + steps, spec.init_time, spec.end_input)
+    d = orc.derive(spec)
+    Vo, _, _, _ = orc.implicit_run(spec, d, spec.dt_abs, 1, 1 + steps, linsolve=0)
+    assert np.abs(s.snapshot() - Vo).max() < TOL_FP64
+
+
+def test_implicit_mixed_precision(gpu, pkg, orc):
+    g = load_golden("im_ytree_d3")
+    spec = g["spec"]
+    steps = int(g["numStepsT"]) - 2
+    s = pkg.SolverIm(problem(pkg, g), precision="mixed", restart=20, tol=1e-10, tol_mode="rel")
+    s.run(1, 1 + steps, spec.init_time, spec.end_input)
+    d = orc.derive(spec)
+    Vo, _, _, _ = orc.implicit_run(spec, d, float(g["dT"]), 1, 1 + steps, linsolve=0)
+    assert np.abs(s.snapshot() - Vo).max() < TOL_MIXED
+    assert s.stats().nonconverged_steps == 0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_implicit_batch_alone_equals_in_mix(gpu, pkg, orc, model, precision):
+    """Uneven trees in one persistent block-per-instance launch give what each gives alone."""
+    specs = [model.random_tree(seed=s, n_target=n, dt=2.5e-5, tspan=1e-3)
+             for s, n in [(1, 1500), (2, 6000), (3, 900), (4, 3000)]]
+    opts = tight() if precision == "fp64" else dict(precision="mixed", restart=20, tol=1e-10,
+                                                     tol_mode="rel")
+    probs = [pkg.ProblemArrays.from_spec(sp, pkg.derive(sp)) for sp in specs]
+    b = pkg.Batch(probs, mode=1, **opts)
+    steps = [25, 40, 10, 33]
+    b.set_runs([(1, 1 + k, sp.init_time, sp.end_input) for k, sp in zip(steps, specs)])
+    b.advance(max(steps))
+    assert (b.remaining() == 0).all()
+    tol = TOL_FP64 if precision == "fp64" else TOL_MIXED
+    for k, sp in enumerate(specs):
+        alone = pkg.SolverIm(pkg.ProblemArrays.from_spec(sp, pkg.derive(sp)), **opts)
+        alone.run(1, 1 + steps[k], sp.init_time, sp.end_input)
+        Va = alone.snapshot()
+        Vb = b.snapshot(k)
+        assert np.abs(Vb - Va).max() < tol
+        d = orc.derive(sp)
+        Vo, _, _, _ = orc.implicit_run(sp, d, sp.dt_abs, 1, 1 + steps[k], linsolve=0)
+        assert np.abs(Vb - Vo).max() < tol
+        alone.close()
+    b.close()
+
+
+def test_implicit_budget_exhaustion_reported(gpu, pkg):
+    """A Krylov budget of one iteration cannot reach 1e-13: calculate() reports
+    NRT_ENOCONV and the state still advances (the reference would exit(0))."""
+    g = load_golden("im_axon300")
+    s = pkg.SolverIm(problem(pkg, g), **tight(max_iter=1, precond="none"))
+    V0 = s.snapshot()
+    s.update(True)
+    with pytest.raises(pkg.NeuriteError) as e:
+        s.calculate()
+    assert e.value.status == 4
+    assert not np.array_equal(s.snapshot(), V0)
+    assert s.stats().nonconverged_steps == 1
