@@ -208,7 +208,8 @@ def run_ours(args, rank: int, world: int):
     t_build = time.time() - t_build
     opts = dict(precision=precision)
     if implicit:
-        opts.update(krylov="gmres", restart=20, tol=1e-10, tol_mode="rel", precond="segment")
+        opts.update(krylov="gmres", restart=20, tol=1e-10, tol_mode="rel", precond="segment",
+                    max_iter=1000)
     mode = pkg._lib.NRT_IMPLICIT_BE if implicit else pkg._lib.NRT_EXPLICIT
     # loop ranges long enough for warm-up + timed steps
     runs = [(a, max(b, a + W + K + 1), c, d_) for a, b, c, d_ in runs]
