@@ -262,7 +262,7 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   size_t bytes = 2 * al(8 * N) + al(sizeof(Topo) * N) + al(sizeof(InstDev) * count) +
                  al(8 * host.terms.size() + 8);
   if (mixed)
-    bytes += 5 * al(4 * N) + al(4 * 3 * N) + al(4 * (size_t)HP_ROWS * N);
+    bytes += 7 * al(4 * N) + al(4 * 3 * N) + al(4 * (size_t)HP_ROWS * N);
   else
     bytes += 5 * al(8 * N) + al(8 * 3 * N) + al(8 * (size_t)HP_ROWS * N);
   if (opt.mode == NRT_IMPLICIT_BE) bytes += implicit_bytes();
@@ -270,6 +270,13 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   cudaStream_t st = stream;
   TRY(upload(arena, V[0], host.V0.data(), N, st));
   TRY(upload(arena, V[1], host.V1.data(), N, st));
+  if (mixed && opt.mode == NRT_EXPLICIT) {
+    hostf.reserve(10);
+    hostf.emplace_back(host.V0.begin(), host.V0.end());
+    TRY(upload(arena, Vf[0], hostf.back().data(), N, st));
+    hostf.emplace_back(host.V1.begin(), host.V1.end());
+    TRY(upload(arena, Vf[1], hostf.back().data(), N, st));
+  }
   Topo *topo = nullptr;
   TRY(upload(arena, topo, host.topo.data(), N, st));
   InstDev *inst = nullptr;
@@ -327,9 +334,10 @@ int Engine::step(int k, int force) {
     TRY(implicit_step(k, force));
   } else {
     TRY(launch_explicit_step(pv, opt.precision, general || !host.fusable, k, force, V[cur],
-                             V[cur ^ 1], stream));
+                             V[cur ^ 1], Vf[cur], Vf[cur ^ 1], stream));
     if (general || !host.fusable)
-      TRY(launch_terminal_fixup(pv.topo, terms, (int64_t)host.terms.size(), V[cur ^ 1], stream));
+      TRY(launch_terminal_fixup(pv.topo, terms, (int64_t)host.terms.size(), V[cur ^ 1],
+                                Vf[cur ^ 1], stream));
   }
   cur ^= 1;
   steps_done++;
@@ -339,7 +347,7 @@ int Engine::step(int k, int force) {
 
 int Engine::fixup() {
   if (!terminals_dirty) return NRT_OK;
-  TRY(launch_terminal_fixup(pv.topo, terms, (int64_t)host.terms.size(), V[cur], stream));
+  TRY(launch_terminal_fixup(pv.topo, terms, (int64_t)host.terms.size(), V[cur], Vf[cur], stream));
   terminals_dirty = false;
   return NRT_OK;
 }
@@ -362,7 +370,8 @@ int Engine::advance(int64_t steps) {
       int rc = NRT_OK;
       for (int k = 0; k < kChunk && rc == NRT_OK; k++)
         rc = launch_explicit_step(pv, opt.precision, false, k, -1, V[(cur + k) & 1],
-                                  V[(cur + k + 1) & 1], stream);
+                                  V[(cur + k + 1) & 1], Vf[(cur + k) & 1], Vf[(cur + k + 1) & 1],
+                                  stream);
       if (rc == NRT_OK) rc = launch_advance_base(pv.inst, pv.ninst, kChunk, stream);
       cudaError_t e = cudaStreamEndCapture(stream, &g);
       if (rc != NRT_OK) return rc;
@@ -441,7 +450,7 @@ static int check_options(const nrt_options *o, std::string &why) {
   if (o->precision != NRT_FP64 && o->precision != NRT_MIXED) return (why = "bad precision", NRT_EINVAL);
   if (o->krylov != NRT_GMRES && o->krylov != NRT_BICGSTAB) return (why = "bad krylov", NRT_EINVAL);
   if (o->precond < NRT_PRECOND_NONE || o->precond > NRT_PRECOND_SEGMENT) return (why = "bad precond", NRT_EINVAL);
-  if (o->restart < 1 || o->restart > nrt::kMaxRestart) return (why = "restart must be in [1, 64]", NRT_EINVAL);
+  if (o->restart < 1 || o->restart > nrt::kMaxRestart) return (why = "restart must be in [1, 32]", NRT_EINVAL);
   if (!(o->tol > 0)) return (why = "tol must be > 0", NRT_EINVAL);
   if (o->max_iter < 0) return (why = "max_iter must be >= 0", NRT_EINVAL);
   return NRT_OK;

@@ -93,13 +93,18 @@ __global__ void __launch_bounds__(256) explicit_step_f64(PackView p, int k, int 
   Vout[j] = v + p.cdt[j] * acc;
 }
 
-// Mixed precision: gates, rates, conductances and currents in FP32; V stays FP64 and the
-// neighbour differences are formed in FP64 before rounding, so the accumulator keeps
-// full precision over long horizons.
+// Mixed precision: gates, rates, conductances and currents in FP32; the potential is
+// accumulated in FP64.  GB300's FP64 pipe runs at 1/61 of the FP32 rate, so the stencil
+// reads an FP32 shadow of V (Vf = (float)V, refreshed from the FP64 value every step):
+// neighbour differences carry an absolute error of ~4e-9 V, while the FP64 accumulator
+// V' = V + dt-scaled current keeps long horizons free of drift.  FP64-pipe work is one
+// conversion, one add and one conversion back per element.
 template <bool kGeneral>
 __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, int force,
                                                            const double *__restrict__ Vin,
-                                                           double *__restrict__ Vout) {
+                                                           double *__restrict__ Vout,
+                                                           const float *__restrict__ Fin,
+                                                           float *__restrict__ Fout) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= p.ntot) return;
   const Topo tj = p.topo[j];
@@ -107,22 +112,22 @@ __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, in
   const int64_t i = in.base + k;
   if (i >= in.iend) {
     Vout[j] = Vin[j];
+    Fout[j] = Fin[j];
     return;
   }
   const int64_t N = p.ntot;
   const float *hp = p.hpf;
   const bool term = (tj.flags & F_TERM) != 0;
   if (term && !(tj.flags & F_HH)) return;
-  const double v = Vin[(kGeneral || !term) ? j : ghost_source(tj, j)];
+  const int64_t self = (kGeneral || !term) ? j : ghost_source(tj, j);
+  const float vf = Fin[self];
   float wdx, kdx;
   if (tj.flags & F_HH) {
-    const double rest = (double)hp[HP_REST * N + j];
-    const float dvna = (float)((v + (double)hp[HP_LSNA * N + j]) - rest);
-    const float dvk = (float)((v + (double)hp[HP_LSK * N + j]) - rest);
-    GateStep32 g = hh_step32(dvna, dvk, p.gatef[j], p.gatef[N + j], p.gatef[2 * N + j],
-                             hp[HP_DTMS * N + j], hp[HP_GNA * N + j], hp[HP_GK * N + j],
-                             hp[HP_GL * N + j], hp[HP_ENA * N + j], hp[HP_EK * N + j],
-                             hp[HP_EL * N + j]);
+    const float dv = vf - hp[HP_REST * N + j];
+    GateStep32 g = hh_step32(dv + hp[HP_LSNA * N + j], dv + hp[HP_LSK * N + j], p.gatef[j],
+                             p.gatef[N + j], p.gatef[2 * N + j], hp[HP_DTMS * N + j],
+                             hp[HP_GNA * N + j], hp[HP_GK * N + j], hp[HP_GL * N + j],
+                             hp[HP_ENA * N + j], hp[HP_EK * N + j], hp[HP_EL * N + j]);
     p.gatef[j] = g.m;
     p.gatef[N + j] = g.h;
     p.gatef[2 * N + j] = g.n;
@@ -137,23 +142,25 @@ __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, in
   const bool active = input_on(in, i, force);
   float acc = 0.0f;
   if ((tj.flags & F_BRANCH) && (kGeneral || !(tj.flags & F_DL_TERM)))
-    acc = (float)(Vin[tj.dl] - v) * p.gaxf[tj.dl];
-  if (kGeneral || !(tj.flags & F_DR_TERM))
-    acc = fmaf((float)(Vin[tj.dr] - v), p.gaxf[tj.dr], acc);
-  if (kGeneral || !(tj.flags & F_MO_TERM))
-    acc = fmaf((float)(Vin[tj.mother] - v), p.gaxf[j], acc);
-  acc = fmaf(wdx, (float)v, acc) + kdx;
+    acc = (Fin[tj.dl] - vf) * p.gaxf[tj.dl];
+  if (kGeneral || !(tj.flags & F_DR_TERM)) acc = fmaf(Fin[tj.dr] - vf, p.gaxf[tj.dr], acc);
+  if (kGeneral || !(tj.flags & F_MO_TERM)) acc = fmaf(Fin[tj.mother] - vf, p.gaxf[j], acc);
+  acc = fmaf(wdx, vf, acc) + kdx;
   if (active) acc += p.inpf[j];
-  Vout[j] = v + (double)(p.cdtf[j] * acc);
+  const double vn = Vin[j] + (double)(p.cdtf[j] * acc);
+  Vout[j] = vn;
+  Fout[j] = (float)vn;
 }
 
 // V_t = V_source(t) for every terminal (src/solverEx-cpu.cpp:155-161).
 __global__ void terminal_fixup(const Topo *__restrict__ topo, const int64_t *__restrict__ terms,
-                               int64_t nterm, double *__restrict__ V) {
+                               int64_t nterm, double *__restrict__ V, float *__restrict__ Vf) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nterm) return;
   const int64_t t = terms[q];
-  V[t] = V[ghost_source(topo[t], t)];
+  const int64_t s = ghost_source(topo[t], t);
+  V[t] = V[s];
+  if (Vf) Vf[t] = Vf[s];
 }
 
 __global__ void advance_base(InstDev *inst, int32_t ninst, int64_t steps) {
@@ -166,7 +173,8 @@ __global__ void advance_base(InstDev *inst, int32_t ninst, int64_t steps) {
 }  // namespace
 
 int launch_explicit_step(const PackView &pv, int precision, bool general, int k, int force,
-                         const double *Vin, double *Vout, cudaStream_t st) {
+                         const double *Vin, double *Vout, const float *Fin, float *Fout,
+                         cudaStream_t st) {
   // Small trees: spread the elements over as many SMs as possible (the FP64 pipe of one
   // SM, not memory, bounds a small block); large packs: 256-thread blocks.
   int threads = 256;
@@ -174,9 +182,9 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
   const unsigned blocks = (unsigned)((pv.ntot + threads - 1) / threads);
   if (precision == NRT_MIXED) {
     if (general)
-      explicit_step_mixed<true><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout);
+      explicit_step_mixed<true><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout, Fin, Fout);
     else
-      explicit_step_mixed<false><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout);
+      explicit_step_mixed<false><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout, Fin, Fout);
   } else {
     if (general)
       explicit_step_f64<true><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout);
@@ -188,9 +196,9 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
 }
 
 int launch_terminal_fixup(const Topo *topo, const int64_t *terms, int64_t nterm, double *V,
-                          cudaStream_t st) {
+                          float *Vf, cudaStream_t st) {
   if (nterm <= 0) return NRT_OK;
-  terminal_fixup<<<(unsigned)((nterm + 255) / 256), 256, 0, st>>>(topo, terms, nterm, V);
+  terminal_fixup<<<(unsigned)((nterm + 255) / 256), 256, 0, st>>>(topo, terms, nterm, V, Vf);
   NRT_CUDA(cudaGetLastError());
   return NRT_OK;
 }

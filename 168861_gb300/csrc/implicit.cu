@@ -19,18 +19,22 @@
 // off-diagonals.  nrt_export_system expands it to the reference's CSR layout.
 //
 // Solver: right-preconditioned GMRES(m) (Saad), classical Gram-Schmidt, Givens
-// rotations; inner products and norms accumulate in FP64 in both precisions.  The
-// preconditioner is an exact tridiagonal (Thomas) solve of every unbranched segment
-// piece: the branch-point couplings are the only ones left to the Krylov iteration.
-// Each cycle starts from the true FP64 residual b - A x, so in mixed precision (FP32
-// basis, FP32 SpMV and preconditioner) every restart is one step of iterative
-// refinement.  The warm start is x0 = V^n.
+// rotations.  The preconditioner is an exact tridiagonal (Thomas) solve of every
+// unbranched segment piece (<= kMaxPiece rows): only the branch-point couplings are left
+// to the Krylov iteration.  Each cycle starts from the true FP64 residual b - A x, so in
+// mixed precision (FP32 basis, SpMV, orthogonalisation update and preconditioner) every
+// restart is one step of iterative refinement.  Inner products and norms: per-thread
+// partial sums in the basis precision over the thread's rows, then FP64 across threads
+// and CTAs in a fixed order (deterministic, identical in every CTA).  Warm start x0 = V^n.
+//
+// Memory-level parallelism: the SpMV is fused with all j+1 Gram-Schmidt products (one
+// pass over the rows, register accumulators), the update and the norm share a pass, and
+// the sequential Thomas sweeps run on tiles of rows staged in shared memory.
 //
 // Two launch shapes from one template:
 //  * kGrid  (one tree): a cooperative launch over the whole GPU; rows are split into
 //    contiguous per-CTA ranges aligned with segment pieces; grid-wide syncs separate the
-//    phases and every CTA reduces the per-CTA partial sums in the same fixed order, so
-//    all CTAs hold identical Krylov scalars.
+//    phases (two per Arnoldi step).
 //  * block  (batches): a persistent block-per-instance scheduler; each CTA takes the next
 //    instance (largest first) from an atomic queue and runs all of its steps with
 //    __syncthreads only.
@@ -47,9 +51,11 @@ namespace cg = cooperative_groups;
 
 namespace nrt {
 
-constexpr int kThreads = 512;
+constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kMaxPiece = 256;  // longest segment piece one thread eliminates
+constexpr int kMaxPiece = 256;                 // longest segment piece one sweep handles
+constexpr int kMaxDots = kMaxRestart + 1;
+constexpr int kTileBytes = 48 * 1024;          // shared-memory staging for the sweeps
 
 struct InstStat {
   int64_t iters;
@@ -64,8 +70,9 @@ struct ImView {
   int precond;
   int tol_mode;
   double tol;
-  int max_iter;      // per step per instance; <= 0 -> instance size
+  int max_iter;      // per step per instance; 0 -> instance size; < 0 -> assembly only
   int ninst;
+  int tile_rows;     // rows per shared-memory tile
   const double *cmdt;  // c_m dX / dT
   const double *g64;   // 1 / (r_a dX)
   const float *gf;
@@ -75,13 +82,14 @@ struct ImView {
   double *rhs;
   void *Wb, *Z, *yv, *pcd, *pcc;  // T-typed workspace
   const int2 *pieces;             // (first row, length) of every segment piece
+  const int *tiles;               // piece index where each tile starts (sentinel at end)
   const int *cta_row;             // kGrid: per-CTA row range [cta_row[c], cta_row[c+1])
-  const int *cta_piece;           // kGrid: per-CTA piece range
+  const int *cta_tile;            // kGrid: per-CTA tile range
   const int64_t *inst_row;        // per instance row range (ninst + 1)
-  const int *inst_piece;          // per instance piece range (ninst + 1)
+  const int *inst_tile;           // per instance tile range (ninst + 1)
   const int *order;               // batch: instance processing order
   int *queue;                     // batch: next index into order
-  double *partials;               // kGrid: 2 x gridDim x (kMaxRestart + 1)
+  double *partials;               // kGrid: 2 x gridDim x kMaxDots
   InstStat *stats;
 };
 
@@ -90,44 +98,94 @@ struct Work {
   T *Wb, *Z, *y, *pd, *pc;
 };
 
+struct Shared {
+  double *H, *cs, *sn, *g, *s, *y, *red, *warp;
+  void *coef;      // T[kMaxDots]: update / solution coefficients
+  int *flag;
+  void *tile;      // staging area
+};
+
+__host__ __device__ inline size_t shared_fixed_bytes(int m) {
+  return sizeof(double) * ((size_t)(m + 1) * m + 2 * m + 2 * (m + 1) + m + kMaxDots +
+                           kWarps * kMaxDots + kMaxDots) + 16;
+}
+
+__device__ Shared carve(double *base, int m) {
+  Shared S;
+  S.H = base;
+  S.cs = S.H + (m + 1) * m;
+  S.sn = S.cs + m;
+  S.g = S.sn + m;
+  S.s = S.g + (m + 1);
+  S.y = S.s + (m + 1);
+  S.red = S.y + m;
+  S.warp = S.red + kMaxDots;
+  S.coef = (void *)(S.warp + kWarps * kMaxDots);
+  S.flag = (int *)((double *)S.coef + kMaxDots);
+  S.tile = (void *)((char *)base + ((shared_fixed_bytes(m) + 127) & ~(size_t)127));
+  return S;
+}
+
 // ---------------------------------------------------------------- reductions
 
-// Per-CTA reduction of k values: each thread passes its contribution for value i through
-// `acc(i)`; warps shuffle-reduce, then warp partials are summed in fixed order.
-template <class F>
-__device__ void block_sums(int k, F acc, double *warp_part, double *out) {
+// Reduces the first k register accumulators of every thread over the CTA into out[0..k)
+// (FP64, fixed order: warp shuffle tree, then warps in index order).
+template <typename T>
+__device__ __forceinline__ void block_reduce(const T (&acc)[kMaxDots], int k, double *warp_part,
+                                             double *out) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int i = 0; i < k; i++) {
-    double v = acc(i);
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) warp_part[w * (kMaxRestart + 1) + i] = v;
+#pragma unroll
+  for (int i = 0; i < kMaxDots; i++) {
+    if (i < k) {
+      double v = (double)acc[i];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) warp_part[w * kMaxDots + i] = v;
+    }
   }
   __syncthreads();
   if (threadIdx.x < k) {
     double s = 0;
-    for (int q = 0; q < kWarps; q++) s += warp_part[q * (kMaxRestart + 1) + threadIdx.x];
+    for (int q = 0; q < kWarps; q++) s += warp_part[q * kMaxDots + threadIdx.x];
     out[threadIdx.x] = s;
   }
   __syncthreads();
 }
 
-// Grid-wide: per-CTA sums -> global partials -> grid sync -> every CTA sums all CTAs'
-// partials in the same order (32 lanes per value, fixed shuffle tree).
+// Grid-wide completion: per-CTA sums -> global partials -> grid sync -> every CTA sums
+// all CTAs' partials in the same order.
 __device__ void grid_finish(cg::grid_group &grid, int k, double *cta_sums, double *partials,
-                            int &parity, double *out) {
-  double *buf = partials + (size_t)parity * gridDim.x * (kMaxRestart + 1);
+                            int &parity) {
+  double *buf = partials + (size_t)parity * gridDim.x * kMaxDots;
   parity ^= 1;
-  if (threadIdx.x < k) buf[(size_t)blockIdx.x * (kMaxRestart + 1) + threadIdx.x] = cta_sums[threadIdx.x];
+  if (threadIdx.x < k) buf[(size_t)blockIdx.x * kMaxDots + threadIdx.x] = cta_sums[threadIdx.x];
+  __syncthreads();
   __threadfence();
   grid.sync();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int i = w; i < k; i += kWarps) {
     double v = 0;
-    for (int c = lane; c < (int)gridDim.x; c += 32) v += buf[(size_t)c * (kMaxRestart + 1) + i];
+    for (int c = lane; c < (int)gridDim.x; c += 32) v += buf[(size_t)c * kMaxDots + i];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) out[i] = v;
+    if (lane == 0) cta_sums[i] = v;
   }
   __syncthreads();
+}
+
+template <bool kGrid, typename T>
+__device__ __forceinline__ void group_reduce(cg::grid_group &grid, const T (&acc)[kMaxDots], int k,
+                                             Shared &S, double *partials, int &parity) {
+  block_reduce(acc, k, S.warp, S.red);
+  if (kGrid) grid_finish(grid, k, S.red, partials, parity);
+}
+
+template <bool kGrid>
+__device__ __forceinline__ void group_sync(cg::grid_group &grid) {
+  if (kGrid) {
+    __threadfence();
+    grid.sync();
+  } else {
+    __syncthreads();
+  }
 }
 
 // ---------------------------------------------------------------- kernel body
@@ -138,12 +196,10 @@ struct Ctx {
   ImView iv;
   Work<T> w;
   int64_t r0, r1;   // rows of this CTA (kGrid) or instance (batch)
-  int p0, p1;       // pieces
-  int inst;
-  int64_t ninst_rows;
+  int t0, t1;       // tiles
 };
 
-// A x over rows [r0, r1) for the physical rows; identity rows yield 0.  FP64 form.
+// (A x)_j for a physical row, FP64 (identity rows yield 0).
 __device__ __forceinline__ double row_apply64(const PackView &pv, const ImView &iv, int64_t j,
                                               const double *x) {
   const Topo t = pv.topo[j];
@@ -176,111 +232,112 @@ __device__ __forceinline__ float row_apply<float>(const PackView &pv, const ImVi
   return s;
 }
 
-// Thomas factorisation of every piece of this CTA: pd = pivots^-1, pc = c'.
-template <typename T, bool kGrid>
-__device__ void factor_pieces(Ctx<T, kGrid> &c) {
-  for (int q = c.p0 + threadIdx.x; q < c.p1; q += blockDim.x) {
-    const int2 pc = c.iv.pieces[q];
-    double cprev = 0;
-    for (int k = 0; k < pc.y; k++) {
-      const int64_t j = pc.x + k;
-      const double a = k ? -c.iv.g64[j] : 0.0;                  // sub-diagonal (j, j-1)
-      const bool last = k + 1 == pc.y;
-      const double cc = last ? 0.0 : -c.iv.g64[j + 1];           // super-diagonal (j, j+1)
-      double piv = c.iv.diag[j] - a * cprev;
-      double d = 1.0 / piv;
-      cprev = cc * d;
-      c.w.pd[j] = (T)d;
-      c.w.pc[j] = (T)cprev;
-    }
-  }
+// Rows covered by tile q: from its first piece's start to its last piece's end.
+__device__ __forceinline__ void tile_rows(const ImView &iv, int q, int64_t &a, int64_t &b) {
+  const int pa = iv.tiles[q], pb = iv.tiles[q + 1];
+  a = iv.pieces[pa].x;
+  const int2 last = iv.pieces[pb - 1];
+  b = (int64_t)last.x + last.y;
 }
 
-// z = M^-1 v over this CTA's pieces (identity rows hold 0 in both).
+// Thomas factorisation of every piece (once per step): pd = 1/pivot, pc = c'.
+// Staged through shared memory tile by tile; one thread per piece.
 template <typename T, bool kGrid>
-__device__ void apply_precond(Ctx<T, kGrid> &c, const T *v, T *z) {
-  if (c.iv.precond == NRT_PRECOND_SEGMENT) {
-    for (int q = c.p0 + threadIdx.x; q < c.p1; q += blockDim.x) {
-      const int2 pc = c.iv.pieces[q];
-      T yprev = 0;
-      for (int k = 0; k < pc.y; k++) {  // forward: y_k = (v_k - a_k y_{k-1}) d_k
-        const int64_t j = pc.x + k;
-        const T a = k ? (T)(-c.iv.g64[j]) : (T)0;
-        yprev = (v[j] - a * yprev) * c.w.pd[j];
-        z[j] = yprev;
-      }
-      T znext = z[pc.x + pc.y - 1];
-      for (int k = pc.y - 2; k >= 0; k--) {  // backward: z_k = y_k - c'_k z_{k+1}
-        const int64_t j = pc.x + k;
-        znext = z[j] - c.w.pc[j] * znext;
-        z[j] = znext;
+__device__ void factor_pieces(Ctx<T, kGrid> &c, Shared &S) {
+  T *sd = (T *)S.tile;                          // diag, then pivots^-1
+  T *sg = sd + c.iv.tile_rows;                  // conductance to the mother
+  T *sc = sg + c.iv.tile_rows;                  // c'
+  for (int q = c.t0; q < c.t1; q++) {
+    int64_t a, b;
+    tile_rows(c.iv, q, a, b);
+    for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
+      sd[r - a] = (T)c.iv.diag[r];
+      sg[r - a] = (T)c.iv.g64[r];
+    }
+    __syncthreads();
+    for (int p = c.iv.tiles[q] + threadIdx.x; p < c.iv.tiles[q + 1]; p += blockDim.x) {
+      const int2 pc = c.iv.pieces[p];
+      const int o = (int)(pc.x - a);
+      double cprev = 0;
+      for (int k = 0; k < pc.y; k++) {
+        const double sub = k ? -(double)sg[o + k] : 0.0;                  // (j, j-1)
+        const double sup = k + 1 < pc.y ? -(double)sg[o + k + 1] : 0.0;   // (j, j+1)
+        const double d = 1.0 / ((double)sd[o + k] - sub * cprev);
+        cprev = sup * d;
+        sd[o + k] = (T)d;
+        sc[o + k] = (T)cprev;
       }
     }
-  } else {
-    for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x) {
-      const uint32_t f = c.pv.topo[j].flags;
-      if (f & F_IDENT) { z[j] = 0; continue; }
-      z[j] = c.iv.precond == NRT_PRECOND_JACOBI ? (T)(v[j] / c.iv.diag[j]) : v[j];
+    __syncthreads();
+    for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
+      c.w.pd[r] = sd[r - a];
+      c.w.pc[r] = sc[r - a];
     }
-  }
-}
-
-template <bool kGrid>
-__device__ __forceinline__ void group_sync(cg::grid_group &grid) {
-  if (kGrid) {
-    __threadfence();
-    grid.sync();
-  } else {
     __syncthreads();
   }
 }
 
-// Sums k values over the group (CTA or grid) into out[0..k).
-template <bool kGrid, class F>
-__device__ void group_sums(cg::grid_group &grid, int k, F acc, double *warp_part, double *cta,
-                           double *partials, int &parity, double *out) {
-  if (kGrid) {
-    block_sums(k, acc, warp_part, cta);
-    grid_finish(grid, k, cta, partials, parity, out);
+// z = M^-1 v over this CTA's rows (identity rows: v and z are 0).
+template <typename T, bool kGrid>
+__device__ void apply_precond(Ctx<T, kGrid> &c, Shared &S, const T *v, T *z) {
+  if (c.iv.precond == NRT_PRECOND_SEGMENT) {
+    T *sv = (T *)S.tile;
+    T *sd = sv + c.iv.tile_rows;
+    T *sc = sd + c.iv.tile_rows;
+    T *sg = sc + c.iv.tile_rows;
+    for (int q = c.t0; q < c.t1; q++) {
+      int64_t a, b;
+      tile_rows(c.iv, q, a, b);
+      for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
+        sv[r - a] = v[r];
+        sd[r - a] = c.w.pd[r];
+        sc[r - a] = c.w.pc[r];
+        sg[r - a] = (T)c.iv.g64[r];
+      }
+      __syncthreads();
+      for (int p = c.iv.tiles[q] + threadIdx.x; p < c.iv.tiles[q + 1]; p += blockDim.x) {
+        const int2 pc = c.iv.pieces[p];
+        const int o = (int)(pc.x - a);
+        T y = sv[o] * sd[o];
+        sv[o] = y;
+        for (int k = 1; k < pc.y; k++) {  // forward: y_k = (v_k + g_k y_{k-1}) d_k
+          y = (sv[o + k] + sg[o + k] * y) * sd[o + k];
+          sv[o + k] = y;
+        }
+        for (int k = pc.y - 2; k >= 0; k--) {  // backward: z_k = y_k - c'_k z_{k+1}
+          y = sv[o + k] - sc[o + k] * y;
+          sv[o + k] = y;
+        }
+      }
+      __syncthreads();
+      for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) z[r] = sv[r - a];
+      __syncthreads();
+    }
   } else {
-    block_sums(k, acc, warp_part, out);
+    for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x) {
+      const uint32_t f = c.pv.topo[j].flags;
+      if (f & F_IDENT) {
+        z[j] = 0;
+        continue;
+      }
+      z[j] = c.iv.precond == NRT_PRECOND_JACOBI ? (T)((double)v[j] / c.iv.diag[j]) : v[j];
+    }
+    __syncthreads();
   }
 }
 
-struct Shared {
-  double *H, *cs, *sn, *g, *s, *y, *red, *cta, *warp;
-  int *flag;
-};
-
-__device__ Shared carve(double *base, int m) {
-  Shared S;
-  S.H = base;
-  S.cs = S.H + (m + 1) * m;
-  S.sn = S.cs + m;
-  S.g = S.sn + m;
-  S.s = S.g + (m + 1);
-  S.y = S.s + (m + 1);
-  S.red = S.y + m;
-  S.cta = S.red + (kMaxRestart + 2);
-  S.warp = S.cta + (kMaxRestart + 2);
-  S.flag = (int *)(S.warp + kWarps * (kMaxRestart + 1));
-  return S;
-}
-
-size_t shared_bytes(int m) {
-  return sizeof(double) * ((size_t)(m + 1) * m + 2 * m + 2 * (m + 1) + m + 2 * (kMaxRestart + 2) +
-                           kWarps * (kMaxRestart + 1)) + 16;
-}
-
-// One backward-Euler step of one group (CTA or grid) for instance c.inst.
+// One backward-Euler step of one group (CTA or grid) for instance `inst`.
 template <typename T, bool kGrid>
 __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared &S, int &parity,
-                                  const double *Vin, double *Vout, bool active, int64_t inst_n) {
+                                  const double *Vin, double *Vout, bool active, int64_t inst_n,
+                                  int inst) {
   const PackView &pv = c.pv;
   const ImView &iv = c.iv;
   const int64_t N = pv.ntot;
   const int m = iv.m;
+  T *coef = (T *)S.coef;
   // ---- assembly: gates (from V^n), W, K, diagonal, right-hand side, x0 = V^n
+  double bacc = 0;
   for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x) {
     const Topo t = pv.topo[j];
     const double v = Vin[j];
@@ -288,9 +345,8 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
     if (t.flags & F_HH) {
       if (pv.hpf) {
         const float *hp = pv.hpf;
-        const double rest = (double)hp[HP_REST * N + j];
-        GateStep32 g = hh_step32((float)((v + (double)hp[HP_LSNA * N + j]) - rest),
-                                 (float)((v + (double)hp[HP_LSK * N + j]) - rest), pv.gatef[j],
+        const float dv = (float)(v - (double)hp[HP_REST * N + j]);
+        GateStep32 g = hh_step32(dv + hp[HP_LSNA * N + j], dv + hp[HP_LSK * N + j], pv.gatef[j],
                                  pv.gatef[N + j], pv.gatef[2 * N + j], hp[HP_DTMS * N + j],
                                  hp[HP_GNA * N + j], hp[HP_GK * N + j], hp[HP_GL * N + j],
                                  hp[HP_ENA * N + j], hp[HP_EK * N + j], hp[HP_EL * N + j]);
@@ -331,24 +387,19 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
     double b = iv.cmdt[j] * v + kdx;
     if (active) b += iv.inp64[j];
     iv.rhs[j] = b;
+    bacc += b * b;
     Vout[j] = v;
   }
   __syncthreads();
-  if (iv.precond == NRT_PRECOND_SEGMENT) factor_pieces(c);
-  // ||b|| over physical rows (relative tolerance)
+  if (iv.precond == NRT_PRECOND_SEGMENT) factor_pieces(c, S);
   double target = iv.tol;
-  if (iv.tol_mode == NRT_TOL_REL) {
-    group_sums<kGrid>(grid, 1, [&](int) {
-      double a = 0;
-      for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x)
-        if (!(pv.topo[j].flags & F_IDENT)) a += iv.rhs[j] * iv.rhs[j];
-      return a;
-    }, S.warp, S.cta, iv.partials, parity, S.red);
-    target = iv.tol * sqrt(S.red[0]);
-  } else {
-    group_sync<kGrid>(grid);  // x0 of every row visible before the first residual
+  {
+    double acc[kMaxDots];
+    acc[0] = bacc;
+    group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);  // also publishes x0
+    if (iv.tol_mode == NRT_TOL_REL) target = iv.tol * sqrt(S.red[0]);
+    if (!kGrid) __syncthreads();
   }
-  // max_iter < 0 is the assembly-only pass of nrt_export_system
   const int budget = iv.max_iter > 0 ? iv.max_iter : (iv.max_iter < 0 ? 0 : (int)inst_n);
   const double inner_rel = sizeof(T) == 4 ? 1e-5 : 0.0;
   int iters = 0;
@@ -356,24 +407,28 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
   bool converged = false;
   for (;;) {
     // ---- cycle start: true residual r = b - A x in FP64, W_0 = r, Z_0 = M^-1 r
-    group_sums<kGrid>(grid, 1, [&](int) {
-      double a = 0;
+    {
+      double acc[kMaxDots];
+      acc[0] = 0;
       for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x) {
-        if (pv.topo[j].flags & F_IDENT) { c.w.Wb[j] = 0; continue; }
+        if (pv.topo[j].flags & F_IDENT) {
+          c.w.Wb[j] = 0;
+          continue;
+        }
         const double r = iv.rhs[j] - row_apply64(pv, iv, j, Vout);
         c.w.Wb[j] = (T)r;
-        a += r * r;
+        acc[0] += r * r;
       }
-      return a;
-    }, S.warp, S.cta, iv.partials, parity, S.red);
+      __syncthreads();
+      if (res >= 0 && iters < budget) apply_precond(c, S, c.w.Wb, c.w.Z);  // local rows
+      group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);         // publishes Z_0
+    }
     res = sqrt(S.red[0]);
     if (res <= target) {
       converged = true;
       break;
     }
     if (iters >= budget) break;
-    apply_precond(c, c.w.Wb, c.w.Z);
-    group_sync<kGrid>(grid);  // Z_0 visible to neighbours
     if (threadIdx.x == 0) {
       S.g[0] = res;
       for (int i = 1; i <= m; i++) S.g[i] = 0;
@@ -385,36 +440,39 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
     for (int j = 0; j < m; j++) {
       const T *Zj = c.w.Z + (size_t)j * N;
       const T sj = (T)S.s[j];
-      // y = s_j A Z_j; p_i = <y, W_i>, i <= j
-      for (int64_t r = c.r0 + threadIdx.x; r < c.r1; r += blockDim.x)
-        c.w.y[r] = sj * row_apply<T>(pv, iv, r, Zj);
-      group_sums<kGrid>(grid, j + 1, [&](int i) {
-        const T *Wi = c.w.Wb + (size_t)i * N;
-        double a = 0;
-        for (int64_t r = c.r0 + threadIdx.x; r < c.r1; r += blockDim.x)
-          a += (double)c.w.y[r] * (double)Wi[r];
-        return a;
-      }, S.warp, S.cta, iv.partials, parity, S.red);
-      if (threadIdx.x <= j) S.H[threadIdx.x * m + j] = S.s[threadIdx.x] * S.red[threadIdx.x];
-      __syncthreads();
-      // w = y - sum_i h_ij s_i W_i -> W_{j+1}; ||w||; Z_{j+1} = M^-1 w
-      T *Wn = c.w.Wb + (size_t)(j + 1) * N;
+      // y = s_j A Z_j fused with p_i = <y, W_i>, i <= j
+      T acc[kMaxDots];
+#pragma unroll
+      for (int i = 0; i < kMaxDots; i++) acc[i] = 0;
       for (int64_t r = c.r0 + threadIdx.x; r < c.r1; r += blockDim.x) {
-        double a = (double)c.w.y[r];
-        for (int i = 0; i <= j; i++)
-          a -= S.H[i * m + j] * S.s[i] * (double)c.w.Wb[(size_t)i * N + r];
-        Wn[r] = (T)a;
+        const T y = sj * row_apply<T>(pv, iv, r, Zj);
+        c.w.y[r] = y;
+#pragma unroll
+        for (int i = 0; i < kMaxDots; i++)
+          if (i <= j) acc[i] += y * c.w.Wb[(size_t)i * N + r];
+      }
+      group_reduce<kGrid>(grid, acc, j + 1, S, iv.partials, parity);
+      if (threadIdx.x <= j) {
+        const double h = S.s[threadIdx.x] * S.red[threadIdx.x];
+        S.H[threadIdx.x * m + j] = h;
+        coef[threadIdx.x] = (T)(h * S.s[threadIdx.x]);
       }
       __syncthreads();
-      apply_precond(c, Wn, c.w.Z + (size_t)(j + 1) * N);
-      group_sums<kGrid>(grid, 1, [&](int) {
-        double a = 0;
-        for (int64_t r = c.r0 + threadIdx.x; r < c.r1; r += blockDim.x) {
-          const double v = (double)Wn[r];
-          a += v * v;
-        }
-        return a;
-      }, S.warp, S.cta, iv.partials, parity, S.red);
+      // w = y - sum_i h_ij s_i W_i -> W_{j+1}; ||w||^2; then Z_{j+1} = M^-1 w
+      T *Wn = c.w.Wb + (size_t)(j + 1) * N;
+      T nacc[kMaxDots];
+      nacc[0] = 0;
+      for (int64_t r = c.r0 + threadIdx.x; r < c.r1; r += blockDim.x) {
+        T a = c.w.y[r];
+#pragma unroll
+        for (int i = 0; i < kMaxDots; i++)
+          if (i <= j) a -= coef[i] * c.w.Wb[(size_t)i * N + r];
+        Wn[r] = a;
+        nacc[0] += a * a;
+      }
+      __syncthreads();
+      apply_precond(c, S, Wn, c.w.Z + (size_t)(j + 1) * N);
+      group_reduce<kGrid>(grid, nacc, 1, S, iv.partials, parity);  // publishes Z_{j+1}
       if (threadIdx.x == 0) {
         const double hn = sqrt(S.red[0]);
         S.s[j + 1] = hn > 0 ? 1.0 / hn : 0.0;
@@ -444,19 +502,21 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
         for (int l = i + 1; l < k; l++) a -= S.H[i * m + l] * S.y[l];
         S.y[i] = a / S.H[i * m + i];
       }
-      for (int i = 0; i < k; i++) S.y[i] *= S.s[i];
+      for (int i = 0; i < k; i++) coef[i] = (T)(S.y[i] * S.s[i]);
     }
     __syncthreads();
     for (int64_t r = c.r0 + threadIdx.x; r < c.r1; r += blockDim.x) {
       if (pv.topo[r].flags & F_IDENT) continue;
-      double a = Vout[r];
-      for (int i = 0; i < k; i++) a += S.y[i] * (double)c.w.Z[(size_t)i * N + r];
-      Vout[r] = a;
+      T a = 0;
+#pragma unroll
+      for (int i = 0; i < kMaxDots; i++)
+        if (i < k) a += coef[i] * c.w.Z[(size_t)i * N + r];
+      Vout[r] += (double)a;
     }
     group_sync<kGrid>(grid);
   }
   if (threadIdx.x == 0 && (!kGrid || blockIdx.x == 0)) {
-    InstStat &st = iv.stats[c.inst];
+    InstStat &st = iv.stats[inst];
     st.iters += iters;
     st.last_iters = iters;
     st.last_res = res;
@@ -469,7 +529,7 @@ template <typename T, bool kGrid>
 __global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView iv, int nsteps,
                                                            int force, double *V0, double *V1,
                                                            int cur) {
-  extern __shared__ double smem[];
+  extern __shared__ __align__(16) double smem[];
   Shared S = carve(smem, iv.m);
   cg::grid_group grid = cg::this_grid();
   int parity = 0;
@@ -481,13 +541,11 @@ __global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView i
   c.w.y = (T *)iv.yv;
   c.w.pd = (T *)iv.pcd;
   c.w.pc = (T *)iv.pcc;
-  double *V[2] = {V0, V1};
   if (kGrid) {
-    c.inst = 0;
     c.r0 = iv.cta_row[blockIdx.x];
     c.r1 = iv.cta_row[blockIdx.x + 1];
-    c.p0 = iv.cta_piece[blockIdx.x];
-    c.p1 = iv.cta_piece[blockIdx.x + 1];
+    c.t0 = iv.cta_tile[blockIdx.x];
+    c.t1 = iv.cta_tile[blockIdx.x + 1];
     const InstDev in = pv.inst[0];
     const int64_t inst_n = iv.inst_row[1] - iv.inst_row[0];
     for (int s = 0; s < nsteps; s++) {
@@ -495,8 +553,8 @@ __global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView i
       if (i >= in.iend) break;
       const bool active = force >= 0 ? force != 0
                                      : ((double)i * in.dT >= in.t0 && (double)i * in.dT <= in.t1);
-      implicit_one_step<T, kGrid>(c, grid, S, parity, V[(cur + s) & 1], V[(cur + s + 1) & 1], active,
-                                  inst_n);
+      implicit_one_step<T, kGrid>(c, grid, S, parity, ((cur + s) & 1) ? V1 : V0,
+                                  ((cur + s + 1) & 1) ? V1 : V0, active, inst_n, 0);
     }
   } else {
     for (;;) {
@@ -506,11 +564,10 @@ __global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView i
       __syncthreads();
       if (q >= iv.ninst) break;
       const int inst = iv.order[q];
-      c.inst = inst;
       c.r0 = iv.inst_row[inst];
       c.r1 = iv.inst_row[inst + 1];
-      c.p0 = iv.inst_piece[inst];
-      c.p1 = iv.inst_piece[inst + 1];
+      c.t0 = iv.inst_tile[inst];
+      c.t1 = iv.inst_tile[inst + 1];
       const InstDev in = pv.inst[inst];
       int s = 0;
       for (; s < nsteps; s++) {
@@ -518,12 +575,13 @@ __global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView i
         if (i >= in.iend) break;
         const bool active = force >= 0 ? force != 0
                                        : ((double)i * in.dT >= in.t0 && (double)i * in.dT <= in.t1);
-        implicit_one_step<T, kGrid>(c, grid, S, parity, V[(cur + s) & 1], V[(cur + s + 1) & 1],
-                                    active, c.r1 - c.r0);
+        implicit_one_step<T, kGrid>(c, grid, S, parity, ((cur + s) & 1) ? V1 : V0,
+                                    ((cur + s + 1) & 1) ? V1 : V0, active, c.r1 - c.r0, inst);
       }
       if ((nsteps - s) & 1) {  // finished early: put its latest V where the others' is
-        for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x)
-          V[(cur + nsteps) & 1][j] = V[(cur + s) & 1][j];
+        double *dst = ((cur + nsteps) & 1) ? V1 : V0;
+        const double *src = ((cur + s) & 1) ? V1 : V0;
+        for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x) dst[j] = src[j];
       }
       __syncthreads();
     }
@@ -535,12 +593,14 @@ __global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView i
 struct ImplicitState {
   ImView iv{};
   std::vector<int2> pieces;
-  std::vector<int> cta_row, cta_piece, inst_piece, order;
+  std::vector<int> tiles, cta_row, cta_tile, inst_tile, order;
   std::vector<int64_t> inst_row;
   int grid_blocks = 0;
   bool grid_mode = false;
-  std::vector<InstStat> last_stats;
+  size_t smem = 0;
 };
+
+static size_t smem_bytes(int m) { return ((shared_fixed_bytes(m) + 127) & ~(size_t)127) + kTileBytes; }
 
 size_t Engine::implicit_bytes() const {
   const int64_t N = host.ntot;
@@ -548,12 +608,12 @@ size_t Engine::implicit_bytes() const {
   const int m = opt.restart;
   size_t b = 0;
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  b += 6 * al(8 * N);                              // cmdt, g64, wdx64, kdx64, inp64, diag
-  b += al(8 * N) + al(4 * N) + al(4 * N);          // rhs, diagf, gf
-  b += al(tb * N * (m + 1)) + al(tb * N * (m + 1)) + 3 * al(tb * N);  // Wb, Z, y, pd, pc
-  b += al(8 * (N + 2)) * 2;                        // pieces (upper bound: one per row)
-  b += al(4 * (N + 2)) * 2 + al(8 * (host.ninst + 1)) + al(4 * (host.ninst + 1)) * 2 + al(4 * host.ninst);
-  b += al(sizeof(double) * 2 * 4096 * (kMaxRestart + 1));
+  b += 6 * al(8 * N);                                   // cmdt, g64, wdx64, kdx64, inp64, diag
+  b += al(8 * N) + al(4 * N) + al(4 * N);               // rhs, diagf, gf
+  b += 2 * al(tb * N * (m + 1)) + 3 * al(tb * N);       // Wb, Z, y, pd, pc
+  b += al(8 * (N + 2)) + al(4 * (N + 2));               // pieces, tiles (upper bounds)
+  b += al(4 * 4100) * 2 + al(8 * (host.ninst + 1)) + al(4 * (host.ninst + 1)) + al(4 * host.ninst);
+  b += al(sizeof(double) * 2 * 4096 * kMaxDots);
   b += al(sizeof(InstStat) * host.ninst) + al(64);
   return b;
 }
@@ -575,13 +635,26 @@ static int up(Arena &a, X *&dst, const X *src, size_t count, cudaStream_t st) {
     if (_rc != NRT_OK) return _rc;  \
   } while (0)
 
+// Groups pieces [pa, pb) into tiles whose row span fits the shared-memory staging area.
+static void make_tiles(const std::vector<int2> &pieces, int pa, int pb, int tile_rows,
+                       std::vector<int> &tiles) {
+  int64_t start_row = -1;
+  for (int p = pa; p < pb; p++) {
+    const int64_t end = (int64_t)pieces[p].x + pieces[p].y;
+    if (start_row < 0 || end - start_row > tile_rows) {
+      tiles.push_back(p);
+      start_row = pieces[p].x;
+    }
+  }
+}
+
 int Engine::implicit_init() {
   im = new ImplicitState();
   ImplicitState &S = *im;
   const int64_t N = host.ntot;
   const int32_t ni = host.ninst;
-  // implicit row structure (flags) per element; the validator guaranteed the
-  // reference numbering, so mother < j, DR == j + 1 off terminals.
+  // Row structure (flags) per element.  The validator guaranteed the reference
+  // numbering: mother < j, DR == j + 1 off terminals, terminals follow their mother.
   std::vector<char> is_term(N, 0);
   for (int64_t t : host.terms) is_term[t] = 1;
   for (int32_t i = 0; i < ni; i++) {
@@ -603,9 +676,9 @@ int Engine::implicit_init() {
   NRT_CUDA(cudaMemcpyAsync((void *)pv.topo, host.topo.data(), sizeof(Topo) * N,
                            cudaMemcpyHostToDevice, stream));
   // Segment pieces: maximal runs of consecutive physical rows linked to their
-  // predecessor (mother == j - 1 with a mother column), cut at kMaxPiece.
+  // predecessor (mother == j - 1 with a mother column), cut at kMaxPiece rows.
   S.inst_row.assign(host.off.begin(), host.off.end());
-  S.inst_piece.assign(ni + 1, 0);
+  std::vector<int> inst_piece(ni + 1, 0);
   for (int32_t i = 0; i < ni; i++) {
     const int64_t o = host.off[i], n = host.num_elem[i];
     int64_t start = -1;
@@ -622,44 +695,52 @@ int Engine::implicit_init() {
       if (!ident && start < 0) start = j;
     }
     if (start >= 0) S.pieces.push_back(make_int2((int)start, (int)(o + n - start)));
-    S.inst_piece[i + 1] = (int)S.pieces.size();
+    inst_piece[i + 1] = (int)S.pieces.size();
   }
-  // One tree: cooperative grid over all SMs, row ranges aligned with pieces.
-  S.grid_mode = ni == 1;
+  const int np = (int)S.pieces.size();
+  const size_t tb = opt.precision == NRT_MIXED ? 4 : 8;
+  const int tile_rows = (int)(kTileBytes / (4 * tb));
   int dev_sms = 0;
   NRT_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, device));
-  const size_t smem = shared_bytes(opt.restart);
+  S.smem = smem_bytes(opt.restart);
+  const bool mixed = opt.precision == NRT_MIXED;
+  S.grid_mode = ni == 1;
   if (S.grid_mode) {
+    // One tree: cooperative grid, row ranges aligned with pieces.
     int per_sm = 0;
-    auto kern = opt.precision == NRT_MIXED ? implicit_steps<float, true> : implicit_steps<double, true>;
-    NRT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    NRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
+    auto kern = mixed ? implicit_steps<float, true> : implicit_steps<double, true>;
+    NRT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
+    NRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, S.smem));
     if (per_sm < 1) {
       set_error("implicit kernel does not fit on an SM");
       return NRT_EDEVICE;
     }
-    // enough CTAs to cover the rows, at most one wave of co-resident CTAs
     const int64_t want = (N + 4 * kThreads - 1) / (4 * kThreads);
     int G = (int)std::min<int64_t>((int64_t)dev_sms * std::min(per_sm, 2), std::max<int64_t>(1, want));
-    G = std::min(G, 4096);
-    const int np = (int)S.pieces.size();
+    G = std::max(1, std::min(G, 4096));
+    std::vector<int> cta_piece(G + 1, np);
     S.cta_row.assign(G + 1, (int)N);
-    S.cta_piece.assign(G + 1, np);
     int q = 0;
     for (int c = 0; c < G; c++) {
       const int64_t goal = (N * (int64_t)c) / G;
       while (q < np && S.pieces[q].x + S.pieces[q].y <= goal) q++;
-      S.cta_piece[c] = std::min(q, np);
+      cta_piece[c] = std::min(q, np);
       S.cta_row[c] = c == 0 ? 0 : (q < np ? S.pieces[q].x : (int)N);
     }
     S.cta_row[0] = 0;
-    S.cta_piece[0] = 0;
-    for (int c = 1; c <= G; c++) {  // keep ranges monotone
+    cta_piece[0] = 0;
+    for (int c = 1; c <= G; c++) {
       S.cta_row[c] = std::max(S.cta_row[c], S.cta_row[c - 1]);
-      S.cta_piece[c] = std::max(S.cta_piece[c], S.cta_piece[c - 1]);
+      cta_piece[c] = std::max(cta_piece[c], cta_piece[c - 1]);
     }
     S.cta_row[G] = (int)N;
-    S.cta_piece[G] = np;
+    cta_piece[G] = np;
+    S.cta_tile.assign(G + 1, 0);
+    for (int c = 0; c < G; c++) {
+      S.cta_tile[c] = (int)S.tiles.size();
+      make_tiles(S.pieces, cta_piece[c], cta_piece[c + 1], tile_rows, S.tiles);
+    }
+    S.cta_tile[G] = (int)S.tiles.size();
     S.grid_blocks = G;
   } else {
     S.order.resize(ni);
@@ -667,11 +748,18 @@ int Engine::implicit_init() {
     std::stable_sort(S.order.begin(), S.order.end(),
                      [&](int a, int b) { return host.num_elem[a] > host.num_elem[b]; });
     int per_sm = 0;
-    auto kern = opt.precision == NRT_MIXED ? implicit_steps<float, false> : implicit_steps<double, false>;
-    NRT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    NRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
+    auto kern = mixed ? implicit_steps<float, false> : implicit_steps<double, false>;
+    NRT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
+    NRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, S.smem));
     S.grid_blocks = std::max(1, std::min<int>(dev_sms * std::max(per_sm, 1), ni));
+    S.inst_tile.assign(ni + 1, 0);
+    for (int32_t i = 0; i < ni; i++) {
+      S.inst_tile[i] = (int)S.tiles.size();
+      make_tiles(S.pieces, inst_piece[i], inst_piece[i + 1], tile_rows, S.tiles);
+    }
+    S.inst_tile[ni] = (int)S.tiles.size();
   }
+  S.tiles.push_back(np);  // sentinel: end piece of the last tile
   // device buffers
   cudaStream_t st = stream;
   ImView &iv = S.iv;
@@ -682,6 +770,7 @@ int Engine::implicit_init() {
   iv.tol = opt.tol;
   iv.max_iter = opt.max_iter;
   iv.ninst = ni;
+  iv.tile_rows = tile_rows;
   std::vector<double> cmdt(N), g64(N), w64(N), k64(N), inp(N);
   std::vector<float> gf(N);
   for (int64_t j = 0; j < N; j++) {
@@ -703,8 +792,7 @@ int Engine::implicit_init() {
   float *pf;
   TRYI(up(arena, pf, gf.data(), N, st)); iv.gf = pf;
   iv.diagf = nullptr;
-  if (opt.precision == NRT_MIXED) TRYI(up(arena, iv.diagf, (const float *)nullptr, N, st));
-  const size_t tb = opt.precision == NRT_MIXED ? 4 : 8;
+  if (mixed) TRYI(up(arena, iv.diagf, (const float *)nullptr, N, st));
   const int m = opt.restart;
   iv.Wb = arena.take(tb * N * (m + 1));
   iv.Z = arena.take(tb * N * (m + 1));
@@ -721,27 +809,27 @@ int Engine::implicit_init() {
   int2 *pc;
   TRYI(up(arena, pc, S.pieces.data(), S.pieces.size(), st)); iv.pieces = pc;
   int *pi;
+  TRYI(up(arena, pi, S.tiles.data(), S.tiles.size(), st)); iv.tiles = pi;
   if (S.grid_mode) {
     TRYI(up(arena, pi, S.cta_row.data(), S.cta_row.size(), st)); iv.cta_row = pi;
-    TRYI(up(arena, pi, S.cta_piece.data(), S.cta_piece.size(), st)); iv.cta_piece = pi;
+    TRYI(up(arena, pi, S.cta_tile.data(), S.cta_tile.size(), st)); iv.cta_tile = pi;
+  } else {
+    TRYI(up(arena, pi, S.inst_tile.data(), S.inst_tile.size(), st)); iv.inst_tile = pi;
+    TRYI(up(arena, pi, S.order.data(), S.order.size(), st)); iv.order = pi;
   }
   int64_t *pl;
   TRYI(up(arena, pl, S.inst_row.data(), S.inst_row.size(), st)); iv.inst_row = pl;
-  TRYI(up(arena, pi, S.inst_piece.data(), S.inst_piece.size(), st)); iv.inst_piece = pi;
-  if (!S.grid_mode) {
-    TRYI(up(arena, pi, S.order.data(), S.order.size(), st)); iv.order = pi;
-  }
   TRYI(up(arena, iv.queue, (const int *)nullptr, 1, st));
-  TRYI(up(arena, iv.partials, (const double *)nullptr, (size_t)2 * 4096 * (kMaxRestart + 1), st));
-  S.last_stats.assign(ni, InstStat{0, 0, 0, 0.0});
-  TRYI(up(arena, iv.stats, S.last_stats.data(), ni, st));
+  TRYI(up(arena, iv.partials, (const double *)nullptr, (size_t)2 * 4096 * kMaxDots, st));
+  std::vector<InstStat> zero(ni, InstStat{0, 0, 0, 0.0});
+  TRYI(up(arena, iv.stats, zero.data(), ni, st));
+  NRT_CUDA(cudaStreamSynchronize(st));
   return NRT_OK;
 }
 
 // Runs `nsteps` implicit steps for every instance (one launch).
 static int implicit_launch(Engine &e, int nsteps, int force) {
   ImplicitState &S = *e.im;
-  const size_t smem = shared_bytes(e.opt.restart);
   NRT_CUDA(cudaMemsetAsync(S.iv.queue, 0, sizeof(int), e.stream));
   PackView pv = e.pv;
   ImView iv = S.iv;
@@ -751,10 +839,10 @@ static int implicit_launch(Engine &e, int nsteps, int force) {
   const bool mixed = e.opt.precision == NRT_MIXED;
   if (S.grid_mode) {
     const void *k = mixed ? (const void *)implicit_steps<float, true> : (const void *)implicit_steps<double, true>;
-    NRT_CUDA(cudaLaunchCooperativeKernel(k, dim3(S.grid_blocks), dim3(kThreads), args, smem, e.stream));
+    NRT_CUDA(cudaLaunchCooperativeKernel(k, dim3(S.grid_blocks), dim3(kThreads), args, S.smem, e.stream));
   } else {
     const void *k = mixed ? (const void *)implicit_steps<float, false> : (const void *)implicit_steps<double, false>;
-    NRT_CUDA(cudaLaunchKernel(k, dim3(S.grid_blocks), dim3(kThreads), args, smem, e.stream));
+    NRT_CUDA(cudaLaunchKernel(k, dim3(S.grid_blocks), dim3(kThreads), args, S.smem, e.stream));
   }
   return NRT_OK;
 }
@@ -815,21 +903,20 @@ int Engine::get_stats(nrt_stats *st) {
 }
 
 // Expands the stored symmetric system to the reference's CSR (src/solverIm-cpu.cpp:29-183
-// column order: mother, diagonal, DR, DL; identity rows 1).
+// column order: mother, diagonal, DR, DL; identity rows 1).  Runs an assembly-only pass
+// for the next step and restores the state it touched.
 int export_system(Engine &e, int input_active, int32_t *row_ptr, int32_t *col, double *val,
                   double *rhs, int32_t *nnz_out) {
   if (e.opt.mode != NRT_IMPLICIT_BE || e.host.ninst != 1) {
     set_error("export_system needs a single-tree implicit solver");
     return NRT_EINVAL;
   }
-  // Assemble on copies of the state: save gates, run one assembly-only pass via a
-  // zero-iteration solve, then restore.
   const int64_t N = e.host.ntot;
   const bool mixed = e.opt.precision == NRT_MIXED;
   const size_t gb = (mixed ? 4 : 8) * 3 * N;
   void *gate = mixed ? (void *)e.pv.gatef : (void *)e.pv.gate;
   std::vector<char> saved(gb);
-  std::vector<double> Vsave(N), Vother(N);
+  std::vector<double> Vother(N);
   ImplicitState &S = *e.im;
   InstStat stat0;
   NRT_CUDA(cudaMemcpyAsync(saved.data(), gate, gb, cudaMemcpyDeviceToHost, e.stream));
@@ -837,7 +924,7 @@ int export_system(Engine &e, int input_active, int32_t *row_ptr, int32_t *col, d
   NRT_CUDA(cudaMemcpyAsync(&stat0, S.iv.stats, sizeof(InstStat), cudaMemcpyDeviceToHost, e.stream));
   NRT_CUDA(cudaStreamSynchronize(e.stream));
   const int saved_iter = S.iv.max_iter;
-  S.iv.max_iter = -1;  // budget 0 after the first residual: assembly only
+  S.iv.max_iter = -1;  // assembly only
   int rc = implicit_launch(e, 1, input_active ? 1 : 0);
   S.iv.max_iter = saved_iter;
   if (rc) return rc;

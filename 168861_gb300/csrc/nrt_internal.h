@@ -101,9 +101,10 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp);
 
 // Kernel launchers (explicit.cu).
 int launch_explicit_step(const PackView &pv, int precision, bool general, int k, int force,
-                         const double *Vin, double *Vout, cudaStream_t st);
+                         const double *Vin, double *Vout, const float *Fin, float *Fout,
+                         cudaStream_t st);
 int launch_terminal_fixup(const Topo *topo, const int64_t *terms, int64_t nterm, double *V,
-                          cudaStream_t st);
+                          float *Vf, cudaStream_t st);
 int launch_advance_base(InstDev *inst, int32_t ninst, int64_t steps, cudaStream_t st);
 
 }  // namespace nrt

@@ -6,7 +6,7 @@
 namespace nrt {
 
 constexpr int kChunk = 64;        // steps per captured graph (even: buffer parity returns)
-constexpr int kMaxRestart = 64;   // GMRES restart limit (Hessenberg kept in shared memory)
+constexpr int kMaxRestart = 32;   // GMRES restart limit (dot accumulators live in registers)
 
 struct Arena {
   void *base = nullptr;
@@ -26,6 +26,7 @@ struct Engine {
   Arena arena;
   PackView pv{};
   double *V[2] = {nullptr, nullptr};
+  float *Vf[2] = {nullptr, nullptr};  // FP32 shadow of V (mixed explicit mode only)
   int cur = 0;
   int64_t *terms = nullptr;
   int64_t steps_done = 0;

@@ -98,7 +98,7 @@ typedef struct nrt_options {
   int32_t precision;             /* nrt_precision */
   int32_t krylov;                /* nrt_krylov */
   int32_t precond;               /* nrt_precond */
-  int32_t restart;               /* GMRES restart length (<= 64) */
+  int32_t restart;               /* GMRES restart length (<= 32) */
   int32_t tol_mode;              /* nrt_tol_mode */
   double tol;                    /* residual tolerance per step */
   int32_t max_iter;              /* Krylov iterations per step; 0 -> num_elem */

@@ -25,7 +25,9 @@ def problem(pkg, g):
 
 
 def tight(**kw):
-    o = dict(tol=1e-13, tol_mode="rel", restart=30, precond="segment")
+    """FP64 solve to a relative residual of 1e-11 (the FP64 floor of b - A x on these
+    stiff dx = 1-4 um trees is ~4e-13 ||b||; 1e-11 keeps the error below ~1e-12 V)."""
+    o = dict(tol=1e-11, tol_mode="rel", restart=30, precond="segment")
     o.update(kw)
     return o
 
@@ -36,7 +38,7 @@ def test_implicit_fp64_matches_exact_solution(gpu, pkg, orc, name, precond):
     g = load_golden(name)
     spec = g["spec"]
     steps = int(g["numStepsT"]) - 2
-    s = pkg.SolverIm(problem(pkg, g), **tight(precond=precond))
+    s = pkg.SolverIm(problem(pkg, g), **tight(precond=precond, max_iter=20000))
     s.run(1, 1 + steps, spec.init_time, spec.end_input)
     V = s.snapshot()
     d = orc.derive(spec)
@@ -149,7 +151,7 @@ def test_implicit_batch_alone_equals_in_mix(gpu, pkg, orc, model, precision):
 
 
 def test_implicit_budget_exhaustion_reported(gpu, pkg):
-    """A Krylov budget of one iteration cannot reach 1e-13: calculate() reports
+    """A Krylov budget of one iteration cannot reach 1e-11: calculate() reports
     NRT_ENOCONV and the state still advances (the reference would exit(0))."""
     g = load_golden("im_axon300")
     s = pkg.SolverIm(problem(pkg, g), **tight(max_iter=1, precond="none"))
