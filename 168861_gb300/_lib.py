@@ -40,8 +40,23 @@ class Options(ctypes.Structure):
         ("mode", ctypes.c_int32), ("precision", ctypes.c_int32), ("krylov", ctypes.c_int32),
         ("precond", ctypes.c_int32), ("restart", ctypes.c_int32), ("tol_mode", ctypes.c_int32),
         ("tol", ctypes.c_double), ("max_iter", ctypes.c_int32), ("device", ctypes.c_int32),
-        ("use_graphs", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7),
+        ("use_graphs", ctypes.c_int32), ("schedule", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 6),
     ]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("budget_bytes", ctypes.c_int64), ("chunk_steps", ctypes.c_int32),
+                ("max_batch", ctypes.c_int32), ("max_wait_us", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 5)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64),
+                ("rejected", ctypes.c_int64), ("batches_created", ctypes.c_int64),
+                ("compartment_steps", ctypes.c_int64), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
+                ("busy_seconds", ctypes.c_double), ("peak_bytes", ctypes.c_int64)]
 
 
 class Stats(ctypes.Structure):
@@ -64,6 +79,8 @@ EXPORTS = (
     "nrt_get_stats", "nrt_destroy", "nrt_status_string", "nrt_last_error", "nrt_derive",
     "nrt_batch_create", "nrt_batch_set_runs", "nrt_batch_advance", "nrt_batch_synchronize", "nrt_batch_get_stream",
     "nrt_batch_snapshot", "nrt_batch_remaining", "nrt_batch_get_stats", "nrt_batch_destroy",
+    "nrt_server_create", "nrt_server_submit", "nrt_server_result", "nrt_server_drain",
+    "nrt_server_get_stats", "nrt_server_destroy",
 )
 
 _lib = None
@@ -105,6 +122,14 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "nrt_batch_remaining": [vp, _i64p],
         "nrt_batch_get_stats": [vp, ctypes.POINTER(Stats)],
         "nrt_batch_destroy": [vp],
+        "nrt_server_create": [ctypes.POINTER(ServerConfig), ctypes.POINTER(Options),
+                              ctypes.POINTER(Options), vpp],
+        "nrt_server_submit": [vp, ctypes.POINTER(Problem), ctypes.c_int,
+                              ctypes.POINTER(InstanceRun), _i64p],
+        "nrt_server_result": [vp, ctypes.c_int64, _f64p],
+        "nrt_server_drain": [vp],
+        "nrt_server_get_stats": [vp, ctypes.POINTER(ServerStats)],
+        "nrt_server_destroy": [vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libneurite_gb300.so")
-SOURCES = ["api.cu", "explicit.cu", "implicit.cu", "derive.cpp"]
+SOURCES = ["api.cu", "explicit.cu", "implicit.cu", "derive.cpp", "serve.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -67,7 +67,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         list(ex.map(run, jobs))
     if jobs or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
-        run([cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
+        run([cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-Xcompiler", "-pthread"])
         os.replace(tmp, LIB)
     return LIB
 

@@ -56,6 +56,7 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kMaxPiece = 256;                 // longest segment piece one sweep handles
 constexpr int kMaxDots = kMaxRestart + 1;
 constexpr int kTileBytes = 48 * 1024;          // shared-memory staging for the sweeps
+constexpr int kU = 4;                          // rows per thread kept in flight in row loops
 
 struct InstStat {
   int64_t iters;
@@ -444,12 +445,26 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
       T acc[kMaxDots];
 #pragma unroll
       for (int i = 0; i < kMaxDots; i++) acc[i] = 0;
-      for (int64_t r = c.r0 + threadIdx.x; r < c.r1; r += blockDim.x) {
-        const T y = sj * row_apply<T>(pv, iv, r, Zj);
-        c.w.y[r] = y;
+      const int64_t stride = (int64_t)blockDim.x;
+      for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kU * stride) {
+        T y[kU];  // kU rows per thread in flight
 #pragma unroll
-        for (int i = 0; i < kMaxDots; i++)
-          if (i <= j) acc[i] += y * c.w.Wb[(size_t)i * N + r];
+        for (int u = 0; u < kU; u++) {
+          const int64_t r = rb + u * stride;
+          y[u] = r < c.r1 ? sj * row_apply<T>(pv, iv, r, Zj) : (T)0;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; u++)
+          if (rb + u * stride < c.r1) c.w.y[rb + u * stride] = y[u];
+#pragma unroll
+        for (int i = 0; i < kMaxDots; i++) {
+          if (i <= j) {
+            const T *Wi = c.w.Wb + (size_t)i * N;
+#pragma unroll
+            for (int u = 0; u < kU; u++)
+              if (rb + u * stride < c.r1) acc[i] += y[u] * Wi[rb + u * stride];
+          }
+        }
       }
       group_reduce<kGrid>(grid, acc, j + 1, S, iv.partials, parity);
       if (threadIdx.x <= j) {
@@ -462,13 +477,26 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
       T *Wn = c.w.Wb + (size_t)(j + 1) * N;
       T nacc[kMaxDots];
       nacc[0] = 0;
-      for (int64_t r = c.r0 + threadIdx.x; r < c.r1; r += blockDim.x) {
-        T a = c.w.y[r];
+      for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kU * stride) {
+        T a[kU];
 #pragma unroll
-        for (int i = 0; i < kMaxDots; i++)
-          if (i <= j) a -= coef[i] * c.w.Wb[(size_t)i * N + r];
-        Wn[r] = a;
-        nacc[0] += a * a;
+        for (int u = 0; u < kU; u++) a[u] = rb + u * stride < c.r1 ? c.w.y[rb + u * stride] : (T)0;
+#pragma unroll
+        for (int i = 0; i < kMaxDots; i++) {
+          if (i <= j) {
+            const T ci = coef[i];
+            const T *Wi = c.w.Wb + (size_t)i * N;
+#pragma unroll
+            for (int u = 0; u < kU; u++)
+              if (rb + u * stride < c.r1) a[u] -= ci * Wi[rb + u * stride];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; u++)
+          if (rb + u * stride < c.r1) {
+            Wn[rb + u * stride] = a[u];
+            nacc[0] += a[u] * a[u];
+          }
       }
       __syncthreads();
       apply_precond(c, S, Wn, c.w.Z + (size_t)(j + 1) * N);
@@ -505,13 +533,28 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
       for (int i = 0; i < k; i++) coef[i] = (T)(S.y[i] * S.s[i]);
     }
     __syncthreads();
-    for (int64_t r = c.r0 + threadIdx.x; r < c.r1; r += blockDim.x) {
-      if (pv.topo[r].flags & F_IDENT) continue;
-      T a = 0;
+    {
+      const int64_t stride = (int64_t)blockDim.x;
+      for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kU * stride) {
+        T a[kU];
 #pragma unroll
-      for (int i = 0; i < kMaxDots; i++)
-        if (i < k) a += coef[i] * c.w.Z[(size_t)i * N + r];
-      Vout[r] += (double)a;
+        for (int u = 0; u < kU; u++) a[u] = 0;
+#pragma unroll
+        for (int i = 0; i < kMaxDots; i++) {
+          if (i < k) {
+            const T ci = coef[i];
+            const T *Zi = c.w.Z + (size_t)i * N;
+#pragma unroll
+            for (int u = 0; u < kU; u++)
+              if (rb + u * stride < c.r1) a[u] += ci * Zi[rb + u * stride];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+          const int64_t r = rb + u * stride;
+          if (r < c.r1 && !(pv.topo[r].flags & F_IDENT)) Vout[r] += (double)a[u];
+        }
+      }
     }
     group_sync<kGrid>(grid);
   }
@@ -704,7 +747,7 @@ int Engine::implicit_init() {
   NRT_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, device));
   S.smem = smem_bytes(opt.restart);
   const bool mixed = opt.precision == NRT_MIXED;
-  S.grid_mode = ni == 1;
+  S.grid_mode = ni == 1 && opt.schedule == 0;
   if (S.grid_mode) {
     // One tree: cooperative grid, row ranges aligned with pieces.
     int per_sm = 0;

@@ -1,0 +1,345 @@
+// Serving loop (nrt_server_*): continuous batching of simulation requests.
+//
+// A worker thread owns every device handle.  Each tick it
+//   1. admits pending requests (FIFO, grouped by kind) while their estimated device
+//      footprint fits what the budget leaves free, and packs the admitted requests of
+//      one kind into a new batch (one device-resident pack, one launch per step);
+//   2. advances every resident batch by `chunk_steps` on the batch's own stream, all
+//      launches enqueued before any wait, so batches admitted at different times run
+//      concurrently on the device;
+//   3. collects the requests whose loop range is exhausted (their potential is copied
+//      out at once) and frees a batch when all of its requests are done.
+// Latency is measured from submit to result-ready on the host clock.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "neurite_gb300.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct OwnedProblem {
+  std::vector<int32_t> mother, dr, dl, branching, terminals, hh_elem;
+  std::vector<double> dx, c_m, r_a, W, K, input, m, h, n, g_Na, g_K, G_L, E_Na, E_K, E_L,
+      ls_Na, ls_K, rest, V0, V1;
+  nrt_problem p;
+
+  template <class T>
+  static void take(std::vector<T> &dst, const T *src, size_t n) {
+    if (src) dst.assign(src, src + n); else dst.clear();
+  }
+  template <class T>
+  static const T *ptr(const std::vector<T> &v) {
+    return v.empty() ? nullptr : v.data();
+  }
+
+  void copy(const nrt_problem &s) {
+    const size_t N = (size_t)s.num_elem, H = (size_t)s.num_hh, T = (size_t)s.num_term;
+    take(mother, s.mother, N); take(dr, s.dr, N); take(dl, s.dl, N);
+    take(branching, s.branching, N); take(terminals, s.terminals, T);
+    take(dx, s.dx, N); take(c_m, s.c_m, N); take(r_a, s.r_a, N); take(W, s.W, N);
+    take(K, s.K, N); take(input, s.input, N); take(V0, s.V0, N); take(V1, s.V1, N);
+    take(hh_elem, s.hh_elem, H); take(m, s.m, H); take(h, s.h, H); take(n, s.n, H);
+    take(g_Na, s.g_Na, H); take(g_K, s.g_K, H); take(G_L, s.G_L, H); take(E_Na, s.E_Na, H);
+    take(E_K, s.E_K, H); take(E_L, s.E_L, H); take(ls_Na, s.ls_Na, H); take(ls_K, s.ls_K, H);
+    take(rest, s.rest, H);
+    p = s;
+    p.mother = ptr(mother); p.dr = ptr(dr); p.dl = ptr(dl); p.branching = ptr(branching);
+    p.terminals = ptr(terminals); p.dx = ptr(dx); p.c_m = ptr(c_m); p.r_a = ptr(r_a);
+    p.W = ptr(W); p.K = ptr(K); p.input = ptr(input); p.V0 = ptr(V0); p.V1 = ptr(V1);
+    p.hh_elem = ptr(hh_elem); p.m = ptr(m); p.h = ptr(h); p.n = ptr(n);
+    p.g_Na = ptr(g_Na); p.g_K = ptr(g_K); p.G_L = ptr(G_L); p.E_Na = ptr(E_Na);
+    p.E_K = ptr(E_K); p.E_L = ptr(E_L); p.ls_Na = ptr(ls_Na); p.ls_K = ptr(ls_K);
+    p.rest = ptr(rest);
+  }
+};
+
+struct Request {
+  int64_t id = 0;
+  bool implicit = false;
+  OwnedProblem prob;
+  nrt_instance_run run{};
+  size_t bytes = 0;
+  Clock::time_point t_submit, t_done;
+  std::vector<double> result;
+  int status = NRT_OK;
+  bool done = false;
+};
+
+struct MicroBatch {
+  nrt_batch *b = nullptr;
+  std::vector<Request *> reqs;
+  std::vector<char> finished;
+  size_t bytes = 0;
+  size_t open = 0;
+};
+
+// Device footprint of one tree in a batch (the arena sizes of the engine, rounded up).
+size_t estimate_bytes(const nrt_problem &p, const nrt_options &o) {
+  const double N = (double)p.num_elem;
+  const bool mixed = o.precision == NRT_MIXED;
+  const double tb = mixed ? 4 : 8;
+  double per = 16 + 16 + 16 + (mixed ? (7 * 4 + 12 + 44) : (5 * 8 + 24 + 88));
+  if (o.mode == NRT_IMPLICIT_BE) per += 48 + 8 + 8 + 2 * tb * (o.restart + 1) + 3 * tb + 16;
+  return (size_t)(N * per * 1.15) + (1 << 20);
+}
+
+}  // namespace
+
+struct nrt_server {
+  nrt_server_config cfg{};
+  nrt_options opt[2];  // [0] explicit, [1] implicit
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Request *> pending;
+  std::map<int64_t, Request *> reqs;
+  std::vector<MicroBatch *> active;  // worker-owned
+  std::thread worker;
+  bool stop = false;
+  int64_t next_id = 1;
+  size_t used = 0;
+  int64_t outstanding = 0;
+  nrt_server_stats st{};
+  std::vector<double> lat_ms;
+  double busy = 0;
+
+  void loop();
+  MicroBatch *admit(bool implicit, std::vector<Request *> &batch);
+};
+
+MicroBatch *nrt_server::admit(bool implicit, std::vector<Request *> &batch) {
+  std::vector<nrt_problem> probs;
+  std::vector<nrt_instance_run> runs;
+  for (Request *r : batch) {
+    probs.push_back(r->prob.p);
+    runs.push_back(r->run);
+  }
+  MicroBatch *mb = new MicroBatch();
+  int rc = nrt_batch_create(probs.data(), (int32_t)probs.size(), &opt[implicit ? 1 : 0], &mb->b);
+  if (rc == NRT_OK) rc = nrt_batch_set_runs(mb->b, runs.data());
+  std::lock_guard<std::mutex> lk(mu);
+  if (rc != NRT_OK) {
+    for (Request *r : batch) {
+      r->status = rc;
+      r->done = true;
+      r->t_done = Clock::now();
+      used -= r->bytes;
+      outstanding--;
+    }
+    if (mb->b) nrt_batch_destroy(mb->b);
+    delete mb;
+    cv_done.notify_all();
+    return nullptr;
+  }
+  mb->reqs = batch;
+  mb->finished.assign(batch.size(), 0);
+  mb->open = batch.size();
+  for (Request *r : batch) mb->bytes += r->bytes;
+  st.batches_created++;
+  return mb;
+}
+
+void nrt_server::loop() {
+  for (;;) {
+    std::vector<Request *> take[2];
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      if (active.empty()) {
+        cv_work.wait(lk, [&] { return stop || !pending.empty(); });
+        if (stop && pending.empty()) break;
+        if (cfg.max_wait_us > 0) {  // let a burst of arrivals gather into one batch
+          lk.unlock();
+          std::this_thread::sleep_for(std::chrono::microseconds(cfg.max_wait_us));
+          lk.lock();
+        }
+      }
+      // admission: FIFO within each kind, while the budget leaves room
+      size_t free_bytes = (size_t)cfg.budget_bytes > used ? (size_t)cfg.budget_bytes - used : 0;
+      for (auto it = pending.begin(); it != pending.end();) {
+        Request *r = *it;
+        std::vector<Request *> &t = take[r->implicit ? 1 : 0];
+        if (r->bytes <= free_bytes && (int)t.size() < cfg.max_batch) {
+          free_bytes -= r->bytes;
+          used += r->bytes;
+          t.push_back(r);
+          it = pending.erase(it);
+        } else {
+          ++it;
+        }
+      }
+      if (stop && pending.empty() && active.empty() && take[0].empty() && take[1].empty()) break;
+    }
+    for (int k = 0; k < 2; k++)
+      if (!take[k].empty()) {
+        MicroBatch *mb = admit(k == 1, take[k]);
+        if (mb) active.push_back(mb);
+      }
+    if (active.empty()) continue;
+    const auto t0 = Clock::now();
+    // one tick: every resident batch advances on its own stream (all enqueued first)
+    for (MicroBatch *mb : active) nrt_batch_advance(mb->b, cfg.chunk_steps);
+    // collect finished requests
+    std::vector<int64_t> rem;
+    for (MicroBatch *mb : active) {
+      rem.assign(mb->reqs.size(), 0);
+      int rc = nrt_batch_remaining(mb->b, rem.data());
+      nrt_stats bs;
+      const bool bad = rc != NRT_OK;
+      for (size_t q = 0; q < mb->reqs.size(); q++) {
+        if (mb->finished[q] || (!bad && rem[q] > 0)) continue;
+        Request *r = mb->reqs[q];
+        r->result.resize(r->prob.p.num_elem);
+        int src = bad ? rc : nrt_batch_snapshot(mb->b, (int32_t)q, r->result.data());
+        std::lock_guard<std::mutex> lk(mu);
+        r->status = src;
+        r->done = true;
+        r->t_done = Clock::now();
+        mb->finished[q] = 1;
+        mb->open--;
+        outstanding--;
+        st.completed++;
+        st.compartment_steps += (int64_t)r->prob.p.num_elem * (r->run.i_end - r->run.i_begin);
+        lat_ms.push_back(std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
+      }
+      if (nrt_batch_get_stats(mb->b, &bs) == NRT_OK && bs.nonconverged_steps > 0) {
+        // report non-convergence on the requests that finished in this batch
+        std::lock_guard<std::mutex> lk(mu);
+        for (size_t q = 0; q < mb->reqs.size(); q++)
+          if (mb->finished[q] && mb->reqs[q]->status == NRT_OK) mb->reqs[q]->status = NRT_ENOCONV;
+      }
+    }
+    cv_done.notify_all();
+    for (size_t a = 0; a < active.size();) {
+      MicroBatch *mb = active[a];
+      if (mb->open == 0) {
+        nrt_batch_destroy(mb->b);
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          used -= mb->bytes;
+        }
+        delete mb;
+        active.erase(active.begin() + a);
+      } else {
+        a++;
+      }
+    }
+    busy += std::chrono::duration<double>(Clock::now() - t0).count();
+  }
+}
+
+extern "C" {
+
+int nrt_server_create(const nrt_server_config *cfg, const nrt_options *explicit_opt,
+                      const nrt_options *implicit_opt, nrt_server **out) {
+  if (!cfg || !out || cfg->budget_bytes <= 0) return NRT_EINVAL;
+  nrt_server *s = new (std::nothrow) nrt_server();
+  if (!s) return NRT_ENOMEM;
+  s->cfg = *cfg;
+  if (s->cfg.chunk_steps <= 0) s->cfg.chunk_steps = 64;
+  if (s->cfg.max_batch <= 0) s->cfg.max_batch = 4096;
+  if (s->cfg.max_wait_us < 0) s->cfg.max_wait_us = 0;
+  nrt_options_default(&s->opt[0]);
+  nrt_options_default(&s->opt[1]);
+  if (explicit_opt) s->opt[0] = *explicit_opt;
+  if (implicit_opt) s->opt[1] = *implicit_opt;
+  s->opt[0].mode = NRT_EXPLICIT;
+  s->opt[1].mode = NRT_IMPLICIT_BE;
+  s->opt[1].schedule = 1;  // block per instance: resident batches share the GPU
+  s->worker = std::thread([s] { s->loop(); });
+  *out = s;
+  return NRT_OK;
+}
+
+int nrt_server_submit(nrt_server *s, const nrt_problem *p, int implicit,
+                      const nrt_instance_run *run, int64_t *request_id) {
+  if (!s || !p || !run || !request_id) return NRT_EINVAL;
+  if (p->num_elem < 4 || run->i_end < run->i_begin) return NRT_EINVAL;
+  Request *r = new (std::nothrow) Request();
+  if (!r) return NRT_ENOMEM;
+  r->implicit = implicit != 0;
+  r->prob.copy(*p);
+  r->run = *run;
+  r->bytes = estimate_bytes(*p, s->opt[r->implicit ? 1 : 0]);
+  r->t_submit = Clock::now();
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->st.submitted++;
+  if (r->bytes > (size_t)s->cfg.budget_bytes) {
+    s->st.rejected++;
+    delete r;
+    return NRT_EBUDGET;
+  }
+  r->id = s->next_id++;
+  *request_id = r->id;
+  s->reqs[r->id] = r;
+  s->pending.push_back(r);
+  s->outstanding++;
+  s->cv_work.notify_one();
+  return NRT_OK;
+}
+
+int nrt_server_result(nrt_server *s, int64_t id, double *potential) {
+  if (!s || !potential) return NRT_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return NRT_ESTATE;
+  Request *r = it->second;
+  if (!r->done) return NRT_ENOTREADY;
+  const int status = r->status;
+  if (!r->result.empty()) memcpy(potential, r->result.data(), sizeof(double) * r->result.size());
+  s->reqs.erase(it);
+  delete r;
+  return status;
+}
+
+int nrt_server_drain(nrt_server *s) {
+  if (!s) return NRT_EINVAL;
+  std::unique_lock<std::mutex> lk(s->mu);
+  s->cv_done.wait(lk, [&] { return s->outstanding == 0; });
+  return NRT_OK;
+}
+
+int nrt_server_get_stats(nrt_server *s, nrt_server_stats *st) {
+  if (!s || !st) return NRT_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);
+  *st = s->st;
+  std::vector<double> l = s->lat_ms;
+  std::sort(l.begin(), l.end());
+  auto pct = [&](double q) {
+    if (l.empty()) return 0.0;
+    const size_t k = (size_t)std::min<double>(l.size() - 1, floor(q * (l.size() - 1) + 0.5));
+    return l[k];
+  };
+  st->p50_ms = pct(0.50);
+  st->p99_ms = pct(0.99);
+  st->max_ms = l.empty() ? 0.0 : l.back();
+  st->busy_seconds = s->busy;
+  st->peak_bytes = 0;
+  return NRT_OK;
+}
+
+int nrt_server_destroy(nrt_server *s) {
+  if (!s) return NRT_EINVAL;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  for (auto &kv : s->reqs) delete kv.second;
+  delete s;
+  return NRT_OK;
+}
+
+}  // extern "C"

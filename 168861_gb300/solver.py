@@ -118,7 +118,7 @@ class ProblemArrays:
 def make_options(mode: int, precision: str = "fp64", krylov: str = "gmres",
                  precond: str = "segment", restart: int = 30, tol: float = 1e-14,
                  tol_mode: str = "abs", max_iter: int = 0, use_graphs: bool = True,
-                 device: int = -1) -> _lib.Options:
+                 device: int = -1, schedule: int = 0) -> _lib.Options:
     lib = _lib.load()
     o = _lib.Options()
     check(lib.nrt_options_default(ctypes.byref(o)), "nrt_options_default")
@@ -132,6 +132,7 @@ def make_options(mode: int, precision: str = "fp64", krylov: str = "gmres",
     o.max_iter = max_iter
     o.use_graphs = int(use_graphs)
     o.device = device
+    o.schedule = int(schedule)
     return o
 
 
@@ -282,6 +283,65 @@ class Batch:
     def close(self) -> None:
         if getattr(self, "h", None):
             self.lib.nrt_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching request loop (nrt_server_*): requests are admitted by device
+    memory budget, packed per admission into resident batches that advance concurrently,
+    and returned as each finishes."""
+
+    def __init__(self, budget_bytes: int, chunk_steps: int = 64, max_batch: int = 4096,
+                 max_wait_us: int = 200, explicit_opts: dict | None = None,
+                 implicit_opts: dict | None = None):
+        self.lib = _lib.load()
+        cfg = _lib.ServerConfig(int(budget_bytes), int(chunk_steps), int(max_batch),
+                                int(max_wait_us))
+        self.ex = make_options(_lib.NRT_EXPLICIT, **(explicit_opts or {}))
+        self.im = make_options(_lib.NRT_IMPLICIT_BE, **(implicit_opts or {}))
+        h = ctypes.c_void_p()
+        check(self.lib.nrt_server_create(ctypes.byref(cfg), ctypes.byref(self.ex),
+                                         ctypes.byref(self.im), ctypes.byref(h)),
+              "nrt_server_create")
+        self.h = h
+        self.sizes = {}
+
+    def submit(self, problem: ProblemArrays, implicit: bool, i_begin: int, i_end: int,
+               init_time: float, end_input: float) -> int:
+        run = _lib.InstanceRun(int(i_begin), int(i_end), float(init_time), float(end_input))
+        rid = ctypes.c_int64(0)
+        check(self.lib.nrt_server_submit(self.h, ctypes.byref(problem.struct), int(bool(implicit)),
+                                         ctypes.byref(run), ctypes.byref(rid)), "nrt_server_submit")
+        self.sizes[rid.value] = problem.num_elem
+        return rid.value
+
+    def result(self, rid: int):
+        """Final potential of a finished request, or None while it runs."""
+        out = np.empty(self.sizes[rid])
+        rc = self.lib.nrt_server_result(self.h, int(rid), _p(out, ctypes.c_double))
+        if rc == _lib.NRT_ENOTREADY:
+            return None
+        check(rc, "nrt_server_result")
+        del self.sizes[rid]
+        return out
+
+    def drain(self) -> None:
+        check(self.lib.nrt_server_drain(self.h), "nrt_server_drain")
+
+    def stats(self) -> _lib.ServerStats:
+        st = _lib.ServerStats()
+        check(self.lib.nrt_server_get_stats(self.h, ctypes.byref(st)), "nrt_server_get_stats")
+        return st
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.nrt_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -104,7 +104,9 @@ typedef struct nrt_options {
   int32_t max_iter;              /* Krylov iterations per step; 0 -> num_elem */
   int32_t device;                /* CUDA device ordinal; -1 -> current device */
   int32_t use_graphs;            /* capture nrt_run time loops in CUDA graphs (default 1) */
-  int32_t reserved[7];
+  int32_t schedule;              /* implicit: 0 = auto (one tree -> cooperative whole-GPU
+                                    launch), 1 = always block per instance */
+  int32_t reserved[6];
 } nrt_options;
 
 typedef struct nrt_stats {
@@ -215,6 +217,48 @@ int nrt_batch_snapshot(nrt_batch *b, int32_t instance, double *potential);
 int nrt_batch_remaining(nrt_batch *b, int64_t *remaining);
 int nrt_batch_get_stats(nrt_batch *b, nrt_stats *st);
 int nrt_batch_destroy(nrt_batch *b);
+
+/* ----------------------------------------------------------------------------------
+ * Serving: a request loop (worker thread) that admits simulation requests by device
+ * memory budget, packs the requests admitted together into one batch, keeps every
+ * batch's state resident, advances all resident batches each tick on their own streams
+ * (work of requests that arrived at different times overlaps on the device), and hands
+ * results back as each request finishes.  No reference counterpart.
+ *
+ * A request is one tree (copied at submit) with its loop range and stimulus window;
+ * `implicit` selects the backward-Euler engine.  The server's two option sets (explicit,
+ * implicit) fix precision and solver settings for all requests of that kind. */
+typedef struct nrt_server nrt_server;
+
+typedef struct nrt_server_config {
+  int64_t budget_bytes;          /* device memory the resident batches may use */
+  int32_t chunk_steps;           /* steps per tick for every resident batch (default 64) */
+  int32_t max_batch;             /* most requests packed into one batch (default 4096) */
+  int32_t max_wait_us;           /* admission waits this long to gather a batch (default 200) */
+  int32_t reserved[5];
+} nrt_server_config;
+
+typedef struct nrt_server_stats {
+  int64_t submitted, completed, rejected;
+  int64_t batches_created;
+  int64_t compartment_steps;     /* sum over completed requests of num_elem * steps */
+  double p50_ms, p99_ms, max_ms; /* submit -> result-ready latency of completed requests */
+  double busy_seconds;           /* wall time with at least one resident batch */
+  int64_t peak_bytes;            /* largest device memory held at once */
+} nrt_server_stats;
+
+int nrt_server_create(const nrt_server_config *cfg, const nrt_options *explicit_opt,
+                      const nrt_options *implicit_opt, nrt_server **out);
+/* Copies the request; returns its id.  NRT_EBUDGET if it can never fit the budget. */
+int nrt_server_submit(nrt_server *s, const nrt_problem *p, int implicit,
+                      const nrt_instance_run *run, int64_t *request_id);
+/* NRT_ENOTREADY until the request finished; then copies its final potential
+ * (num_elem doubles) and releases it.  Returns the request's solver status. */
+int nrt_server_result(nrt_server *s, int64_t request_id, double *potential);
+/* Blocks until every submitted request has finished (or failed). */
+int nrt_server_drain(nrt_server *s);
+int nrt_server_get_stats(nrt_server *s, nrt_server_stats *st);
+int nrt_server_destroy(nrt_server *s);
 
 #ifdef __cplusplus
 }

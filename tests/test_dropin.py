@@ -45,17 +45,18 @@ def _write_case(path, g, mode, steps, V0=None):
     e = g["eparam"]
     hp = g["hparam"]
     V0 = spec.rest_pot if V0 is None else V0
+    r = lambda x: repr(float(x))  # plain decimal text (numpy 2 reprs carry a type prefix)
     with open(path, "w") as f:
-        f.write(f"{mode} {spec.n} {len(spec.terminals)} {steps} {float(g['dT'])!r} "
-                f"{spec.init_time!r} {spec.end_input!r}\n")
+        f.write(f"{mode} {spec.n} {len(spec.terminals)} {steps} {r(g['dT'])} "
+                f"{r(spec.init_time)} {r(spec.end_input)}\n")
         f.write(" ".join(str(int(t)) for t in spec.terminals) + "\n")
         f.write(f"{len(g['hh_elem'])} " + " ".join(str(int(x)) for x in g["hh_elem"]) + "\n")
         for i in range(spec.n):
-            f.write(f"{spec.mother[i]} {spec.dr[i]} {spec.dl[i]} {spec.branching[i]} "
-                    f"{e[2, i]!r} {e[0, i]!r} {e[1, i]!r} {e[3, i]!r} {e[4, i]!r} "
-                    f"{spec.input_current[i]!r} {V0[i]!r}\n")
+            f.write(f"{int(spec.mother[i])} {int(spec.dr[i])} {int(spec.dl[i])} "
+                    f"{int(spec.branching[i])} {r(e[2, i])} {r(e[0, i])} {r(e[1, i])} "
+                    f"{r(e[3, i])} {r(e[4, i])} {r(spec.input_current[i])} {r(V0[i])}\n")
         for k in range(len(g["hh_elem"])):
-            f.write(" ".join(repr(float(hp[q, k])) for q in range(12)) + "\n")
+            f.write(" ".join(r(hp[q, k]) for q in range(12)) + "\n")
 
 
 @pytest.mark.gpu
