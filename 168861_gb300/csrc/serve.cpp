@@ -24,6 +24,8 @@
 #include <thread>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "neurite_gb300.h"
 
 namespace {
@@ -84,7 +86,12 @@ struct MicroBatch {
   std::vector<char> finished;
   size_t bytes = 0;
   size_t open = 0;
+  int64_t per_tick = 0;            // steps per tick, adapted to the target tick time
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaStream_t stream = nullptr;
 };
+
+constexpr double kTickMs = 10.0;   // target device time of one tick per resident batch
 
 // Device footprint of one tree in a batch (the arena sizes of the engine, rounded up).
 size_t estimate_bytes(const nrt_problem &p, const nrt_options &o) {
@@ -109,7 +116,7 @@ struct nrt_server {
   std::thread worker;
   bool stop = false;
   int64_t next_id = 1;
-  size_t used = 0;
+  size_t used = 0, peak = 0;
   int64_t outstanding = 0;
   nrt_server_stats st{};
   std::vector<double> lat_ms;
@@ -147,8 +154,21 @@ MicroBatch *nrt_server::admit(bool implicit, std::vector<Request *> &batch) {
   mb->finished.assign(batch.size(), 0);
   mb->open = batch.size();
   for (Request *r : batch) mb->bytes += r->bytes;
+  mb->per_tick = cfg.chunk_steps;
+  void *sp = nullptr;
+  nrt_batch_get_stream(mb->b, &sp);
+  mb->stream = (cudaStream_t)sp;
+  cudaEventCreate(&mb->ev0);
+  cudaEventCreate(&mb->ev1);
   st.batches_created++;
   return mb;
+}
+
+static void release(MicroBatch *mb) {
+  if (mb->ev0) cudaEventDestroy(mb->ev0);
+  if (mb->ev1) cudaEventDestroy(mb->ev1);
+  nrt_batch_destroy(mb->b);
+  delete mb;
 }
 
 void nrt_server::loop() {
@@ -173,6 +193,7 @@ void nrt_server::loop() {
         if (r->bytes <= free_bytes && (int)t.size() < cfg.max_batch) {
           free_bytes -= r->bytes;
           used += r->bytes;
+          peak = std::max(peak, used);
           t.push_back(r);
           it = pending.erase(it);
         } else {
@@ -189,12 +210,23 @@ void nrt_server::loop() {
     if (active.empty()) continue;
     const auto t0 = Clock::now();
     // one tick: every resident batch advances on its own stream (all enqueued first)
-    for (MicroBatch *mb : active) nrt_batch_advance(mb->b, cfg.chunk_steps);
+    for (MicroBatch *mb : active) {
+      cudaEventRecord(mb->ev0, mb->stream);
+      nrt_batch_advance(mb->b, mb->per_tick);
+      cudaEventRecord(mb->ev1, mb->stream);
+    }
     // collect finished requests
     std::vector<int64_t> rem;
     for (MicroBatch *mb : active) {
       rem.assign(mb->reqs.size(), 0);
       int rc = nrt_batch_remaining(mb->b, rem.data());
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, mb->ev0, mb->ev1) == cudaSuccess && ms > 0) {
+        // steps per tick toward the target tick time (explicit steps are ~1000x cheaper)
+        const double want = (double)mb->per_tick * kTickMs / ms;
+        mb->per_tick = (int64_t)std::max(1.0, std::min(want, 4.0 * mb->per_tick + 1));
+        mb->per_tick = std::min<int64_t>(mb->per_tick, 1 << 20);
+      }
       nrt_stats bs;
       const bool bad = rc != NRT_OK;
       for (size_t q = 0; q < mb->reqs.size(); q++) {
@@ -224,12 +256,11 @@ void nrt_server::loop() {
     for (size_t a = 0; a < active.size();) {
       MicroBatch *mb = active[a];
       if (mb->open == 0) {
-        nrt_batch_destroy(mb->b);
         {
           std::lock_guard<std::mutex> lk(mu);
           used -= mb->bytes;
         }
-        delete mb;
+        release(mb);
         active.erase(active.begin() + a);
       } else {
         a++;
@@ -325,7 +356,7 @@ int nrt_server_get_stats(nrt_server *s, nrt_server_stats *st) {
   st->p99_ms = pct(0.99);
   st->max_ms = l.empty() ? 0.0 : l.back();
   st->busy_seconds = s->busy;
-  st->peak_bytes = 0;
+  st->peak_bytes = (int64_t)s->peak;
   return NRT_OK;
 }
 

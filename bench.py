@@ -40,7 +40,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "compartment-steps/s"
 WORKLOADS = ("batch-implicit-mixed", "batch-explicit-mixed", "batch-explicit-fp64",
-             "axon-explicit-fp64")
+             "axon-explicit-fp64", "serve")
 DEFAULT_WORKLOAD = "batch-explicit-mixed"
 
 
@@ -291,6 +291,84 @@ def run_ours(args, rank: int, world: int):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------------------------ serving
+
+def serve_requests(count: int, seed: int):
+    """Request stream: Poisson arrivals (mean 2000 req/s); half explicit squid axons of
+    the 1 cm / 1002-element kind, half implicit random trees of the batched population;
+    simulated time U(10, 100) ms."""
+    pkg = importlib.import_module("168861_gb300")
+    model = pkg.model
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / 2000.0, size=count)
+    out = []
+    sizes = model.log_uniform_sizes(count, 1e3, 1e5, seed + 1)
+    for q in range(count):
+        t_ms = rng.uniform(10.0, 100.0)
+        if q % 2 == 0:
+            spec = model.straight_axon(dtf=0.8, tspan=t_ms * 1e-3)
+            d = pkg.derive(spec)
+            dT = pkg.step_size(spec, d)
+            implicit = False
+        else:
+            spec = model.random_tree(seed=seed * 31 + q, n_target=int(sizes[q]), tspan=t_ms * 1e-3)
+            d = pkg.derive(spec)
+            dT = spec.dt_abs
+            implicit = True
+        p = pkg.ProblemArrays.from_spec(spec, d, dT)
+        out.append((float(gaps[q]), p, implicit,
+                    (1, spec.num_steps(dT) - 1, spec.init_time, spec.end_input)))
+    return out
+
+
+def run_serve(args, rank: int, world: int):
+    import torch
+    pkg = importlib.import_module("168861_gb300")
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    count = args.trees or 64
+    reqs = serve_requests(count, args.seed)
+    ex = dict(precision="mixed")
+    im = dict(precision="mixed", restart=20, tol=1e-10, tol_mode="rel", precond="segment",
+              max_iter=1000)
+    # warm-up: one small request of each kind through a throwaway server
+    w = pkg.Server(budget_bytes=8 << 30, explicit_opts=ex, implicit_opts=im)
+    for gap, p, imp, run in reqs[:2]:
+        w.submit(p, imp, run[0], min(run[1], run[0] + 16), run[2], run[3])
+    w.drain()
+    w.close()
+    srv = pkg.Server(budget_bytes=64 << 30, chunk_steps=64, max_wait_us=200,
+                     explicit_opts=ex, implicit_opts=im)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        t0 = time.perf_counter()
+        nxt = t0
+        for gap, p, imp, run in reqs:
+            nxt += gap
+            dt = nxt - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            srv.submit(p, imp, *run)
+        srv.drain()
+        wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    work = float(st.compartment_steps)
+    line = {"metric": "serve compartment-steps/s", "value": work / wall,
+            "unit": "compartment-steps/s", "n_gpus": world, "steps": count, "warmup": 2,
+            "ms_per_step": wall * 1e3 / count, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded requests)",
+            "config": {"workload": "serve", "requests": count, "arrivals": "Poisson 2000/s",
+                       "mix": "50% explicit 1 cm axon (mixed), 50% implicit random tree 1e3-1e5 "
+                              "(mixed GMRES(20)+FP64 refinement)", "sim_time_ms": "U(10,100)"},
+            "p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "max_ms": st.max_ms,
+            "batches": int(st.batches_created), "completed": int(st.completed),
+            "clocks": clk.summary(),
+            "e2e": {"value": work / wall, "unit": "compartment-steps/s",
+                    "h2d_bytes_per_step": sum(sum(a.nbytes for a in r[1].arrays.values())
+                                              for r in reqs) / count,
+                    "d2h_bytes_per_step": sum(r[1].num_elem * 8 for r in reqs) / count}}
+    print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------------ CPU (reference) arm
 
 def _oracle_job(job):
@@ -379,6 +457,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", args.gpus))
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "serve":
+        run_serve(args, rank, world)
     else:
         run_ours(args, rank, world)
 
