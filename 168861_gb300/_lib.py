@@ -15,7 +15,7 @@ NRT_EDEVICE, NRT_EBUDGET, NRT_ESTATE, NRT_ENOTREADY = 5, 6, 7, 8
 NRT_EXPLICIT, NRT_IMPLICIT_BE = 0, 1
 NRT_FP64, NRT_MIXED = 0, 1
 NRT_GMRES, NRT_BICGSTAB = 0, 1
-NRT_PRECOND_NONE, NRT_PRECOND_JACOBI, NRT_PRECOND_SEGMENT = 0, 1, 2
+NRT_PRECOND_NONE, NRT_PRECOND_JACOBI, NRT_PRECOND_SEGMENT, NRT_PRECOND_TREE = 0, 1, 2, 3
 NRT_TOL_ABS, NRT_TOL_REL = 0, 1
 
 _i32p = ctypes.POINTER(ctypes.c_int32)

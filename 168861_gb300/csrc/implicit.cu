@@ -92,6 +92,17 @@ struct ImView {
   int *queue;                     // batch: next index into order
   double *partials;               // kGrid: 2 x gridDim x kMaxDots
   InstStat *stats;
+  // exact tree preconditioner (NRT_PRECOND_TREE): segments in tile order
+  const int *seg_len, *seg_c1, *seg_c2, *seg_prow, *seg_soff;
+  const int *tile_seg;            // segments of tree tile q: [tile_seg[q], tile_seg[q+1])
+  const int *tile_slot;           // staging slots of tree tile q
+  const int *slot_row;            // global row behind each staging slot
+  const int *lev_tile;            // tree tiles of level entry e: [lev_tile[e], lev_tile[e+1])
+  const int *work_lev;            // level entries of a worker (CTA or instance), deepest first
+  void *tinv;                     // T[ntot]: 1 / (eliminated pivot) per row
+  double *exp_d;                  // per segment: g^2 / pivot exported to the parent row
+  void *exp_b;                    // T per segment: g b' / pivot exported to the parent row
+  int tree_cap;                   // staging slots per tree tile
 };
 
 template <typename T>
@@ -197,8 +208,114 @@ struct Ctx {
   ImView iv;
   Work<T> w;
   int64_t r0, r1;   // rows of this CTA (kGrid) or instance (batch)
-  int t0, t1;       // tiles
+  int t0, t1;       // segment-preconditioner tiles
+  int l0, l1;       // tree-preconditioner level entries (deepest first)
 };
+
+template <bool kGrid>
+__device__ __forceinline__ void level_sync(cg::grid_group &grid) {
+  if (kGrid) {
+    __threadfence();
+    grid.sync();
+  } else {
+    __syncthreads();
+  }
+}
+
+// Exact tree factorisation (Hines elimination order, leaves to root): for every segment,
+// the parent rows' pivots absorb g^2 / pivot of their child segments; one thread per
+// segment, the segments of one level at a time, staged in shared memory.
+template <typename T, bool kGrid>
+__device__ void tree_factor(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared &S) {
+  const ImView &iv = c.iv;
+  double *sd = (double *)S.tile;
+  double *sg = sd + iv.tree_cap;
+  T *tinv = (T *)iv.tinv;
+  for (int e = c.l0; e < c.l1; e++) {
+    for (int q = iv.lev_tile[e]; q < iv.lev_tile[e + 1]; q++) {
+      const int s0 = iv.tile_slot[q], s1 = iv.tile_slot[q + 1];
+      for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) {
+        const int r = iv.slot_row[k];
+        sd[k - s0] = iv.diag[r];
+        sg[k - s0] = iv.g64[r];
+      }
+      __syncthreads();
+      for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {
+        const int o = iv.seg_soff[s], L = iv.seg_len[s];
+        double d = sd[o + L - 1];
+        if (iv.seg_c1[s] >= 0) d -= iv.exp_d[iv.seg_c1[s]];
+        if (iv.seg_c2[s] >= 0) d -= iv.exp_d[iv.seg_c2[s]];
+        for (int k = L - 1; k >= 1; k--) {
+          const double inv = 1.0 / d;
+          sd[o + k] = inv;
+          const double gk = sg[o + k];
+          d = sd[o + k - 1] - gk * gk * inv;
+        }
+        const double inv0 = 1.0 / d;
+        sd[o] = inv0;
+        iv.exp_d[s] = iv.seg_prow[s] >= 0 ? sg[o] * sg[o] * inv0 : 0.0;
+      }
+      __syncthreads();
+      for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) tinv[iv.slot_row[k]] = (T)sd[k - s0];
+      __syncthreads();
+    }
+    level_sync<kGrid>(grid);
+  }
+}
+
+// z = A^-1 v (up to rounding) with the factors of tree_factor: elimination of every
+// segment into its parent row, leaves to root, then back-substitution root to leaves.
+template <typename T, bool kGrid>
+__device__ void tree_apply(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared &S, const T *v, T *z) {
+  const ImView &iv = c.iv;
+  T *sb = (T *)S.tile;
+  T *si = sb + iv.tree_cap;
+  T *sg = si + iv.tree_cap;
+  const T *tinv = (const T *)iv.tinv;
+  const T *g = sizeof(T) == 4 ? (const T *)(const void *)iv.gf : (const T *)(const void *)iv.g64;
+  T *exp_b = (T *)iv.exp_b;
+  for (int pass = 0; pass < 2; pass++) {
+    for (int ee = 0; ee < c.l1 - c.l0; ee++) {
+      const int e = pass == 0 ? c.l0 + ee : c.l1 - 1 - ee;  // deepest first, then root first
+      for (int q = iv.lev_tile[e]; q < iv.lev_tile[e + 1]; q++) {
+        const int s0 = iv.tile_slot[q], s1 = iv.tile_slot[q + 1];
+        for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) {
+          const int r = iv.slot_row[k];
+          sb[k - s0] = pass == 0 ? v[r] : z[r];
+          si[k - s0] = tinv[r];
+          sg[k - s0] = g[r];
+        }
+        __syncthreads();
+        for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {
+          const int o = iv.seg_soff[s], L = iv.seg_len[s];
+          if (pass == 0) {
+            T b = sb[o + L - 1];
+            if (iv.seg_c1[s] >= 0) b += exp_b[iv.seg_c1[s]];
+            if (iv.seg_c2[s] >= 0) b += exp_b[iv.seg_c2[s]];
+            sb[o + L - 1] = b;
+            for (int k = L - 1; k >= 1; k--) {
+              b = sb[o + k - 1] + sg[o + k] * b * si[o + k];
+              sb[o + k - 1] = b;
+            }
+            exp_b[s] = iv.seg_prow[s] >= 0 ? sg[o] * sb[o] * si[o] : (T)0;
+          } else {
+            const int pr = iv.seg_prow[s];
+            T x = (sb[o] + (pr >= 0 ? sg[o] * z[pr] : (T)0)) * si[o];
+            sb[o] = x;
+            for (int k = 1; k < L; k++) {
+              x = (sb[o + k] + sg[o + k] * x) * si[o + k];
+              sb[o + k] = x;
+            }
+          }
+        }
+        __syncthreads();
+        for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) z[iv.slot_row[k]] = sb[k - s0];
+        __syncthreads();
+      }
+      level_sync<kGrid>(grid);
+    }
+  }
+}
 
 // (A x)_j for a physical row, FP64 (identity rows yield 0).
 __device__ __forceinline__ double row_apply64(const PackView &pv, const ImView &iv, int64_t j,
@@ -280,8 +397,11 @@ __device__ void factor_pieces(Ctx<T, kGrid> &c, Shared &S) {
 
 // z = M^-1 v over this CTA's rows (identity rows: v and z are 0).
 template <typename T, bool kGrid>
-__device__ void apply_precond(Ctx<T, kGrid> &c, Shared &S, const T *v, T *z) {
-  if (c.iv.precond == NRT_PRECOND_SEGMENT) {
+__device__ void apply_precond(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared &S, const T *v, T *z) {
+  if (c.iv.precond == NRT_PRECOND_TREE) {
+    level_sync<kGrid>(grid);  // v of every row visible (tree tiles span other CTAs' rows)
+    tree_apply(c, grid, S, v, z);
+  } else if (c.iv.precond == NRT_PRECOND_SEGMENT) {
     T *sv = (T *)S.tile;
     T *sd = sv + c.iv.tile_rows;
     T *sc = sd + c.iv.tile_rows;
@@ -392,7 +512,12 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
     Vout[j] = v;
   }
   __syncthreads();
-  if (iv.precond == NRT_PRECOND_SEGMENT) factor_pieces(c, S);
+  if (iv.precond == NRT_PRECOND_SEGMENT) {
+    factor_pieces(c, S);
+  } else if (iv.precond == NRT_PRECOND_TREE) {
+    level_sync<kGrid>(grid);  // diagonal of every row visible before the elimination
+    tree_factor(c, grid, S);
+  }
   double target = iv.tol;
   {
     double acc[kMaxDots];
@@ -421,7 +546,7 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
         acc[0] += r * r;
       }
       __syncthreads();
-      if (res >= 0 && iters < budget) apply_precond(c, S, c.w.Wb, c.w.Z);  // local rows
+      if (iters < budget) apply_precond(c, grid, S, c.w.Wb, c.w.Z);
       group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);         // publishes Z_0
     }
     res = sqrt(S.red[0]);
@@ -499,7 +624,7 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
           }
       }
       __syncthreads();
-      apply_precond(c, S, Wn, c.w.Z + (size_t)(j + 1) * N);
+      apply_precond(c, grid, S, Wn, c.w.Z + (size_t)(j + 1) * N);
       group_reduce<kGrid>(grid, nacc, 1, S, iv.partials, parity);  // publishes Z_{j+1}
       if (threadIdx.x == 0) {
         const double hn = sqrt(S.red[0]);
@@ -589,6 +714,8 @@ __global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView i
     c.r1 = iv.cta_row[blockIdx.x + 1];
     c.t0 = iv.cta_tile[blockIdx.x];
     c.t1 = iv.cta_tile[blockIdx.x + 1];
+    c.l0 = iv.work_lev ? iv.work_lev[blockIdx.x] : 0;
+    c.l1 = iv.work_lev ? iv.work_lev[blockIdx.x + 1] : 0;
     const InstDev in = pv.inst[0];
     const int64_t inst_n = iv.inst_row[1] - iv.inst_row[0];
     for (int s = 0; s < nsteps; s++) {
@@ -611,6 +738,8 @@ __global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView i
       c.r1 = iv.inst_row[inst + 1];
       c.t0 = iv.inst_tile[inst];
       c.t1 = iv.inst_tile[inst + 1];
+      c.l0 = iv.work_lev ? iv.work_lev[inst] : 0;
+      c.l1 = iv.work_lev ? iv.work_lev[inst + 1] : 0;
       const InstDev in = pv.inst[inst];
       int s = 0;
       for (; s < nsteps; s++) {
@@ -658,6 +787,8 @@ size_t Engine::implicit_bytes() const {
   b += al(4 * 4100) * 2 + al(8 * (host.ninst + 1)) + al(4 * (host.ninst + 1)) + al(4 * host.ninst);
   b += al(sizeof(double) * 2 * 4096 * kMaxDots);
   b += al(sizeof(InstStat) * host.ninst) + al(64);
+  if (opt.precond == NRT_PRECOND_TREE)  // schedule arrays, factors, export slots (bounds)
+    b += 12 * al(4 * (N + 8)) + al(tb * N) + al(8 * N) + al(tb * N) + al(4 * (4096 + 8));
   return b;
 }
 
@@ -677,6 +808,122 @@ static int up(Arena &a, X *&dst, const X *src, size_t count, cudaStream_t st) {
     int _rc = (x);                  \
     if (_rc != NRT_OK) return _rc;  \
   } while (0)
+
+// Schedule of the exact tree preconditioner.  Segments are maximal runs of physical rows
+// each linked to the previous row (mother == j - 1), broken after every branch point and
+// at `cap` rows; a segment's parent row (the mother of its first row) is then always the
+// last row of its parent segment.  Level = number of segments above.  Each worker (one
+// CTA of the cooperative launch, or one instance of a batch) gets, per level (deepest
+// first), tiles of whole segments whose rows fit the shared-memory staging area.
+struct TreeSchedule {
+  std::vector<int> seg_len, seg_c1, seg_c2, seg_prow, seg_soff;  // tile order
+  std::vector<int> tile_seg, tile_slot, slot_row, lev_tile, work_lev;
+};
+
+static void build_tree_schedule(const HostPack &host, int cap, bool grid_mode, int ctas,
+                                TreeSchedule &T) {
+  struct Seg {
+    int start, len, prow, parent, level, c1, c2;
+  };
+  std::vector<Seg> segs;
+  std::vector<int> seg_of(host.ntot, -1);
+  std::vector<int> inst_seg(host.ninst + 1, 0);
+  for (int32_t i = 0; i < host.ninst; i++) {
+    const int64_t o = host.off[i], n = host.num_elem[i];
+    int cur = -1;
+    for (int64_t jl = 0; jl < n; jl++) {
+      const int64_t j = o + jl;
+      const Topo &t = host.topo[j];
+      if (t.flags & F_IDENT) {
+        cur = -1;
+        continue;
+      }
+      const bool linked = cur >= 0 && (t.flags & F_UP) && t.mother == j - 1 &&
+                          !(host.topo[j - 1].flags & F_BRANCH) && segs[cur].len < cap;
+      if (linked) {
+        segs[cur].len++;
+      } else {
+        Seg s;
+        s.start = (int)j;
+        s.len = 1;
+        s.prow = (t.flags & F_UP) ? t.mother : -1;
+        s.parent = s.prow >= 0 ? seg_of[s.prow] : -1;
+        s.level = s.parent >= 0 ? segs[s.parent].level + 1 : 0;
+        s.c1 = s.c2 = -1;
+        segs.push_back(s);
+        cur = (int)segs.size() - 1;
+        if (s.parent >= 0) {
+          Seg &p = segs[s.parent];
+          (p.c1 < 0 ? p.c1 : p.c2) = cur;
+        }
+      }
+      seg_of[j] = cur;
+    }
+    inst_seg[i + 1] = (int)segs.size();
+  }
+  // Workers: instances (batch) or CTAs (one tree; each level's segments dealt out to the
+  // CTAs by rows).  Every worker of a cooperative launch sees the same number of levels.
+  const int nwork = grid_mode ? ctas : host.ninst;
+  int max_level = 0;
+  for (const Seg &s : segs) max_level = std::max(max_level, s.level);
+  std::vector<std::vector<std::vector<int>>> lists(nwork);  // [worker][level] -> segments
+  if (grid_mode) {
+    std::vector<std::vector<int>> by_level(max_level + 1);
+    for (int s = 0; s < (int)segs.size(); s++) by_level[segs[s].level].push_back(s);
+    for (int w = 0; w < nwork; w++) lists[w].resize(max_level + 1);
+    for (int L = 0; L <= max_level; L++) {
+      int64_t rows = 0;
+      for (int s : by_level[L]) rows += segs[s].len;
+      int64_t acc = 0;
+      for (int s : by_level[L]) {
+        const int w = (int)std::min<int64_t>(nwork - 1, acc * nwork / std::max<int64_t>(rows, 1));
+        lists[w][L].push_back(s);
+        acc += segs[s].len;
+      }
+    }
+  } else {
+    for (int32_t i = 0; i < host.ninst; i++) {
+      int ml = 0;
+      for (int s = inst_seg[i]; s < inst_seg[i + 1]; s++) ml = std::max(ml, segs[s].level);
+      lists[i].resize(ml + 1);
+      for (int s = inst_seg[i]; s < inst_seg[i + 1]; s++) lists[i][segs[s].level].push_back(s);
+    }
+  }
+  // Emit in (worker, level deepest first, tile) order; renumber segments accordingly.
+  std::vector<int> newid(segs.size(), -1);
+  std::vector<int> order;
+  T.work_lev.assign(nwork + 1, 0);
+  for (int w = 0; w < nwork; w++) {
+    T.work_lev[w] = (int)T.lev_tile.size();
+    for (int L = (int)lists[w].size() - 1; L >= 0; L--) {
+      T.lev_tile.push_back((int)T.tile_seg.size());
+      int used = cap;  // forces a new tile for the first segment
+      for (int s : lists[w][L]) {
+        if (used + segs[s].len > cap) {
+          T.tile_seg.push_back((int)order.size());
+          T.tile_slot.push_back((int)T.slot_row.size());
+          used = 0;
+        }
+        newid[s] = (int)order.size();
+        order.push_back(s);
+        T.seg_soff.push_back(used);
+        for (int k = 0; k < segs[s].len; k++) T.slot_row.push_back(segs[s].start + k);
+        used += segs[s].len;
+      }
+    }
+  }
+  T.work_lev[nwork] = (int)T.lev_tile.size();
+  T.lev_tile.push_back((int)T.tile_seg.size());
+  T.tile_seg.push_back((int)order.size());
+  T.tile_slot.push_back((int)T.slot_row.size());
+  for (int s : order) {
+    const Seg &g = segs[s];
+    T.seg_len.push_back(g.len);
+    T.seg_prow.push_back(g.prow);
+    T.seg_c1.push_back(g.c1 >= 0 ? newid[g.c1] : -1);
+    T.seg_c2.push_back(g.c2 >= 0 ? newid[g.c2] : -1);
+  }
+}
 
 // Groups pieces [pa, pb) into tiles whose row span fits the shared-memory staging area.
 static void make_tiles(const std::vector<int2> &pieces, int pa, int pb, int tile_rows,
@@ -866,6 +1113,30 @@ int Engine::implicit_init() {
   TRYI(up(arena, iv.partials, (const double *)nullptr, (size_t)2 * 4096 * kMaxDots, st));
   std::vector<InstStat> zero(ni, InstStat{0, 0, 0, 0.0});
   TRYI(up(arena, iv.stats, zero.data(), ni, st));
+  iv.work_lev = nullptr;
+  if (opt.precond == NRT_PRECOND_TREE) {
+    TreeSchedule T;
+    iv.tree_cap = (int)(kTileBytes / (3 * sizeof(double)));
+    build_tree_schedule(host, iv.tree_cap, S.grid_mode, S.grid_blocks, T);
+    TRYI(up(arena, pi, T.seg_len.data(), T.seg_len.size(), st)); iv.seg_len = pi;
+    TRYI(up(arena, pi, T.seg_c1.data(), T.seg_c1.size(), st)); iv.seg_c1 = pi;
+    TRYI(up(arena, pi, T.seg_c2.data(), T.seg_c2.size(), st)); iv.seg_c2 = pi;
+    TRYI(up(arena, pi, T.seg_prow.data(), T.seg_prow.size(), st)); iv.seg_prow = pi;
+    TRYI(up(arena, pi, T.seg_soff.data(), T.seg_soff.size(), st)); iv.seg_soff = pi;
+    TRYI(up(arena, pi, T.tile_seg.data(), T.tile_seg.size(), st)); iv.tile_seg = pi;
+    TRYI(up(arena, pi, T.tile_slot.data(), T.tile_slot.size(), st)); iv.tile_slot = pi;
+    TRYI(up(arena, pi, T.slot_row.data(), T.slot_row.size(), st)); iv.slot_row = pi;
+    TRYI(up(arena, pi, T.lev_tile.data(), T.lev_tile.size(), st)); iv.lev_tile = pi;
+    TRYI(up(arena, pi, T.work_lev.data(), T.work_lev.size(), st)); iv.work_lev = pi;
+    const size_t nseg = std::max<size_t>(1, T.seg_len.size());
+    iv.tinv = arena.take(tb * N);
+    iv.exp_b = arena.take(tb * nseg);
+    TRYI(up(arena, iv.exp_d, (const double *)nullptr, nseg, st));
+    if (!iv.tinv || !iv.exp_b) {
+      set_error("arena exhausted (tree preconditioner)");
+      return NRT_ENOMEM;
+    }
+  }
   NRT_CUDA(cudaStreamSynchronize(st));
   return NRT_OK;
 }

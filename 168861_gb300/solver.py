@@ -22,7 +22,7 @@ from ._lib import check
 _PREC = {"fp64": _lib.NRT_FP64, "mixed": _lib.NRT_MIXED}
 _KRY = {"gmres": _lib.NRT_GMRES, "bicgstab": _lib.NRT_BICGSTAB}
 _PC = {"none": _lib.NRT_PRECOND_NONE, "jacobi": _lib.NRT_PRECOND_JACOBI,
-       "segment": _lib.NRT_PRECOND_SEGMENT}
+       "segment": _lib.NRT_PRECOND_SEGMENT, "tree": _lib.NRT_PRECOND_TREE}
 
 
 @dataclasses.dataclass

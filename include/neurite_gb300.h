@@ -56,8 +56,11 @@ typedef enum nrt_krylov {
 typedef enum nrt_precond {
   NRT_PRECOND_NONE = 0,
   NRT_PRECOND_JACOBI = 1,    /* diagonal scaling */
-  NRT_PRECOND_SEGMENT = 2    /* exact tridiagonal solve of every unbranched segment
+  NRT_PRECOND_SEGMENT = 2,   /* exact tridiagonal solve of every unbranched segment
                                 (block Jacobi with the branch-point couplings cut) */
+  NRT_PRECOND_TREE = 3       /* exact solve of the whole tree (Hines elimination, parallel
+                                over the segments of each branch level); GMRES then needs
+                                about one iteration per refinement cycle */
 } nrt_precond;
 
 typedef enum nrt_tol_mode {
@@ -259,6 +262,7 @@ int nrt_server_result(nrt_server *s, int64_t request_id, double *potential);
 int nrt_server_drain(nrt_server *s);
 int nrt_server_get_stats(nrt_server *s, nrt_server_stats *st);
 int nrt_server_destroy(nrt_server *s);
+
 
 #ifdef __cplusplus
 }

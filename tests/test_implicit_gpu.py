@@ -33,7 +33,7 @@ def tight(**kw):
 
 
 @pytest.mark.parametrize("name", golden_names("i"))
-@pytest.mark.parametrize("precond", ["segment", "jacobi"])
+@pytest.mark.parametrize("precond", ["segment", "jacobi", "tree"])
 def test_implicit_fp64_matches_exact_solution(gpu, pkg, orc, name, precond):
     g = load_golden(name)
     spec = g["spec"]
@@ -100,11 +100,12 @@ def test_implicit_dropin_loop_equals_device_loop(gpu, pkg):
     np.testing.assert_array_equal(a.snapshot(), b.snapshot())
 
 
-def test_implicit_large_tree_cooperative(gpu, pkg, orc, model):
+@pytest.mark.parametrize("precond", ["segment", "tree"])
+def test_implicit_large_tree_cooperative(gpu, pkg, orc, model, precond):
     """~6.5e4-element tree on the whole-GPU cooperative kernel vs the exact solution."""
     spec = model.random_binary_tree(depth=8, seed=5, dt=2.5e-5, tspan=5e-3)
     steps = 20
-    s = pkg.SolverIm(pkg.ProblemArrays.from_spec(spec, pkg.derive(spec)), **tight())
+    s = pkg.SolverIm(pkg.ProblemArrays.from_spec(spec, pkg.derive(spec)), **tight(precond=precond))
     s.run(1, 1 + steps, spec.init_time, spec.end_input)
     d = orc.derive(spec)
     Vo, _, _, _ = orc.implicit_run(spec, d, spec.dt_abs, 1, 1 + steps, linsolve=0)
@@ -123,13 +124,14 @@ def test_implicit_mixed_precision(gpu, pkg, orc):
     assert s.stats().nonconverged_steps == 0
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_implicit_batch_alone_equals_in_mix(gpu, pkg, orc, model, precision):
+@pytest.mark.parametrize("precision,precond", [("fp64", "segment"), ("mixed", "segment"),
+                                               ("fp64", "tree"), ("mixed", "tree")])
+def test_implicit_batch_alone_equals_in_mix(gpu, pkg, orc, model, precision, precond):
     """Uneven trees in one persistent block-per-instance launch give what each gives alone."""
     specs = [model.random_tree(seed=s, n_target=n, dt=2.5e-5, tspan=1e-3)
              for s, n in [(1, 1500), (2, 6000), (3, 900), (4, 3000)]]
-    opts = tight() if precision == "fp64" else dict(precision="mixed", restart=20, tol=1e-10,
-                                                     tol_mode="rel")
+    opts = tight(precond=precond) if precision == "fp64" else dict(
+        precision="mixed", restart=20, tol=1e-10, tol_mode="rel", precond=precond)
     probs = [pkg.ProblemArrays.from_spec(sp, pkg.derive(sp)) for sp in specs]
     b = pkg.Batch(probs, mode=1, **opts)
     steps = [25, 40, 10, 33]
@@ -162,3 +164,15 @@ def test_implicit_budget_exhaustion_reported(gpu, pkg):
     assert e.value.status == 4
     assert not np.array_equal(s.snapshot(), V0)
     assert s.stats().nonconverged_steps == 1
+
+
+def test_tree_preconditioner_needs_few_iterations(gpu, pkg, model):
+    """With the exact tree solve as preconditioner, each FP64 GMRES solve needs about one
+    iteration per refinement cycle, whatever the branching."""
+    spec = model.random_tree(seed=5, n_target=20000, dt=2.5e-5, tspan=1e-3)
+    prob = pkg.ProblemArrays.from_spec(spec, pkg.derive(spec))
+    s = pkg.SolverIm(prob, **tight(precond="tree"))
+    s.run(1, 21, spec.init_time, spec.end_input)
+    st = s.stats()
+    assert st.nonconverged_steps == 0
+    assert st.krylov_iters <= 20 * 3
