@@ -80,7 +80,7 @@ EXPORTS = (
     "nrt_batch_create", "nrt_batch_set_runs", "nrt_batch_advance", "nrt_batch_synchronize", "nrt_batch_get_stream",
     "nrt_batch_snapshot", "nrt_batch_remaining", "nrt_batch_get_stats", "nrt_batch_destroy",
     "nrt_server_create", "nrt_server_submit", "nrt_server_result", "nrt_server_drain",
-    "nrt_server_get_stats", "nrt_server_destroy",
+    "nrt_server_get_stats", "nrt_server_destroy", "nrt_solve_csr_static",
 )
 
 _lib = None
@@ -130,6 +130,9 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "nrt_server_drain": [vp],
         "nrt_server_get_stats": [vp, ctypes.POINTER(ServerStats)],
         "nrt_server_destroy": [vp],
+        "nrt_solve_csr_static": [ctypes.c_int32, vp, vp, vp, vp, vp, ctypes.c_int32,
+                                 ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp,
+                                 ctypes.POINTER(ctypes.c_int32), _f64p],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

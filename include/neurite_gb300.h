@@ -263,6 +263,41 @@ int nrt_server_drain(nrt_server *s);
 int nrt_server_get_stats(nrt_server *s, nrt_server_stats *st);
 int nrt_server_destroy(nrt_server *s);
 
+/* ----------------------------------------------------------------------------------
+ * Allocation-free solve.  No counterpart in the reference: it exists for callers that
+ * cannot call cudaMalloc -- a host application that owns the device memory pool and
+ * forbids other allocators, a loop that must not allocate once it runs, or a plugin that
+ * is handed pre-allocated device buffers only.
+ *
+ * Solves A x = b for one tree's backward-Euler system in the reference's CSR layout
+ * (row_ptr[n+1], col, val -- what nrt_export_system returns, copied to device memory by
+ * the caller).  Method: FP64 right-preconditioned GMRES(restart) with an exact
+ * tridiagonal solve of fixed 64-row blocks as the preconditioner.  Stops on
+ * ||b - A x||_2 <= tol (NRT_TOL_ABS) or <= tol * ||b||_2 (NRT_TOL_REL, with ||b|| taken over
+ * the rows that have off-diagonal entries: decoupled rows such as the reference's identity
+ * rows are solved exactly and would otherwise dominate it), or after max_iter iterations
+ * (0 -> n; then NRT_ENOCONV, x still holds the last iterate).
+ * All array pointers are DEVICE memory; x holds the initial guess on entry and the
+ * solution on return.  The call is asynchronous only up to the final read of the
+ * iteration count: it returns after the work on `stream` (a cudaStream_t; NULL = legacy
+ * default stream) has finished.
+ *
+ * Memory: nothing is allocated, by this function or by anything it calls.  Every
+ * temporary lives in one static device array of NRT_STATIC_SCRATCH_BYTES, present on
+ * every GPU that loads the library until the process exits.  It must hold
+ * n * (2*restart + 5) + 2*1024*(NRT_STATIC_MAX_RESTART + 1) + 4 doubles (about 110,000 rows
+ * at restart 16, 180,000 at restart 8); larger systems are refused with NRT_EBUDGET.
+ * The first call on a device looks up the array's device address (a one-time set-up with
+ * that device current), so make that first call before any stream capture.
+ * Every call shares the one array and leaves its contents behind; each region is written
+ * before it is read within a call, so nothing needs clearing, but calls that overlap on the
+ * GPU (other streams or host threads without ordering) race on it. */
+#define NRT_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
+#define NRT_STATIC_MAX_RESTART 16
+int nrt_solve_csr_static(int32_t n, const int32_t *row_ptr, const int32_t *col,
+                         const double *val, const double *b, double *x, int32_t restart,
+                         double tol, int32_t tol_mode, int32_t max_iter, void *stream,
+                         int32_t *iters_out, double *residual_out);
 
 #ifdef __cplusplus
 }
