@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the CPU baseline leg (profiling runs)")
+    ap.add_argument("--precond", default="tree", choices=("tree", "segment", "jacobi"),
+                    help="implicit workloads: GMRES preconditioner")
     return ap.parse_args()
 
 
@@ -208,7 +210,7 @@ def run_ours(args, rank: int, world: int):
     t_build = time.time() - t_build
     opts = dict(precision=precision)
     if implicit:
-        opts.update(krylov="gmres", restart=20, tol=1e-10, tol_mode="rel", precond="segment",
+        opts.update(krylov="gmres", restart=20, tol=1e-10, tol_mode="rel", precond=args.precond,
                     max_iter=1000)
     mode = pkg._lib.NRT_IMPLICIT_BE if implicit else pkg._lib.NRT_EXPLICIT
     # loop ranges long enough for warm-up + timed steps
@@ -328,7 +330,7 @@ def run_serve(args, rank: int, world: int):
     count = args.trees or 64
     reqs = serve_requests(count, args.seed)
     ex = dict(precision="mixed")
-    im = dict(precision="mixed", restart=20, tol=1e-10, tol_mode="rel", precond="segment",
+    im = dict(precision="mixed", restart=20, tol=1e-10, tol_mode="rel", precond=args.precond,
               max_iter=1000)
     # warm-up: one small request of each kind through a throwaway server
     w = pkg.Server(budget_bytes=8 << 30, explicit_opts=ex, implicit_opts=im)
