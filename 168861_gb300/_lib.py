@@ -79,6 +79,7 @@ EXPORTS = (
     "nrt_get_stats", "nrt_destroy", "nrt_status_string", "nrt_last_error", "nrt_derive",
     "nrt_batch_create", "nrt_batch_set_runs", "nrt_batch_advance", "nrt_batch_synchronize", "nrt_batch_get_stream",
     "nrt_batch_snapshot", "nrt_batch_remaining", "nrt_batch_get_stats", "nrt_batch_destroy",
+    "nrt_batch_instance_stats",
     "nrt_server_create", "nrt_server_submit", "nrt_server_result", "nrt_server_drain",
     "nrt_server_get_stats", "nrt_server_destroy", "nrt_solve_csr_static",
 )
@@ -122,6 +123,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "nrt_batch_remaining": [vp, _i64p],
         "nrt_batch_get_stats": [vp, ctypes.POINTER(Stats)],
         "nrt_batch_destroy": [vp],
+        "nrt_batch_instance_stats": [vp, _i64p, ctypes.POINTER(ctypes.c_int32),
+                                     ctypes.POINTER(ctypes.c_int32), _f64p],
         "nrt_server_create": [ctypes.POINTER(ServerConfig), ctypes.POINTER(Options),
                               ctypes.POINTER(Options), vpp],
         "nrt_server_submit": [vp, ctypes.POINTER(Problem), ctypes.c_int,

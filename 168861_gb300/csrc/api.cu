@@ -697,6 +697,13 @@ int nrt_batch_get_stats(nrt_batch *b, nrt_stats *st) {
   return b->eng.get_stats(st);
 }
 
+int nrt_batch_instance_stats(nrt_batch *b, int64_t *iters, int32_t *last_iters,
+                             int32_t *nonconverged, double *last_residual) {
+  if (!b) return nrt::fail(NRT_EINVAL, "null batch");
+  NRT_CUDA(cudaSetDevice(b->eng.device));
+  return nrt::instance_stats(b->eng, iters, last_iters, nonconverged, last_residual);
+}
+
 int nrt_batch_destroy(nrt_batch *b) {
   delete b;
   return NRT_OK;

@@ -1179,6 +1179,24 @@ int implicit_advance(Engine &e, int64_t steps) {
   return NRT_OK;
 }
 
+int instance_stats(Engine &e, int64_t *iters, int32_t *last_iters, int32_t *nonconv,
+                   double *last_res) {
+  const int32_t ni = e.host.ninst;
+  std::vector<InstStat> s(ni, InstStat{0, 0, 0, 0.0});
+  if (e.im) {
+    NRT_CUDA(cudaMemcpyAsync(s.data(), e.im->iv.stats, sizeof(InstStat) * ni,
+                             cudaMemcpyDeviceToHost, e.stream));
+    NRT_CUDA(cudaStreamSynchronize(e.stream));
+  }
+  for (int32_t i = 0; i < ni; i++) {
+    if (iters) iters[i] = s[i].iters;
+    if (last_iters) last_iters[i] = s[i].last_iters;
+    if (nonconv) nonconv[i] = s[i].nonconv;
+    if (last_res) last_res[i] = s[i].last_res;
+  }
+  return NRT_OK;
+}
+
 // Sum of non-converged steps over all instances (-1 on a device error).
 int64_t nonconverged_total(Engine &e) {
   if (!e.im) return 0;

@@ -280,6 +280,18 @@ class Batch:
         check(self.lib.nrt_batch_get_stats(self.h, ctypes.byref(st)), "nrt_batch_get_stats")
         return st
 
+    def instance_stats(self) -> dict:
+        """Per-instance Krylov statistics (implicit): iters, last_iters, nonconverged,
+        last_residual."""
+        it = np.zeros(self.count, np.int64)
+        li = np.zeros(self.count, np.int32)
+        nc = np.zeros(self.count, np.int32)
+        lr = np.zeros(self.count)
+        check(self.lib.nrt_batch_instance_stats(self.h, _p(it, ctypes.c_int64),
+                                                _p(li, ctypes.c_int32), _p(nc, ctypes.c_int32),
+                                                _p(lr, ctypes.c_double)), "nrt_batch_instance_stats")
+        return dict(iters=it, last_iters=li, nonconverged=nc, last_residual=lr)
+
     def close(self) -> None:
         if getattr(self, "h", None):
             self.lib.nrt_batch_destroy(self.h)

@@ -219,6 +219,11 @@ int nrt_batch_snapshot(nrt_batch *b, int32_t instance, double *potential);
 /* Number of loop iterations still to run per instance (count entries). */
 int nrt_batch_remaining(nrt_batch *b, int64_t *remaining);
 int nrt_batch_get_stats(nrt_batch *b, nrt_stats *st);
+/* Per-instance Krylov statistics (implicit): total iterations, iterations of the last
+ * step, non-converged steps and the last step's residual; arrays of `count` entries,
+ * any of which may be NULL. */
+int nrt_batch_instance_stats(nrt_batch *b, int64_t *iters, int32_t *last_iters,
+                             int32_t *nonconverged, double *last_residual);
 int nrt_batch_destroy(nrt_batch *b);
 
 /* ----------------------------------------------------------------------------------
