@@ -206,6 +206,7 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
     in.dT = p.dT;
     in.t0 = 0;
     in.t1 = -1;
+    set_window(in);
     hp.inst[i] = in;
   }
   return NRT_OK;
@@ -529,6 +530,7 @@ int nrt_run(nrt_solver *s, int64_t i_begin, int64_t i_end, double init_time, dou
   in.iend = i_end;
   in.t0 = init_time;
   in.t1 = end_input;
+  nrt::set_window(in);
   e.host.inst[0] = in;
   NRT_CUDA(cudaMemcpyAsync(e.pv.inst, &e.host.inst[0], sizeof(in), cudaMemcpyHostToDevice, e.stream));
   const bool implicit = e.opt.mode == NRT_IMPLICIT_BE;
@@ -646,6 +648,7 @@ int nrt_batch_set_runs(nrt_batch *b, const nrt_instance_run *runs) {
     e.host.inst[i].iend = runs[i].i_end;
     e.host.inst[i].t0 = runs[i].init_time;
     e.host.inst[i].t1 = runs[i].end_input;
+    nrt::set_window(e.host.inst[i]);
   }
   NRT_CUDA(cudaMemcpyAsync(e.pv.inst, e.host.inst.data(), sizeof(nrt::InstDev) * e.pv.ninst,
                            cudaMemcpyHostToDevice, e.stream));

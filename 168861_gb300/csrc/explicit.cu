@@ -34,8 +34,8 @@ namespace {
 
 __device__ __forceinline__ bool input_on(const InstDev &in, int64_t i, int force) {
   if (force >= 0) return force != 0;
-  const double t = (double)i * in.dT;   // time_run = i * dT, src/neurite.cpp:227
-  return (t >= in.t0) && (t <= in.t1);  // src/neurite.cpp:230
+  // t0 <= i*dT <= t1 (src/neurite.cpp:227-230), precomputed as loop-index bounds
+  return i >= in.ion && i <= in.ioff;
 }
 
 __device__ __forceinline__ int64_t ghost_source(const Topo &t, int64_t j) {

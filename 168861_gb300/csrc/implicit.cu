@@ -509,7 +509,7 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
     if (active) b += iv.inp64[j];
     iv.rhs[j] = b;
     bacc += b * b;
-    Vout[j] = v;
+    Vout[j] = 2.0 * v - Vout[j];  // x0: linear extrapolation from V^{n-1} (held in Vout)
   }
   __syncthreads();
   if (iv.precond == NRT_PRECOND_SEGMENT) {
@@ -545,9 +545,7 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
         c.w.Wb[j] = (T)r;
         acc[0] += r * r;
       }
-      __syncthreads();
-      if (iters < budget) apply_precond(c, grid, S, c.w.Wb, c.w.Z);
-      group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);         // publishes Z_0
+      group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);
     }
     res = sqrt(S.red[0]);
     if (res <= target) {
@@ -555,6 +553,8 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
       break;
     }
     if (iters >= budget) break;
+    apply_precond(c, grid, S, c.w.Wb, c.w.Z);
+    group_sync<kGrid>(grid);  // Z_0 of every row visible before the SpMV
     if (threadIdx.x == 0) {
       S.g[0] = res;
       for (int i = 1; i <= m; i++) S.g[i] = 0;
@@ -722,7 +722,7 @@ __global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView i
       const int64_t i = in.base + s;
       if (i >= in.iend) break;
       const bool active = force >= 0 ? force != 0
-                                     : ((double)i * in.dT >= in.t0 && (double)i * in.dT <= in.t1);
+                                     : (i >= in.ion && i <= in.ioff);
       implicit_one_step<T, kGrid>(c, grid, S, parity, ((cur + s) & 1) ? V1 : V0,
                                   ((cur + s + 1) & 1) ? V1 : V0, active, inst_n, 0);
     }
@@ -746,7 +746,7 @@ __global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView i
         const int64_t i = in.base + s;
         if (i >= in.iend) break;
         const bool active = force >= 0 ? force != 0
-                                       : ((double)i * in.dT >= in.t0 && (double)i * in.dT <= in.t1);
+                                       : (i >= in.ion && i <= in.ioff);
         implicit_one_step<T, kGrid>(c, grid, S, parity, ((cur + s) & 1) ? V1 : V0,
                                     ((cur + s + 1) & 1) ? V1 : V0, active, c.r1 - c.r0, inst);
       }
@@ -1116,7 +1116,8 @@ int Engine::implicit_init() {
   iv.work_lev = nullptr;
   if (opt.precond == NRT_PRECOND_TREE) {
     TreeSchedule T;
-    iv.tree_cap = (int)(kTileBytes / (3 * sizeof(double)));
+    // staging slots: the factorisation stages two FP64 rows, a solve three T rows
+    iv.tree_cap = (int)(kTileBytes / std::max<size_t>(2 * sizeof(double), 3 * tb));
     build_tree_schedule(host, iv.tree_cap, S.grid_mode, S.grid_blocks, T);
     TRYI(up(arena, pi, T.seg_len.data(), T.seg_len.size(), st)); iv.seg_len = pi;
     TRYI(up(arena, pi, T.seg_c1.data(), T.seg_c1.size(), st)); iv.seg_c1 = pi;

@@ -43,7 +43,31 @@ struct InstDev {
   int64_t iend;     // one past the last loop index
   double dT;
   double t0, t1;    // stimulus window
+  int64_t ion, ioff;  // loop indices i with t0 <= i*dT <= t1 (the window as integers)
 };
+
+// Fills ion/ioff so that (ion <= i && i <= ioff) == (t0 <= i*dT && i*dT <= t1) for every
+// loop index i, evaluating the reference's own test (src/neurite.cpp:227-230) at the bounds.
+inline void set_window(InstDev &in) {
+  auto on = [&](int64_t i) { const double t = (double)i * in.dT; return t >= in.t0; };
+  auto below = [&](int64_t i) { const double t = (double)i * in.dT; return t <= in.t1; };
+  const double lim = 9.0e15;
+  double a = in.t0 / in.dT, b = in.t1 / in.dT;
+  if (!(a == a) || !(b == b) || in.t1 < in.t0) {
+    in.ion = 1;
+    in.ioff = 0;
+    return;
+  }
+  a = a < -lim ? -lim : (a > lim ? lim : a);
+  b = b < -lim ? -lim : (b > lim ? lim : b);
+  int64_t i0 = (int64_t)a, i1 = (int64_t)b;
+  while (on(i0 - 1)) i0--;
+  while (!on(i0)) i0++;
+  while (!below(i1) && i1 > i0 - 1) i1--;
+  while (below(i1 + 1)) i1++;
+  in.ion = i0;
+  in.ioff = i1;
+}
 
 // Device-side view passed by value to the kernels.
 struct PackView {
