@@ -439,6 +439,7 @@ int nro_implicit_run(int n, const int32_t *ispec, const double *eparam, const do
       int its = 0;
       rc = nro_gmres(n, row_ptr, col, val, currT, sol, 150, 1e-14, n, &its);
       kit += its;
+      if (rc == NRO_ENOCONV && linsolve == 2) rc = NRO_OK;
       memcpy(currT, sol, sizeof(double) * n);
     }
     if (rc) goto out;

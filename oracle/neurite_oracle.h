@@ -68,7 +68,9 @@ int nro_gmres(int n, const int32_t *row_ptr, const int32_t *col, const double *v
               const double *b, double *x, int restart, double tol, int max_it, int *iters_out);
 
 /* Implicit run: SolverImCPU::update + calculate (src/solverIm-cpu.cpp:307-370) per step.
- * linsolve = 0: exact tree solve; 1: GMRES(min(150,n)) with ||r|| <= 1e-14, x0 = 0.
+ * linsolve = 0: exact tree solve; 1: GMRES(min(150,n)) with ||r|| <= 1e-14, x0 = 0;
+ * 2: as 1, but a step that reaches the n-iteration limit keeps its last iterate and the
+ * run goes on (the reference program exits there instead, src/solverIm-cpu.cpp:247-250).
  * V [n] is the latest potential (the reference's prevT), Vother [n] its second buffer
  * (currT), which supplies the right-hand side of the rows the reference never writes. */
 int nro_implicit_run(int n, const int32_t *ispec, const double *eparam, const double *input_on,
