@@ -7,6 +7,7 @@
 #include <memory>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "nrt_internal.h"
@@ -147,6 +148,7 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
       if (p.branching[j]) f |= F_BRANCH;
       if (is_term[j]) f |= F_TERM;
       if (j == p.terminals[0]) f |= F_ROOT;
+      if (p.input[j] != 0.0) f |= F_INP;
       // Flux through a terminal neighbour is zero when that terminal copies this element.
       auto src_of = [&](int32_t t_) { return t_ == p.terminals[0] ? t_ + 1 : p.mother[t_]; };
       if (!is_term[j]) {
@@ -209,6 +211,78 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
     set_window(in);
     hp.inst[i] = in;
   }
+  // One parameter column per instance when every HH element of each instance carries
+  // the same parameters (then the step reads them from a small, cached table).
+  hp.hp_inst = true;
+  for (int32_t i = 0; i < count && hp.hp_inst; i++) {
+    const int64_t a = hp.hh_off[i], b = hp.hh_off[i + 1];
+    for (int64_t k = a + 1; k < b && hp.hp_inst; k++) {
+      const int64_t e0 = hp.off[i] + hp.hh_local[a], e = hp.off[i] + hp.hh_local[k];
+      for (int r = 0; r < HP_ROWS; r++)
+        if (memcmp(&hp.hp[(size_t)r * N + e0], &hp.hp[(size_t)r * N + e], sizeof(double)) != 0) {
+          hp.hp_inst = false;
+          break;
+        }
+    }
+  }
+  if (hp.hp_inst) {
+    std::vector<double> tab((size_t)HP_ROWS * count, 0.0);
+    for (int32_t i = 0; i < count; i++) {
+      if (hp.hh_off[i + 1] == hp.hh_off[i]) continue;
+      const int64_t e0 = hp.off[i] + hp.hh_local[hp.hh_off[i]];
+      for (int r = 0; r < HP_ROWS; r++) tab[(size_t)r * count + i] = hp.hp[(size_t)r * N + e0];
+    }
+    hp.hp.swap(tab);
+    hp.hp_ld = count;
+    return NRT_OK;
+  }
+  // Otherwise: distinct parameter sets (consecutive elements mostly share one).
+  struct Key {
+    double v[HP_ROWS];
+    bool operator==(const Key &o) const { return memcmp(v, o.v, sizeof(v)) == 0; }
+  };
+  struct KeyHash {
+    size_t operator()(const Key &k) const {
+      uint64_t h = 1469598103934665603ull;
+      const unsigned char *b = (const unsigned char *)k.v;
+      for (size_t q = 0; q < sizeof(k.v); q++) h = (h ^ b[q]) * 1099511628211ull;
+      return (size_t)h;
+    }
+  };
+  std::unordered_map<Key, uint32_t, KeyHash> ids;
+  std::vector<uint32_t> cls(N, 0);
+  std::vector<Key> keys;
+  Key prev{};
+  uint32_t prev_id = UINT32_MAX;
+  for (int32_t i = 0; i < count; i++) {
+    for (int64_t k = hp.hh_off[i]; k < hp.hh_off[i + 1]; k++) {
+      const int64_t e = hp.off[i] + hp.hh_local[k];
+      Key key;
+      for (int r = 0; r < HP_ROWS; r++) key.v[r] = hp.hp[(size_t)r * N + e];
+      if (prev_id == UINT32_MAX || !(key == prev)) {
+        auto it = ids.find(key);
+        if (it == ids.end()) {
+          it = ids.emplace(key, (uint32_t)keys.size()).first;
+          keys.push_back(key);
+        }
+        prev = key;
+        prev_id = it->second;
+      }
+      cls[e] = prev_id;
+    }
+    if ((int64_t)keys.size() * 4 > N) break;
+  }
+  if ((int64_t)keys.size() * 4 > N || keys.empty()) {
+    hp.hp_ld = N;
+    return NRT_OK;
+  }
+  const size_t nc = keys.size();
+  std::vector<double> tab((size_t)HP_ROWS * nc);
+  for (size_t c = 0; c < nc; c++)
+    for (int r = 0; r < HP_ROWS; r++) tab[(size_t)r * nc + c] = keys[c].v[r];
+  hp.hp.swap(tab);
+  hp.hp_cls.swap(cls);
+  hp.hp_ld = (int64_t)nc;
   return NRT_OK;
 }
 
@@ -262,11 +336,17 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   // Sizes: V x2, topo, coefficient rows, gates, HH rows, instances, terminals, implicit.
   size_t bytes = 2 * al(8 * N) + al(sizeof(Topo) * N) + al(sizeof(InstDev) * count) +
                  al(8 * host.terms.size() + 8);
+  const size_t hpn = (size_t)HP_ROWS * host.hp_ld;
+  if (!host.hp_cls.empty()) bytes += al(4 * N);
   if (mixed)
-    bytes += 7 * al(4 * N) + al(4 * 3 * N) + al(4 * (size_t)HP_ROWS * N);
+    bytes += 7 * al(4 * N) + al(4 * 3 * N) + al(4 * hpn);
   else
-    bytes += 5 * al(8 * N) + al(8 * 3 * N) + al(8 * (size_t)HP_ROWS * N);
-  if (opt.mode == NRT_IMPLICIT_BE) bytes += implicit_bytes();
+    bytes += 5 * al(8 * N) + al(8 * 3 * N) + al(8 * hpn);
+  if (opt.mode == NRT_IMPLICIT_BE) {
+    size_t ib = 0;
+    TRY(implicit_plan(ib));
+    bytes += ib;
+  }
   TRY(arena.reserve(bytes + 4096));
   cudaStream_t st = stream;
   TRY(upload(arena, V[0], host.V0.data(), N, st));
@@ -285,6 +365,14 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   TRY(upload(arena, terms, host.terms.data(), host.terms.size(), st));
   pv.ntot = N;
   pv.ninst = count;
+  pv.hp_ld = host.hp_ld;
+  pv.hp_inst = host.hp_inst ? 1 : 0;
+  pv.hp_cls = nullptr;
+  if (!host.hp_cls.empty()) {
+    uint32_t *pc = nullptr;
+    TRY(upload(arena, pc, host.hp_cls.data(), N, st));
+    pv.hp_cls = pc;
+  }
   pv.topo = topo;
   pv.inst = inst;
   if (mixed) {
@@ -300,7 +388,7 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
     TRY(upload(arena, p, f32(host.kdx), N, st)); pv.kdxf = p;
     TRY(upload(arena, p, f32(host.inp), N, st)); pv.inpf = p;
     TRY(upload(arena, p, f32(host.gate), 3 * N, st)); pv.gatef = p;
-    TRY(upload(arena, p, f32(host.hp), (size_t)HP_ROWS * N, st)); pv.hpf = p;
+    TRY(upload(arena, p, f32(host.hp), hpn, st)); pv.hpf = p;
   } else {
     double *p;
     TRY(upload(arena, p, host.cdt.data(), N, st)); pv.cdt = p;
@@ -309,7 +397,7 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
     TRY(upload(arena, p, host.kdx.data(), N, st)); pv.kdx = p;
     TRY(upload(arena, p, host.inp.data(), N, st)); pv.inp = p;
     TRY(upload(arena, p, host.gate.data(), 3 * N, st)); pv.gate = p;
-    TRY(upload(arena, p, host.hp.data(), (size_t)HP_ROWS * N, st)); pv.hp = p;
+    TRY(upload(arena, p, host.hp.data(), hpn, st)); pv.hp = p;
   }
   if (opt.mode == NRT_IMPLICIT_BE) TRY(implicit_init());
   NRT_CUDA(cudaStreamSynchronize(st));

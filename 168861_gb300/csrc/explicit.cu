@@ -56,22 +56,23 @@ __global__ void __launch_bounds__(256) explicit_step_f64(PackView p, int k, int 
     return;
   }
   const int64_t N = p.ntot;
-  const double *hp = p.hp;
   const bool term = (tj.flags & F_TERM) != 0;
   if (term && !(tj.flags & F_HH)) return;
   const double v = Vin[(kGeneral || !term) ? j : ghost_source(tj, j)];
   double wdx = 0, kdx = 0;
   if (tj.flags & F_HH) {
+    const int64_t L = p.hp_ld;
+    const double *hp = p.hp + hp_col(p, j, tj.flags >> INST_SHIFT);
     GateStep64 g = hh_step64(v, p.gate[j], p.gate[N + j], p.gate[2 * N + j],
-                             hp[HP_LSNA * N + j], hp[HP_LSK * N + j], hp[HP_REST * N + j],
-                             hp[HP_DTMS * N + j], hp[HP_GNA * N + j], hp[HP_GK * N + j],
-                             hp[HP_GL * N + j], hp[HP_ENA * N + j], hp[HP_EK * N + j],
-                             hp[HP_EL * N + j]);
+                             hp[HP_LSNA * L], hp[HP_LSK * L], hp[HP_REST * L],
+                             hp[HP_DTMS * L], hp[HP_GNA * L], hp[HP_GK * L],
+                             hp[HP_GL * L], hp[HP_ENA * L], hp[HP_EK * L],
+                             hp[HP_EL * L]);
     p.gate[j] = g.m;
     p.gate[N + j] = g.h;
     p.gate[2 * N + j] = g.n;
     if (term) return;  // ghost: only its gates move
-    const double dx = hp[HP_DX * N + j];
+    const double dx = hp[HP_DX * L];
     wdx = g.W * dx;
     kdx = g.K * dx;
   } else {
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(256) explicit_step_f64(PackView p, int k, int 
   if (!skip_mo) acc = acc + (Vin[tj.mother] - v) * p.gax[j];
   acc = acc + wdx * v;
   acc = acc + kdx;
-  if (active) acc = acc + p.inp[j];
+  if (active && (tj.flags & F_INP)) acc = acc + p.inp[j];  // adding a zero input is exact
   Vout[j] = v + p.cdt[j] * acc;
 }
 
@@ -116,23 +117,24 @@ __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, in
     return;
   }
   const int64_t N = p.ntot;
-  const float *hp = p.hpf;
   const bool term = (tj.flags & F_TERM) != 0;
   if (term && !(tj.flags & F_HH)) return;
   const int64_t self = (kGeneral || !term) ? j : ghost_source(tj, j);
   const float vf = Fin[self];
   float wdx, kdx;
   if (tj.flags & F_HH) {
-    const float dv = vf - hp[HP_REST * N + j];
-    GateStep32 g = hh_step32(dv + hp[HP_LSNA * N + j], dv + hp[HP_LSK * N + j], p.gatef[j],
-                             p.gatef[N + j], p.gatef[2 * N + j], hp[HP_DTMS * N + j],
-                             hp[HP_GNA * N + j], hp[HP_GK * N + j], hp[HP_GL * N + j],
-                             hp[HP_ENA * N + j], hp[HP_EK * N + j], hp[HP_EL * N + j]);
+    const int64_t L = p.hp_ld;
+    const float *hp = p.hpf + hp_col(p, j, tj.flags >> INST_SHIFT);
+    const float dv = vf - hp[HP_REST * L];
+    GateStep32 g = hh_step32(dv + hp[HP_LSNA * L], dv + hp[HP_LSK * L], p.gatef[j],
+                             p.gatef[N + j], p.gatef[2 * N + j], hp[HP_DTMS * L],
+                             hp[HP_GNA * L], hp[HP_GK * L], hp[HP_GL * L],
+                             hp[HP_ENA * L], hp[HP_EK * L], hp[HP_EL * L]);
     p.gatef[j] = g.m;
     p.gatef[N + j] = g.h;
     p.gatef[2 * N + j] = g.n;
     if (term) return;
-    const float dx = hp[HP_DX * N + j];
+    const float dx = hp[HP_DX * L];
     wdx = g.W * dx;
     kdx = g.K * dx;
   } else {
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, in
   if (kGeneral || !(tj.flags & F_DR_TERM)) acc = fmaf(Fin[tj.dr] - vf, p.gaxf[tj.dr], acc);
   if (kGeneral || !(tj.flags & F_MO_TERM)) acc = fmaf(Fin[tj.mother] - vf, p.gaxf[j], acc);
   acc = fmaf(wdx, vf, acc) + kdx;
-  if (active) acc += p.inpf[j];
+  if (active && (tj.flags & F_INP)) acc += p.inpf[j];
   const double vn = Vin[j] + (double)(p.cdtf[j] * acc);
   Vout[j] = vn;
   Fout[j] = (float)vn;

@@ -7,7 +7,7 @@
 // (src/solverIm-cpu.cpp:29-183):
 //
 //   row j (physical):  -g_j V_mother + d_j V_j - g_DR V_DR - b_j g_DL V_DL = rhs_j
-//   d_j   = c_m dX/dT - W dX + b_j g_DL + [DR column] g_DR + [mother column] g_j
+//   d_j   = c_j + b_j g_DL + [DR column] g_DR + [mother column] g_j,  c_j = c_m dX/dT - W dX
 //   rhs_j = c_m dX V^n_j/dT + K dX + I_j,      g_x = 1/(r_a dX)_x
 //
 // with the reference's sealed ends: row 1 has no mother column, a row whose next element
@@ -19,17 +19,22 @@
 // off-diagonals.  nrt_export_system expands it to the reference's CSR layout.
 //
 // Solver: right-preconditioned GMRES(m) (Saad), classical Gram-Schmidt, Givens
-// rotations.  The preconditioner is an exact tridiagonal (Thomas) solve of every
-// unbranched segment piece (<= kMaxPiece rows): only the branch-point couplings are left
-// to the Krylov iteration.  Each cycle starts from the true FP64 residual b - A x, so in
-// mixed precision (FP32 basis, SpMV, orthogonalisation update and preconditioner) every
-// restart is one step of iterative refinement.  Inner products and norms: per-thread
-// partial sums in the basis precision over the thread's rows, then FP64 across threads
-// and CTAs in a fixed order (deterministic, identical in every CTA).  Warm start x0 = V^n.
+// rotations.  Each cycle starts from the true FP64 residual b - A x, so in mixed precision
+// (FP32 basis, SpMV, orthogonalisation update and preconditioner) every restart is one
+// step of iterative refinement.  Inner products and norms: per-thread partial sums in the
+// basis precision over the thread's rows, then FP64 across threads and CTAs in a fixed
+// order (deterministic, identical in every CTA).  Initial guess: V^n extrapolated
+// linearly from V^{n-1}.
 //
-// Memory-level parallelism: the SpMV is fused with all j+1 Gram-Schmidt products (one
-// pass over the rows, register accumulators), the update and the norm share a pass, and
-// the sequential Thomas sweeps run on tiles of rows staged in shared memory.
+// Preconditioners: the exact tree factorisation (Hines order, see tree_factor), an exact
+// tridiagonal solve of every unbranched segment piece, Jacobi, or none.
+//
+// Memory-level parallelism: every row loop keeps several rows per thread in flight and
+// issues all of a row's independent loads before it uses any: a compact per-row flag
+// byte replaces the topology record, the neighbours j-1 and j+1 are loaded speculatively
+// (the mother is j-1 except on the first row of a DL child), and only the rare rows with
+// a far neighbour make a second, dependent load.  The SpMV is fused with up to kG
+// Gram-Schmidt products; the update and the norm share a pass.
 //
 // Two launch shapes from one template:
 //  * kGrid  (one tree): a cooperative launch over the whole GPU; rows are split into
@@ -56,7 +61,22 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kMaxPiece = 256;                 // longest segment piece one sweep handles
 constexpr int kMaxDots = kMaxRestart + 1;
 constexpr int kTileBytes = 48 * 1024;          // shared-memory staging for the sweeps
-constexpr int kU = 4;                          // rows per thread kept in flight in row loops
+constexpr int kTileFlagBytes = 4096;           // tree tiles: one flag byte per slot
+constexpr int kU = 4;                          // rows per thread in flight: SpMV + products
+constexpr int kV = 8;                          // rows per thread in flight: streaming passes
+constexpr int kA = 1;                          // rows per thread in flight: assembly
+constexpr int kR = 4;                          // rows per thread in flight: FP64 residual
+constexpr int kG = 8;                          // Gram-Schmidt products per pass over the rows
+
+// Per-row flags of the implicit system (ImView::rowf).
+enum : uint8_t {
+  R_IDENT = 1,   // identity row
+  R_UP = 2,      // column at the mother
+  R_DOWNR = 4,   // column at DR == j + 1
+  R_DOWNL = 8,   // column at DL
+  R_FAR = 16,    // the mother is not j - 1 (first row of a DL child)
+  R_HH = 32,     // Hodgkin_Huxley element
+};
 
 struct InstStat {
   int64_t iters;
@@ -73,7 +93,8 @@ struct ImView {
   double tol;
   int max_iter;      // per step per instance; 0 -> instance size; < 0 -> assembly only
   int ninst;
-  int tile_rows;     // rows per shared-memory tile
+  int tile_rows;     // rows per shared-memory tile (segment preconditioner)
+  const uint8_t *rowf;
   const double *cmdt;  // c_m dX / dT
   const double *g64;   // 1 / (r_a dX)
   const float *gf;
@@ -92,17 +113,21 @@ struct ImView {
   int *queue;                     // batch: next index into order
   double *partials;               // kGrid: 2 x gridDim x kMaxDots
   InstStat *stats;
-  // exact tree preconditioner (NRT_PRECOND_TREE): segments in tile order
+  // exact tree preconditioner (NRT_PRECOND_TREE).  Segments in tile order; per-slot
+  // arrays in slot order (slots: the rows of a worker's segments, level by level, deepest
+  // level first; every tile starts on a multiple of 4 slots, padding slots have row -1).
+  void *cdiag;                    // T[ntot]: c_j, written by the assembly
   const int *seg_len, *seg_c1, *seg_c2, *seg_prow, *seg_soff;
   const int *tile_seg;            // segments of tree tile q: [tile_seg[q], tile_seg[q+1])
-  const int *tile_slot;           // staging slots of tree tile q
-  const int *slot_row;            // global row behind each staging slot
+  const int *tile_slot;           // slots of tree tile q: [tile_slot[q], tile_slot[q+1])
+  const int *srow;                // row behind each slot (-1: padding)
+  const uint8_t *sflag;           // SL_* flags per slot
   const int *lev_tile;            // tree tiles of level entry e: [lev_tile[e], lev_tile[e+1])
   const int *work_lev;            // level entries of a worker (CTA or instance), deepest first
-  void *tinv;                     // T[ntot]: 1 / (eliminated pivot) per row
-  double *exp_d;                  // per segment: g^2 / pivot exported to the parent row
-  void *exp_b;                    // T per segment: g b' / pivot exported to the parent row
-  int tree_cap;                   // staging slots per tree tile
+  const void *sg;                 // T per slot: conductance to the mother (0 without a column)
+  void *sinv, *se, *sy;           // T per slot: 1 / pivot, g / pivot, eliminated right side
+  void *exp_d, *exp_b;            // T per segment: what it passes to its parent row
+  int tree_cap;                   // staging slots per tree tile (multiple of 4)
 };
 
 template <typename T>
@@ -120,6 +145,12 @@ struct Shared {
 __host__ __device__ inline size_t shared_fixed_bytes(int m) {
   return sizeof(double) * ((size_t)(m + 1) * m + 2 * m + 2 * (m + 1) + m + kMaxDots +
                            kWarps * kMaxDots + kMaxDots) + 16;
+}
+
+// The dynamic shared memory of the launch.
+__device__ __forceinline__ double *dyn_smem() {
+  extern __shared__ __align__(16) double nrt_dyn_smem[];
+  return nrt_dyn_smem;
 }
 
 __device__ Shared carve(double *base, int m) {
@@ -142,12 +173,12 @@ __device__ Shared carve(double *base, int m) {
 
 // Reduces the first k register accumulators of every thread over the CTA into out[0..k)
 // (FP64, fixed order: warp shuffle tree, then warps in index order).
-template <typename T>
-__device__ __forceinline__ void block_reduce(const T (&acc)[kMaxDots], int k, double *warp_part,
+template <typename T, int kN>
+__device__ __forceinline__ void block_reduce(const T (&acc)[kN], int k, double *warp_part,
                                              double *out) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-  for (int i = 0; i < kMaxDots; i++) {
+  for (int i = 0; i < kN; i++) {
     if (i < k) {
       double v = (double)acc[i];
       for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -183,11 +214,13 @@ __device__ void grid_finish(cg::grid_group &grid, int k, double *cta_sums, doubl
   __syncthreads();
 }
 
-template <bool kGrid, typename T>
-__device__ __forceinline__ void group_reduce(cg::grid_group &grid, const T (&acc)[kMaxDots], int k,
-                                             Shared &S, double *partials, int &parity) {
-  block_reduce(acc, k, S.warp, S.red);
-  if (kGrid) grid_finish(grid, k, S.red, partials, parity);
+// Sums k accumulators over the group into S.red[off .. off + k).
+template <bool kGrid, typename T, int kN>
+__device__ __forceinline__ void group_reduce(cg::grid_group &grid, const T (&acc)[kN], int k,
+                                             Shared &S, double *partials, int &parity,
+                                             int off = 0) {
+  block_reduce(acc, k, S.warp, S.red + off);
+  if (kGrid) grid_finish(grid, k, S.red + off, partials, parity);
 }
 
 template <bool kGrid>
@@ -200,12 +233,63 @@ __device__ __forceinline__ void group_sync(cg::grid_group &grid) {
   }
 }
 
-// ---------------------------------------------------------------- kernel body
+// ---------------------------------------------------------------- row kernels
+
+// (A x)_r for the kN rows r = rb + u * stride (rows >= r1 give 0, flag R_IDENT).  D / G:
+// diagonal and conductance arrays (FP32 or FP64), x the vector.  All independent loads of
+// the kN rows are issued before any use.
+template <int kN, typename C, typename X>
+__device__ __forceinline__ void apply_rows(const PackView &pv, const ImView &iv,
+                                           const C *__restrict__ D, const C *__restrict__ G,
+                                           const X *x, int64_t rb, int64_t stride, int64_t r1,
+                                           X (&out)[kN], uint8_t (&fl)[kN]) {
+  const int64_t N = pv.ntot;
+  C dg[kN], gm[kN], gp[kN];
+  X xs[kN], xm[kN], xp[kN];
+#pragma unroll
+  for (int u = 0; u < kN; u++) {
+    const int64_t r = rb + u * stride;
+    const bool ok = r < r1;
+    const int64_t rm = r > 0 ? r - 1 : r, rp = r + 1 < N ? r + 1 : r;
+    fl[u] = ok ? iv.rowf[r] : (uint8_t)R_IDENT;
+    dg[u] = ok ? D[r] : (C)0;
+    gm[u] = ok ? G[r] : (C)0;
+    gp[u] = ok ? G[rp] : (C)0;
+    xs[u] = ok ? x[r] : (X)0;
+    xm[u] = ok ? x[rm] : (X)0;
+    xp[u] = ok ? x[rp] : (X)0;
+  }
+#pragma unroll
+  for (int u = 0; u < kN; u++) {
+    const uint8_t f = fl[u];
+    X s = 0;
+    if (!(f & R_IDENT)) {
+      X mo = xm[u], xl = 0;
+      C gl = 0;
+      if (f & (R_FAR | R_DOWNL)) {
+        const Topo t = pv.topo[rb + u * stride];
+        if (f & R_FAR) mo = x[t.mother];
+        if (f & R_DOWNL) {
+          gl = G[t.dl];
+          xl = x[t.dl];
+        }
+      }
+      s = dg[u] * xs[u];
+      if (f & R_UP) s -= gm[u] * mo;
+      if (f & R_DOWNR) s -= gp[u] * xp[u];
+      if (f & R_DOWNL) s -= gl * xl;
+    }
+    out[u] = s;
+  }
+}
+
+// ---------------------------------------------------------------- kernel context
 
 template <typename T, bool kGrid>
 struct Ctx {
-  PackView pv;
-  ImView iv;
+  // device-memory copies of the launch's views: phases read the fields they need
+  const PackView *pv;
+  const ImView *iv;
   Work<T> w;
   int64_t r0, r1;   // rows of this CTA (kGrid) or instance (batch)
   int t0, t1;       // segment-preconditioner tiles
@@ -217,138 +301,420 @@ __device__ __forceinline__ void level_sync(cg::grid_group &grid) {
   if (kGrid) {
     __threadfence();
     grid.sync();
-  } else {
-    __syncthreads();
   }
 }
 
-// Exact tree factorisation (Hines elimination order, leaves to root): for every segment,
-// the parent rows' pivots absorb g^2 / pivot of their child segments; one thread per
-// segment, the segments of one level at a time, staged in shared memory.
+// ---------------------------------------------------------------- tree preconditioner
+//
+// Exact factorisation of the tree matrix in Hines order (leaves to root), written for
+// the input conductance eta of the subtree below each row: with d_k = g_k + eta_k (g_k
+// the conductance to the mother, 0 on a row without that column),
+//
+//   eta_k = c_k + sum over children ch of g_ch eta_ch / (g_ch + eta_ch),
+//
+// which is d_k = D_k - sum g_ch^2 / d_ch rewritten without the cancellation between D_k
+// and the children's terms (every term is positive), so the pivots keep full relative
+// precision in FP32.  Per slot it stores inv_k = 1 / d_k and e_k = g_k / d_k; a segment
+// passes e_first * eta_first (= g eta / (g + eta)) to its parent row.  Solve: elimination
+// y_k = v_k + e_{k+1} y_{k+1} leaves to root, then x_k = inv_k y_k + e_k x_mother root to
+// leaves.
+//
+// Work order: the segments of one level at a time (deepest first for the factorisation
+// and the elimination), tile by tile through shared memory.  Inside a tile the
+// recurrences along the segments run as segmented parallel scans over all the tile's
+// slots, so a long unbranched cable costs a few scan rounds, not one thread walking it:
+// the elimination and the substitution are first-order affine recurrences (maps
+// y -> A + M y compose associatively), and the pivot recurrence is a Moebius map of eta,
+// i.e. a product of 2x2 matrices acting on (p, q) with eta = p / q, normalised by powers
+// of two as it goes.
+
+enum : uint8_t { SL_FIRST = 1, SL_LAST = 2, SL_PAD = 4 };  // slot flags (ImView::sflag)
+
+// Contiguous copy of `count` T values from src[s0 ..] into shared memory in 16-byte
+// chunks (s0 is 4-aligned; the slot arrays are padded so the rounded tail stays in bounds).
+template <typename T>
+__device__ __forceinline__ void stage_contig(T *dst, const T *src, int s0, int count) {
+  const int n16 = (int)(((size_t)count * sizeof(T) + 15) >> 4);
+  const uint4 *s = reinterpret_cast<const uint4 *>(src + s0);
+  uint4 *d = reinterpret_cast<uint4 *>(dst);
+  for (int q = threadIdx.x; q < n16; q += 4 * blockDim.x) {
+    uint4 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int qq = q + u * blockDim.x;
+      if (qq < n16) v[u] = s[qq];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int qq = q + u * blockDim.x;
+      if (qq < n16) d[qq] = v[u];
+    }
+  }
+}
+
+// dst[k] = src[srow[s0 + k]] (0 for padding slots).
+template <typename T>
+__device__ __forceinline__ void stage_gather(T *dst, const int *srow, const T *src, int s0,
+                                             int count) {
+  for (int k = threadIdx.x; k < count; k += 8 * blockDim.x) {
+    int r[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const int kk = k + u * blockDim.x;
+      r[u] = kk < count ? srow[s0 + kk] : -1;
+    }
+    T v[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) v[u] = r[u] >= 0 ? src[r[u]] : (T)0;
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const int kk = k + u * blockDim.x;
+      if (kk < count) dst[kk] = v[u];
+    }
+  }
+}
+
+// Slot flags from src[s0 ..] in 4-byte words (s0 is a multiple of 4, so the words are
+// aligned; the flag array is padded past its last slot).
+__device__ __forceinline__ void stage_flags(uint8_t *dst, const uint8_t *src, int s0, int count) {
+  const int n4 = (count + 3) >> 2;
+  const uint32_t *s = reinterpret_cast<const uint32_t *>(src + s0);
+  uint32_t *d = reinterpret_cast<uint32_t *>(dst);
+  for (int q = threadIdx.x; q < n4; q += blockDim.x) d[q] = s[q];
+}
+
+template <typename T>
+__device__ __forceinline__ void store_contig(T *dst, const T *src, int s0, int count) {
+  for (int k = threadIdx.x; k < count; k += blockDim.x) dst[s0 + k] = src[k];
+}
+
+// dst[srow[s0 + k]] = src[k] for the real slots.
+template <typename T>
+__device__ __forceinline__ void scatter_rows(T *dst, const int *srow, const T *src, int s0,
+                                             int count) {
+  for (int k = threadIdx.x; k < count; k += 4 * blockDim.x) {
+    int r[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int kk = k + u * blockDim.x;
+      r[u] = kk < count ? srow[s0 + kk] : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (r[u] >= 0) dst[r[u]] = src[k + u * blockDim.x];
+  }
+}
+
+// The contiguous run of slots thread t owns in a tile scan.  The run length is odd, so
+// the threads of a warp touch distinct shared-memory banks.
+__device__ __forceinline__ void scan_run(int cnt, int &k0, int &k1) {
+  const int R = ((cnt + (int)blockDim.x - 1) / (int)blockDim.x) | 1;
+  k0 = min(cnt, (int)threadIdx.x * R);
+  k1 = min(cnt, k0 + R);
+}
+
+// Segmented first-order recurrence over a tile's slots, in place in a[]:
+//   kDesc:  y_k = a_k + m_k y_{k+1}, k = cnt-1 .. 0 (nothing enters the top)
+//   !kDesc: y_k = a_k + m_k y_{k-1}, k = 0 .. cnt-1
+// with m_k = link(k) (0 where a segment starts in scan order).  Each thread composes the
+// maps of its run, a warp shuffle scan and one pass over the warps give every run its
+// entering value, and the run is then evaluated.  scratch: 3 * warps T values.
+// Links of the two solve recurrences: elimination (descending) uses e_{k+1} unless slot k
+// ends its segment; substitution (ascending) uses e_k unless slot k starts one.
+template <typename T, bool kDesc>
+struct SlotLink {
+  const T *e;
+  const uint8_t *f;
+  __device__ __forceinline__ T operator()(int k) const {
+    if (kDesc) return (f[k] & SL_LAST) ? (T)0 : e[k + 1];
+    return (f[k] & SL_FIRST) ? (T)0 : e[k];
+  }
+};
+
+template <typename T, bool kDesc>
+__device__ __noinline__ void tile_affine_scan(T *a, int cnt, SlotLink<T, kDesc> link, T *scratch) {
+  int k0, k1;
+  scan_run(cnt, k0, k1);
+  T A = 0, M = 1;  // the run's map y_in -> A + M y_in
+  if (kDesc) {
+    for (int k = k1 - 1; k >= k0; k--) {
+      const T m = link(k);
+      A = a[k] + m * A;
+      M = m * M;
+    }
+  } else {
+    for (int k = k0; k < k1; k++) {
+      const T m = link(k);
+      A = a[k] + m * A;
+      M = m * M;
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int sl = kDesc ? 31 - lane : lane;  // position in scan order inside the warp
+  T iA = A, iM = M;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int src = (kDesc ? lane + off : lane - off) & 31;
+    const T pA = __shfl_sync(0xffffffffu, iA, src), pM = __shfl_sync(0xffffffffu, iM, src);
+    if (sl >= off) {  // (this part) after (the earlier part)
+      iA = iA + iM * pA;
+      iM = iM * pM;
+    }
+  }
+  const int prv = (kDesc ? lane + 1 : lane - 1) & 31;
+  T eA = __shfl_sync(0xffffffffu, iA, prv), eM = __shfl_sync(0xffffffffu, iM, prv);
+  if (sl == 0) {
+    eA = 0;
+    eM = 1;
+  }
+  if (sl == 31) {
+    scratch[2 * w] = iA;
+    scratch[2 * w + 1] = iM;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T y = 0;
+    for (int q = 0; q < nw; q++) {
+      const int ww = kDesc ? nw - 1 - q : q;
+      scratch[2 * nw + ww] = y;
+      y = scratch[2 * ww] + scratch[2 * ww + 1] * y;
+    }
+  }
+  __syncthreads();
+  T y = eA + eM * scratch[2 * nw + w];
+  if (kDesc) {
+    for (int k = k1 - 1; k >= k0; k--) {
+      y = a[k] + link(k) * y;
+      a[k] = y;
+    }
+  } else {
+    for (int k = k0; k < k1; k++) {
+      y = a[k] + link(k) * y;
+      a[k] = y;
+    }
+  }
+  __syncthreads();
+}
+
+// 2x2 matrices and vectors of the pivot recurrence, scaled by powers of two.
+template <typename T>
+struct Mob {
+  T a, b, c, d;  // [[a, b], [c, d]]
+};
+
+template <typename T>
+__device__ __forceinline__ T pow2_scale_of(T m) {
+  int e;
+  frexp(m, &e);
+  return ldexp((T)1, -e);
+}
+
+template <typename T>
+__device__ __forceinline__ Mob<T> mob_mul(const Mob<T> &x, const Mob<T> &y) {  // x * y
+  Mob<T> r{x.a * y.a + x.b * y.c, x.a * y.b + x.b * y.d, x.c * y.a + x.d * y.c,
+           x.c * y.b + x.d * y.d};
+  const T m = fmax(fmax(r.a, r.b), fmax(r.c, r.d));  // entries are non-negative
+  if (m > (T)0) {
+    const T s = pow2_scale_of(m);
+    r.a *= s;
+    r.b *= s;
+    r.c *= s;
+    r.d *= s;
+  }
+  return r;
+}
+
+// Per-slot map of the pivot recurrence.  The vector entering slot k is (a, b) with
+// a / b = g_{k+1} eta_{k+1} / (g_{k+1} + eta_{k+1}) when slot k+1 continues the segment;
+// the slot forms (p, q) = (a + c b, b) (or (c b, b) at a segment's last slot, where c
+// already holds the children's terms), eta_k = p / q, and passes (g p, p + g q) on.
+template <typename T>
+__device__ __forceinline__ Mob<T> slot_map(T c, T g, uint8_t f) {
+  if (f & SL_PAD) return Mob<T>{1, 0, 0, 1};
+  if (f & SL_LAST) return Mob<T>{0, g * c, 0, c + g};
+  return Mob<T>{g, g * c, 1, c + g};
+}
+
+// One tile of the factorisation: sc = c (in) -> 1/pivot, sg = g -> e = g / pivot,
+// sh -> e * eta; scratch: 12 * warps T values.
+template <typename T>
+__device__ __noinline__ void tile_factor_scan(T *sc, T *sg, T *sh, const uint8_t *sf, int cnt,
+                                              T *scratch) {
+  int k0, k1;
+  scan_run(cnt, k0, k1);
+  Mob<T> P{1, 0, 0, 1};  // the run's map, scan order = descending slots
+  for (int k = k1 - 1; k >= k0; k--) P = mob_mul(slot_map(sc[k], sg[k], sf[k]), P);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int sl = 31 - lane;
+  Mob<T> I = P;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int src = (lane + off) & 31;
+    Mob<T> Q{__shfl_sync(0xffffffffu, I.a, src), __shfl_sync(0xffffffffu, I.b, src),
+             __shfl_sync(0xffffffffu, I.c, src), __shfl_sync(0xffffffffu, I.d, src)};
+    if (sl >= off) I = mob_mul(I, Q);
+  }
+  const int prv = (lane + 1) & 31;
+  Mob<T> E{__shfl_sync(0xffffffffu, I.a, prv), __shfl_sync(0xffffffffu, I.b, prv),
+           __shfl_sync(0xffffffffu, I.c, prv), __shfl_sync(0xffffffffu, I.d, prv)};
+  if (sl == 0) E = Mob<T>{1, 0, 0, 1};
+  if (sl == 31) {
+    scratch[4 * w] = I.a;
+    scratch[4 * w + 1] = I.b;
+    scratch[4 * w + 2] = I.c;
+    scratch[4 * w + 3] = I.d;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // vector entering each warp; (0, 1) enters the tile's top slot
+    T va = 0, vb = 1;
+    for (int q = nw - 1; q >= 0; q--) {
+      scratch[4 * nw + 2 * q] = va;
+      scratch[4 * nw + 2 * q + 1] = vb;
+      const T na = scratch[4 * q] * va + scratch[4 * q + 1] * vb;
+      const T nb = scratch[4 * q + 2] * va + scratch[4 * q + 3] * vb;
+      const T s = pow2_scale_of(fmax(na, nb));
+      va = na * s;
+      vb = nb * s;
+    }
+  }
+  __syncthreads();
+  T va = scratch[4 * nw + 2 * w], vb = scratch[4 * nw + 2 * w + 1];
+  {
+    const T na = E.a * va + E.b * vb, nb = E.c * va + E.d * vb;
+    const T s = pow2_scale_of(fmax(na, nb));
+    va = na * s;
+    vb = nb * s;
+  }
+  for (int k = k1 - 1; k >= k0; k--) {
+    const uint8_t f = sf[k];
+    const T c = sc[k], g = sg[k];
+    if (f & SL_PAD) {
+      sc[k] = 0;
+      sg[k] = 0;
+      sh[k] = 0;
+      continue;
+    }
+    const T p = (f & SL_LAST) ? c * vb : va + c * vb;
+    const T eta = p / vb;
+    const T inv = (T)1 / (g + eta);
+    const T e = g * inv;
+    sc[k] = inv;
+    sg[k] = e;
+    sh[k] = e * eta;
+    const T na = g * p, nb = p + g * vb;
+    const T s = pow2_scale_of(fmax(na, nb));
+    va = na * s;
+    vb = nb * s;
+  }
+  __syncthreads();
+}
+
 template <typename T, bool kGrid>
-__device__ void tree_factor(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared &S) {
-  const ImView &iv = c.iv;
-  double *sd = (double *)S.tile;
-  double *sg = sd + iv.tree_cap;
-  T *tinv = (T *)iv.tinv;
+__device__ __noinline__ void tree_factor(Ctx<T, kGrid> c) {
+  const ImView &iv = *c.iv;
+  cg::grid_group grid = cg::this_grid();
+  Shared S = carve(dyn_smem(), iv.m);
+  T *sc = (T *)S.tile;
+  T *sgg = sc + iv.tree_cap;
+  T *sh = sgg + iv.tree_cap;
+  uint8_t *sf = (uint8_t *)(sh + iv.tree_cap);
+  T *scratch = (T *)S.warp;
+  const T *cdiag = (const T *)iv.cdiag;
+  T *exp_d = (T *)iv.exp_d;
   for (int e = c.l0; e < c.l1; e++) {
     for (int q = iv.lev_tile[e]; q < iv.lev_tile[e + 1]; q++) {
-      const int s0 = iv.tile_slot[q], s1 = iv.tile_slot[q + 1];
-      for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) {
-        const int r = iv.slot_row[k];
-        sd[k - s0] = iv.diag[r];
-        sg[k - s0] = iv.g64[r];
-      }
+      const int s0 = iv.tile_slot[q], cnt = iv.tile_slot[q + 1] - s0;
+      stage_gather(sc, iv.srow, cdiag, s0, cnt);
+      stage_contig(sgg, (const T *)iv.sg, s0, cnt);
+      stage_flags(sf, iv.sflag, s0, cnt);
       __syncthreads();
       for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {
-        const int o = iv.seg_soff[s], L = iv.seg_len[s];
-        double d = sd[o + L - 1];
-        if (iv.seg_c1[s] >= 0) d -= iv.exp_d[iv.seg_c1[s]];
-        if (iv.seg_c2[s] >= 0) d -= iv.exp_d[iv.seg_c2[s]];
-        for (int k = L - 1; k >= 1; k--) {
-          const double inv = 1.0 / d;
-          sd[o + k] = inv;
-          const double gk = sg[o + k];
-          d = sd[o + k - 1] - gk * gk * inv;
-        }
-        const double inv0 = 1.0 / d;
-        sd[o] = inv0;
-        iv.exp_d[s] = iv.seg_prow[s] >= 0 ? sg[o] * sg[o] * inv0 : 0.0;
+        const int last = iv.seg_soff[s] + iv.seg_len[s] - 1;
+        const int c1 = iv.seg_c1[s], c2 = iv.seg_c2[s];
+        T add = 0;
+        if (c1 >= 0) add += exp_d[c1];
+        if (c2 >= 0) add += exp_d[c2];
+        sc[last] += add;
       }
       __syncthreads();
-      for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) tinv[iv.slot_row[k]] = (T)sd[k - s0];
+      tile_factor_scan(sc, sgg, sh, sf, cnt, scratch);
+      for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x)
+        exp_d[s] = sh[iv.seg_soff[s]];  // 0 when the first row has no mother column
+      store_contig((T *)iv.sinv, sc, s0, cnt);
+      store_contig((T *)iv.se, sgg, s0, cnt);
       __syncthreads();
     }
     level_sync<kGrid>(grid);
   }
 }
 
-// z = A^-1 v (up to rounding) with the factors of tree_factor: elimination of every
-// segment into its parent row, leaves to root, then back-substitution root to leaves.
+// z = A^-1 v (up to rounding) with the factors of tree_factor.
 template <typename T, bool kGrid>
-__device__ void tree_apply(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared &S, const T *v, T *z) {
-  const ImView &iv = c.iv;
-  T *sb = (T *)S.tile;
-  T *si = sb + iv.tree_cap;
-  T *sg = si + iv.tree_cap;
-  const T *tinv = (const T *)iv.tinv;
-  const T *g = sizeof(T) == 4 ? (const T *)(const void *)iv.gf : (const T *)(const void *)iv.g64;
+__device__ __noinline__ void tree_apply(Ctx<T, kGrid> c, const T *v, T *z) {
+  const ImView &iv = *c.iv;
+  cg::grid_group grid = cg::this_grid();
+  Shared S = carve(dyn_smem(), iv.m);
+  T *sa = (T *)S.tile;
+  T *sb = sa + iv.tree_cap;
+  T *sd = sb + iv.tree_cap;
+  uint8_t *sf = (uint8_t *)(sd + iv.tree_cap);
+  T *scratch = (T *)S.warp;
   T *exp_b = (T *)iv.exp_b;
-  for (int pass = 0; pass < 2; pass++) {
-    for (int ee = 0; ee < c.l1 - c.l0; ee++) {
-      const int e = pass == 0 ? c.l0 + ee : c.l1 - 1 - ee;  // deepest first, then root first
-      for (int q = iv.lev_tile[e]; q < iv.lev_tile[e + 1]; q++) {
-        const int s0 = iv.tile_slot[q], s1 = iv.tile_slot[q + 1];
-        for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) {
-          const int r = iv.slot_row[k];
-          sb[k - s0] = pass == 0 ? v[r] : z[r];
-          si[k - s0] = tinv[r];
-          sg[k - s0] = g[r];
-        }
-        __syncthreads();
-        for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {
-          const int o = iv.seg_soff[s], L = iv.seg_len[s];
-          if (pass == 0) {
-            T b = sb[o + L - 1];
-            if (iv.seg_c1[s] >= 0) b += exp_b[iv.seg_c1[s]];
-            if (iv.seg_c2[s] >= 0) b += exp_b[iv.seg_c2[s]];
-            sb[o + L - 1] = b;
-            for (int k = L - 1; k >= 1; k--) {
-              b = sb[o + k - 1] + sg[o + k] * b * si[o + k];
-              sb[o + k - 1] = b;
-            }
-            exp_b[s] = iv.seg_prow[s] >= 0 ? sg[o] * sb[o] * si[o] : (T)0;
-          } else {
-            const int pr = iv.seg_prow[s];
-            T x = (sb[o] + (pr >= 0 ? sg[o] * z[pr] : (T)0)) * si[o];
-            sb[o] = x;
-            for (int k = 1; k < L; k++) {
-              x = (sb[o + k] + sg[o + k] * x) * si[o + k];
-              sb[o + k] = x;
-            }
-          }
-        }
-        __syncthreads();
-        for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) z[iv.slot_row[k]] = sb[k - s0];
-        __syncthreads();
+  // elimination, deepest level first: y_k = v_k + e_{k+1} y_{k+1} inside a segment
+  for (int e = c.l0; e < c.l1; e++) {
+    for (int q = iv.lev_tile[e]; q < iv.lev_tile[e + 1]; q++) {
+      const int s0 = iv.tile_slot[q], cnt = iv.tile_slot[q + 1] - s0;
+      stage_gather(sa, iv.srow, v, s0, cnt);
+      stage_contig(sb, (const T *)iv.se, s0, cnt);
+      stage_flags(sf, iv.sflag, s0, cnt);
+      __syncthreads();
+      for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {
+        const int last = iv.seg_soff[s] + iv.seg_len[s] - 1;
+        const int c1 = iv.seg_c1[s], c2 = iv.seg_c2[s];
+        T add = 0;
+        if (c1 >= 0) add += exp_b[c1];
+        if (c2 >= 0) add += exp_b[c2];
+        sa[last] += add;
       }
-      level_sync<kGrid>(grid);
+      __syncthreads();
+      tile_affine_scan<T, true>(sa, cnt, SlotLink<T, true>{sb, sf}, scratch);
+      for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {
+        const int o = iv.seg_soff[s];
+        exp_b[s] = sb[o] * sa[o];
+      }
+      store_contig((T *)iv.sy, sa, s0, cnt);
+      __syncthreads();
     }
+    level_sync<kGrid>(grid);
+  }
+  // substitution, root level first: x_k = inv_k y_k + e_k x_{k-1} (x_mother on a first row)
+  for (int e = c.l1 - 1; e >= c.l0; e--) {
+    for (int q = iv.lev_tile[e]; q < iv.lev_tile[e + 1]; q++) {
+      const int s0 = iv.tile_slot[q], cnt = iv.tile_slot[q + 1] - s0;
+      stage_contig(sa, (const T *)iv.sy, s0, cnt);
+      stage_contig(sb, (const T *)iv.se, s0, cnt);
+      stage_contig(sd, (const T *)iv.sinv, s0, cnt);
+      stage_flags(sf, iv.sflag, s0, cnt);
+      __syncthreads();
+      for (int k = threadIdx.x; k < cnt; k += blockDim.x) sa[k] *= sd[k];
+      __syncthreads();
+      for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {
+        const int pr = iv.seg_prow[s];
+        if (pr >= 0) {
+          const int o = iv.seg_soff[s];
+          sa[o] += sb[o] * z[pr];
+        }
+      }
+      __syncthreads();
+      tile_affine_scan<T, false>(sa, cnt, SlotLink<T, false>{sb, sf}, scratch);
+      scatter_rows(z, iv.srow, sa, s0, cnt);
+      __syncthreads();
+    }
+    level_sync<kGrid>(grid);
   }
 }
 
-// (A x)_j for a physical row, FP64 (identity rows yield 0).
-__device__ __forceinline__ double row_apply64(const PackView &pv, const ImView &iv, int64_t j,
-                                              const double *x) {
-  const Topo t = pv.topo[j];
-  if (t.flags & F_IDENT) return 0.0;
-  double s = iv.diag[j] * x[j];
-  if (t.flags & F_UP) s -= iv.g64[j] * x[t.mother];
-  if (t.flags & F_DOWNR) s -= iv.g64[j + 1] * x[j + 1];
-  if (t.flags & F_DOWNL) s -= iv.g64[t.dl] * x[t.dl];
-  return s;
-}
-
-template <typename T>
-__device__ __forceinline__ T row_apply(const PackView &pv, const ImView &iv, int64_t j, const T *x);
-
-template <>
-__device__ __forceinline__ double row_apply<double>(const PackView &pv, const ImView &iv, int64_t j,
-                                                    const double *x) {
-  return row_apply64(pv, iv, j, x);
-}
-
-template <>
-__device__ __forceinline__ float row_apply<float>(const PackView &pv, const ImView &iv, int64_t j,
-                                                  const float *x) {
-  const Topo t = pv.topo[j];
-  if (t.flags & F_IDENT) return 0.0f;
-  float s = iv.diagf[j] * x[j];
-  if (t.flags & F_UP) s = fmaf(-iv.gf[j], x[t.mother], s);
-  if (t.flags & F_DOWNR) s = fmaf(-iv.gf[j + 1], x[j + 1], s);
-  if (t.flags & F_DOWNL) s = fmaf(-iv.gf[t.dl], x[t.dl], s);
-  return s;
-}
+// ---------------------------------------------------------------- segment preconditioner
 
 // Rows covered by tile q: from its first piece's start to its last piece's end.
 __device__ __forceinline__ void tile_rows(const ImView &iv, int q, int64_t &a, int64_t &b) {
@@ -361,20 +727,21 @@ __device__ __forceinline__ void tile_rows(const ImView &iv, int q, int64_t &a, i
 // Thomas factorisation of every piece (once per step): pd = 1/pivot, pc = c'.
 // Staged through shared memory tile by tile; one thread per piece.
 template <typename T, bool kGrid>
-__device__ void factor_pieces(Ctx<T, kGrid> &c, Shared &S) {
+__device__ __noinline__ void factor_pieces(Ctx<T, kGrid> c) {
+  Shared S = carve(dyn_smem(), c.iv->m);
   T *sd = (T *)S.tile;                          // diag, then pivots^-1
-  T *sg = sd + c.iv.tile_rows;                  // conductance to the mother
-  T *sc = sg + c.iv.tile_rows;                  // c'
+  T *sg = sd + c.iv->tile_rows;                  // conductance to the mother
+  T *sc = sg + c.iv->tile_rows;                  // c'
   for (int q = c.t0; q < c.t1; q++) {
     int64_t a, b;
-    tile_rows(c.iv, q, a, b);
+    tile_rows(*c.iv, q, a, b);
     for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
-      sd[r - a] = (T)c.iv.diag[r];
-      sg[r - a] = (T)c.iv.g64[r];
+      sd[r - a] = (T)c.iv->diag[r];
+      sg[r - a] = (T)c.iv->g64[r];
     }
     __syncthreads();
-    for (int p = c.iv.tiles[q] + threadIdx.x; p < c.iv.tiles[q + 1]; p += blockDim.x) {
-      const int2 pc = c.iv.pieces[p];
+    for (int p = c.iv->tiles[q] + threadIdx.x; p < c.iv->tiles[q + 1]; p += blockDim.x) {
+      const int2 pc = c.iv->pieces[p];
       const int o = (int)(pc.x - a);
       double cprev = 0;
       for (int k = 0; k < pc.y; k++) {
@@ -397,27 +764,29 @@ __device__ void factor_pieces(Ctx<T, kGrid> &c, Shared &S) {
 
 // z = M^-1 v over this CTA's rows (identity rows: v and z are 0).
 template <typename T, bool kGrid>
-__device__ void apply_precond(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared &S, const T *v, T *z) {
-  if (c.iv.precond == NRT_PRECOND_TREE) {
+__device__ __noinline__ void apply_precond(Ctx<T, kGrid> c, const T *v, T *z) {
+  cg::grid_group grid = cg::this_grid();
+  Shared S = carve(dyn_smem(), c.iv->m);
+  if (c.iv->precond == NRT_PRECOND_TREE) {
     level_sync<kGrid>(grid);  // v of every row visible (tree tiles span other CTAs' rows)
-    tree_apply(c, grid, S, v, z);
-  } else if (c.iv.precond == NRT_PRECOND_SEGMENT) {
+    tree_apply(c, v, z);
+  } else if (c.iv->precond == NRT_PRECOND_SEGMENT) {
     T *sv = (T *)S.tile;
-    T *sd = sv + c.iv.tile_rows;
-    T *sc = sd + c.iv.tile_rows;
-    T *sg = sc + c.iv.tile_rows;
+    T *sd = sv + c.iv->tile_rows;
+    T *sc = sd + c.iv->tile_rows;
+    T *sg = sc + c.iv->tile_rows;
     for (int q = c.t0; q < c.t1; q++) {
       int64_t a, b;
-      tile_rows(c.iv, q, a, b);
+      tile_rows(*c.iv, q, a, b);
       for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
         sv[r - a] = v[r];
         sd[r - a] = c.w.pd[r];
         sc[r - a] = c.w.pc[r];
-        sg[r - a] = (T)c.iv.g64[r];
+        sg[r - a] = (T)c.iv->g64[r];
       }
       __syncthreads();
-      for (int p = c.iv.tiles[q] + threadIdx.x; p < c.iv.tiles[q + 1]; p += blockDim.x) {
-        const int2 pc = c.iv.pieces[p];
+      for (int p = c.iv->tiles[q] + threadIdx.x; p < c.iv->tiles[q + 1]; p += blockDim.x) {
+        const int2 pc = c.iv->pieces[p];
         const int o = (int)(pc.x - a);
         T y = sv[o] * sd[o];
         sv[o] = y;
@@ -436,92 +805,307 @@ __device__ void apply_precond(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared &S,
     }
   } else {
     for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x) {
-      const uint32_t f = c.pv.topo[j].flags;
-      if (f & F_IDENT) {
+      const uint8_t f = c.iv->rowf[j];
+      if (f & R_IDENT) {
         z[j] = 0;
         continue;
       }
-      z[j] = c.iv.precond == NRT_PRECOND_JACOBI ? (T)((double)v[j] / c.iv.diag[j]) : v[j];
+      z[j] = c.iv->precond == NRT_PRECOND_JACOBI ? (T)((double)v[j] / c.iv->diag[j]) : v[j];
     }
     __syncthreads();
   }
 }
 
+// ---------------------------------------------------------------- one step
+//
+// The row passes below are separate (not inlined) functions: each keeps its own rows in
+// flight in registers, and none of them has to share the register file with the state
+// of the others.
+
+template <typename T>
+struct DotAcc {
+  T v[kG];
+};
+
+// Assembly: gates (from V^n), W, K, diagonal, c, right-hand side and the initial guess
+// (V^n extrapolated from V^{n-1}, which Vout holds); returns the thread's part of ||b||^2.
+template <typename T, bool kGrid>
+__device__ __noinline__ double ph_assemble(Ctx<T, kGrid> c, const double *Vin, double *Vout,
+                                           int active, int inst) {
+  const PackView &pv = *c.pv;
+  const ImView &iv = *c.iv;
+  const int64_t N = pv.ntot, stride = blockDim.x;
+  T *cdiag = (T *)iv.cdiag;
+  double bacc = 0;
+  for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kA * stride) {
+    uint8_t f[kA];
+    double v[kA], vo[kA], cm[kA], gj[kA], gn[kA], inp[kA];
+#pragma unroll
+    for (int u = 0; u < kA; u++) {
+      const int64_t r = rb + u * stride;
+      const bool ok = r < c.r1;
+      const int64_t rp = r + 1 < N ? r + 1 : r;
+      f[u] = ok ? iv.rowf[r] : (uint8_t)R_IDENT;
+      v[u] = ok ? Vin[r] : 0.0;
+      vo[u] = ok ? Vout[r] : 0.0;
+      cm[u] = ok ? iv.cmdt[r] : 0.0;
+      gj[u] = ok ? iv.g64[r] : 0.0;
+      gn[u] = ok ? iv.g64[rp] : 0.0;
+      inp[u] = ok && active ? iv.inp64[r] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kA; u++) {
+      const int64_t r = rb + u * stride;
+      if (r >= c.r1) continue;
+      double wdx, kdx;
+      if (f[u] & R_HH) {
+        const int64_t L = pv.hp_ld, hc = hp_col(pv, r, (uint32_t)inst);
+        if (pv.hpf) {
+          const float *hp = pv.hpf + hc;
+          const float dv = (float)(v[u] - (double)hp[HP_REST * L]);
+          GateStep32 g = hh_step32(dv + hp[HP_LSNA * L], dv + hp[HP_LSK * L], pv.gatef[r],
+                                   pv.gatef[N + r], pv.gatef[2 * N + r], hp[HP_DTMS * L],
+                                   hp[HP_GNA * L], hp[HP_GK * L], hp[HP_GL * L],
+                                   hp[HP_ENA * L], hp[HP_EK * L], hp[HP_EL * L]);
+          pv.gatef[r] = g.m;
+          pv.gatef[N + r] = g.h;
+          pv.gatef[2 * N + r] = g.n;
+          const double dx = (double)hp[HP_DX * L];
+          wdx = (double)g.W * dx;
+          kdx = (double)g.K * dx;
+        } else {
+          const double *hp = pv.hp + hc;
+          GateStep64 g = hh_step64(v[u], pv.gate[r], pv.gate[N + r], pv.gate[2 * N + r],
+                                   hp[HP_LSNA * L], hp[HP_LSK * L], hp[HP_REST * L],
+                                   hp[HP_DTMS * L], hp[HP_GNA * L], hp[HP_GK * L],
+                                   hp[HP_GL * L], hp[HP_ENA * L], hp[HP_EK * L],
+                                   hp[HP_EL * L]);
+          pv.gate[r] = g.m;
+          pv.gate[N + r] = g.h;
+          pv.gate[2 * N + r] = g.n;
+          const double dx = hp[HP_DX * L];
+          wdx = g.W * dx;
+          kdx = g.K * dx;
+        }
+      } else {
+        wdx = iv.wdx64[r];
+        kdx = iv.kdx64[r];
+      }
+      if (f[u] & R_IDENT) {
+        c.w.y[r] = 0;
+        continue;
+      }
+      const double cj = cm[u] - wdx;
+      double d = cj;
+      if (f[u] & R_DOWNL) d += iv.g64[pv.topo[r].dl];
+      if (f[u] & R_DOWNR) d += gn[u];
+      if (f[u] & R_UP) d += gj[u];
+      iv.diag[r] = d;
+      if (iv.diagf) iv.diagf[r] = (float)d;
+      if (cdiag) cdiag[r] = (T)cj;
+      double b = cm[u] * v[u] + kdx;
+      if (active) b += inp[u];
+      iv.rhs[r] = b;
+      bacc += b * b;
+      Vout[r] = 2.0 * v[u] - vo[u];
+    }
+  }
+  return bacc;
+}
+
+// True residual r = b - A x in FP64 into W_0 (identity rows 0); returns the thread's
+// part of ||r||^2.
+template <typename T, bool kGrid>
+__device__ __noinline__ double ph_residual(Ctx<T, kGrid> c, const double *x) {
+  const PackView &pv = *c.pv;
+  const ImView &iv = *c.iv;
+  const int64_t stride = blockDim.x;
+  double acc = 0;
+  for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kR * stride) {
+    double rh[kR], ax[kR];
+    uint8_t fl[kR];
+#pragma unroll
+    for (int u = 0; u < kR; u++) {
+      const int64_t r = rb + u * stride;
+      rh[u] = r < c.r1 ? iv.rhs[r] : 0.0;
+    }
+    apply_rows<kR>(pv, iv, iv.diag, iv.g64, x, rb, stride, c.r1, ax, fl);
+#pragma unroll
+    for (int u = 0; u < kR; u++) {
+      const int64_t r = rb + u * stride;
+      if (r >= c.r1) continue;
+      if (fl[u] & R_IDENT) {
+        c.w.Wb[r] = 0;
+        continue;
+      }
+      const double rr = rh[u] - ax[u];
+      c.w.Wb[r] = (T)rr;
+      acc += rr * rr;
+    }
+  }
+  return acc;
+}
+
+// y = s_j A Z_j, fused with the thread's parts of <y, W_i> for i < g1.
+template <typename T, bool kGrid>
+__device__ __noinline__ DotAcc<T> ph_spmv(Ctx<T, kGrid> c, int j, T sj, int g1) {
+  const PackView &pv = *c.pv;
+  const ImView &iv = *c.iv;
+  const int64_t N = pv.ntot, stride = blockDim.x;
+  const T *DT = sizeof(T) == 4 ? (const T *)(const void *)iv.diagf : (const T *)(const void *)iv.diag;
+  const T *GT = sizeof(T) == 4 ? (const T *)(const void *)iv.gf : (const T *)(const void *)iv.g64;
+  const T *Zj = c.w.Z + (size_t)j * N;
+  DotAcc<T> acc;
+#pragma unroll
+  for (int i = 0; i < kG; i++) acc.v[i] = 0;
+  for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kU * stride) {
+    T y[kU];
+    uint8_t fl[kU];
+    apply_rows<kU>(pv, iv, DT, GT, Zj, rb, stride, c.r1, y, fl);
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int64_t r = rb + u * stride;
+      y[u] *= sj;
+      if (r < c.r1) c.w.y[r] = y[u];
+    }
+#pragma unroll
+    for (int i = 0; i < kG; i++) {
+      if (i < g1) {
+        const T *Wi = c.w.Wb + (size_t)i * N;
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+          const int64_t r = rb + u * stride;
+          if (r < c.r1) acc.v[i] += y[u] * Wi[r];
+        }
+      }
+    }
+  }
+  return acc;
+}
+
+// The thread's parts of <y, W_{i0+i}> for i < gk.
+template <typename T, bool kGrid>
+__device__ __noinline__ DotAcc<T> ph_products(Ctx<T, kGrid> c, int i0, int gk) {
+  const int64_t N = c.pv->ntot, stride = blockDim.x;
+  DotAcc<T> acc;
+#pragma unroll
+  for (int i = 0; i < kG; i++) acc.v[i] = 0;
+  for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kV * stride) {
+    T y[kV];
+#pragma unroll
+    for (int u = 0; u < kV; u++) {
+      const int64_t r = rb + u * stride;
+      y[u] = r < c.r1 ? c.w.y[r] : (T)0;
+    }
+#pragma unroll
+    for (int i = 0; i < kG; i++) {
+      if (i < gk) {
+        const T *Wi = c.w.Wb + (size_t)(i0 + i) * N;
+#pragma unroll
+        for (int u = 0; u < kV; u++) {
+          const int64_t r = rb + u * stride;
+          if (r < c.r1) acc.v[i] += y[u] * Wi[r];
+        }
+      }
+    }
+  }
+  return acc;
+}
+
+// W_{j+1} = y - sum_{i <= j} coef_i W_i; returns the thread's part of ||W_{j+1}||^2.
+template <typename T, bool kGrid>
+__device__ __noinline__ T ph_update(Ctx<T, kGrid> c, int j, const T *coef) {
+  const int64_t N = c.pv->ntot, stride = blockDim.x;
+  T *Wn = c.w.Wb + (size_t)(j + 1) * N;
+  T nacc = 0;
+  for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kV * stride) {
+    T a[kV];
+#pragma unroll
+    for (int u = 0; u < kV; u++) {
+      const int64_t r = rb + u * stride;
+      a[u] = r < c.r1 ? c.w.y[r] : (T)0;
+    }
+#pragma unroll 1
+    for (int i = 0; i <= j; i++) {
+      const T ci = coef[i];
+      const T *Wi = c.w.Wb + (size_t)i * N;
+      T w[kV];
+#pragma unroll
+      for (int u = 0; u < kV; u++) {
+        const int64_t r = rb + u * stride;
+        w[u] = r < c.r1 ? Wi[r] : (T)0;
+      }
+#pragma unroll
+      for (int u = 0; u < kV; u++) a[u] -= ci * w[u];
+    }
+#pragma unroll
+    for (int u = 0; u < kV; u++) {
+      const int64_t r = rb + u * stride;
+      if (r < c.r1) {
+        Wn[r] = a[u];
+        nacc += a[u] * a[u];
+      }
+    }
+  }
+  return nacc;
+}
+
+// V += sum_{i < k} coef_i Z_i (identity rows keep their value).
+template <typename T, bool kGrid>
+__device__ __noinline__ void ph_xupdate(Ctx<T, kGrid> c, int k, const T *coef, double *Vout) {
+  const int64_t N = c.pv->ntot, stride = blockDim.x;
+  const uint8_t *rowf = c.iv->rowf;
+  for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kV * stride) {
+    T a[kV];
+    uint8_t fl[kV];
+#pragma unroll
+    for (int u = 0; u < kV; u++) {
+      const int64_t r = rb + u * stride;
+      a[u] = 0;
+      fl[u] = r < c.r1 ? rowf[r] : (uint8_t)R_IDENT;
+    }
+#pragma unroll 1
+    for (int i = 0; i < k; i++) {
+      const T ci = coef[i];
+      const T *Zi = c.w.Z + (size_t)i * N;
+      T z[kV];
+#pragma unroll
+      for (int u = 0; u < kV; u++) {
+        const int64_t r = rb + u * stride;
+        z[u] = r < c.r1 ? Zi[r] : (T)0;
+      }
+#pragma unroll
+      for (int u = 0; u < kV; u++) a[u] += ci * z[u];
+    }
+#pragma unroll
+    for (int u = 0; u < kV; u++) {
+      const int64_t r = rb + u * stride;
+      if (!(fl[u] & R_IDENT)) Vout[r] += (double)a[u];
+    }
+  }
+}
+
 // One backward-Euler step of one group (CTA or grid) for instance `inst`.
 template <typename T, bool kGrid>
-__device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared &S, int &parity,
-                                  const double *Vin, double *Vout, bool active, int64_t inst_n,
-                                  int inst) {
-  const PackView &pv = c.pv;
-  const ImView &iv = c.iv;
-  const int64_t N = pv.ntot;
+__device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid,
+                                                  Shared &S, int &parity, const double *Vin,
+                                                  double *Vout, bool active, int64_t inst_n,
+                                                  int inst) {
+  const ImView &iv = *c.iv;
   const int m = iv.m;
   T *coef = (T *)S.coef;
-  // ---- assembly: gates (from V^n), W, K, diagonal, right-hand side, x0 = V^n
-  double bacc = 0;
-  for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x) {
-    const Topo t = pv.topo[j];
-    const double v = Vin[j];
-    double wdx, kdx;
-    if (t.flags & F_HH) {
-      if (pv.hpf) {
-        const float *hp = pv.hpf;
-        const float dv = (float)(v - (double)hp[HP_REST * N + j]);
-        GateStep32 g = hh_step32(dv + hp[HP_LSNA * N + j], dv + hp[HP_LSK * N + j], pv.gatef[j],
-                                 pv.gatef[N + j], pv.gatef[2 * N + j], hp[HP_DTMS * N + j],
-                                 hp[HP_GNA * N + j], hp[HP_GK * N + j], hp[HP_GL * N + j],
-                                 hp[HP_ENA * N + j], hp[HP_EK * N + j], hp[HP_EL * N + j]);
-        pv.gatef[j] = g.m;
-        pv.gatef[N + j] = g.h;
-        pv.gatef[2 * N + j] = g.n;
-        const double dx = (double)hp[HP_DX * N + j];
-        wdx = (double)g.W * dx;
-        kdx = (double)g.K * dx;
-      } else {
-        const double *hp = pv.hp;
-        GateStep64 g = hh_step64(v, pv.gate[j], pv.gate[N + j], pv.gate[2 * N + j],
-                                 hp[HP_LSNA * N + j], hp[HP_LSK * N + j], hp[HP_REST * N + j],
-                                 hp[HP_DTMS * N + j], hp[HP_GNA * N + j], hp[HP_GK * N + j],
-                                 hp[HP_GL * N + j], hp[HP_ENA * N + j], hp[HP_EK * N + j],
-                                 hp[HP_EL * N + j]);
-        pv.gate[j] = g.m;
-        pv.gate[N + j] = g.h;
-        pv.gate[2 * N + j] = g.n;
-        const double dx = hp[HP_DX * N + j];
-        wdx = g.W * dx;
-        kdx = g.K * dx;
-      }
-    } else {
-      wdx = iv.wdx64[j];
-      kdx = iv.kdx64[j];
-    }
-    if (t.flags & F_IDENT) {
-      c.w.y[j] = 0;
-      continue;
-    }
-    double d = iv.cmdt[j] - wdx;
-    if (t.flags & F_DOWNL) d += iv.g64[t.dl];
-    if (t.flags & F_DOWNR) d += iv.g64[j + 1];
-    if (t.flags & F_UP) d += iv.g64[j];
-    iv.diag[j] = d;
-    if (iv.diagf) iv.diagf[j] = (float)d;
-    double b = iv.cmdt[j] * v + kdx;
-    if (active) b += iv.inp64[j];
-    iv.rhs[j] = b;
-    bacc += b * b;
-    Vout[j] = 2.0 * v - Vout[j];  // x0: linear extrapolation from V^{n-1} (held in Vout)
-  }
+  // ---- assembly
+  const double bacc = ph_assemble(c, Vin, Vout, active ? 1 : 0, inst);
   __syncthreads();
   if (iv.precond == NRT_PRECOND_SEGMENT) {
-    factor_pieces(c, S);
+    factor_pieces(c);
   } else if (iv.precond == NRT_PRECOND_TREE) {
-    level_sync<kGrid>(grid);  // diagonal of every row visible before the elimination
-    tree_factor(c, grid, S);
+    level_sync<kGrid>(grid);  // c of every row visible before the elimination
+    tree_factor(c);
   }
   double target = iv.tol;
   {
-    double acc[kMaxDots];
-    acc[0] = bacc;
+    double acc[1] = {bacc};
     group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);  // also publishes x0
     if (iv.tol_mode == NRT_TOL_REL) target = iv.tol * sqrt(S.red[0]);
     if (!kGrid) __syncthreads();
@@ -534,17 +1118,7 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
   for (;;) {
     // ---- cycle start: true residual r = b - A x in FP64, W_0 = r, Z_0 = M^-1 r
     {
-      double acc[kMaxDots];
-      acc[0] = 0;
-      for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x) {
-        if (pv.topo[j].flags & F_IDENT) {
-          c.w.Wb[j] = 0;
-          continue;
-        }
-        const double r = iv.rhs[j] - row_apply64(pv, iv, j, Vout);
-        c.w.Wb[j] = (T)r;
-        acc[0] += r * r;
-      }
+      double acc[1] = {ph_residual(c, Vout)};
       group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);
     }
     res = sqrt(S.red[0]);
@@ -553,7 +1127,7 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
       break;
     }
     if (iters >= budget) break;
-    apply_precond(c, grid, S, c.w.Wb, c.w.Z);
+    apply_precond(c, c.w.Wb, c.w.Z);
     group_sync<kGrid>(grid);  // Z_0 of every row visible before the SpMV
     if (threadIdx.x == 0) {
       S.g[0] = res;
@@ -564,34 +1138,17 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
     const double cycle_target = fmax(target, inner_rel * res);
     int k = 0;
     for (int j = 0; j < m; j++) {
-      const T *Zj = c.w.Z + (size_t)j * N;
-      const T sj = (T)S.s[j];
-      // y = s_j A Z_j fused with p_i = <y, W_i>, i <= j
-      T acc[kMaxDots];
-#pragma unroll
-      for (int i = 0; i < kMaxDots; i++) acc[i] = 0;
-      const int64_t stride = (int64_t)blockDim.x;
-      for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kU * stride) {
-        T y[kU];  // kU rows per thread in flight
-#pragma unroll
-        for (int u = 0; u < kU; u++) {
-          const int64_t r = rb + u * stride;
-          y[u] = r < c.r1 ? sj * row_apply<T>(pv, iv, r, Zj) : (T)0;
-        }
-#pragma unroll
-        for (int u = 0; u < kU; u++)
-          if (rb + u * stride < c.r1) c.w.y[rb + u * stride] = y[u];
-#pragma unroll
-        for (int i = 0; i < kMaxDots; i++) {
-          if (i <= j) {
-            const T *Wi = c.w.Wb + (size_t)i * N;
-#pragma unroll
-            for (int u = 0; u < kU; u++)
-              if (rb + u * stride < c.r1) acc[i] += y[u] * Wi[rb + u * stride];
-          }
-        }
+      // y = s_j A Z_j fused with p_i = <y, W_i> for the first kG of i <= j
+      const int g1 = min(j + 1, kG);
+      {
+        DotAcc<T> acc = ph_spmv(c, j, (T)S.s[j], g1);
+        group_reduce<kGrid>(grid, acc.v, g1, S, iv.partials, parity);
       }
-      group_reduce<kGrid>(grid, acc, j + 1, S, iv.partials, parity);
+      for (int i0 = kG; i0 <= j; i0 += kG) {  // remaining products, kG at a time
+        const int gk = min(j + 1 - i0, kG);
+        DotAcc<T> acc = ph_products(c, i0, gk);
+        group_reduce<kGrid>(grid, acc.v, gk, S, iv.partials, parity, i0);
+      }
       if (threadIdx.x <= j) {
         const double h = S.s[threadIdx.x] * S.red[threadIdx.x];
         S.H[threadIdx.x * m + j] = h;
@@ -599,32 +1156,9 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
       }
       __syncthreads();
       // w = y - sum_i h_ij s_i W_i -> W_{j+1}; ||w||^2; then Z_{j+1} = M^-1 w
-      T *Wn = c.w.Wb + (size_t)(j + 1) * N;
-      T nacc[kMaxDots];
-      nacc[0] = 0;
-      for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kU * stride) {
-        T a[kU];
-#pragma unroll
-        for (int u = 0; u < kU; u++) a[u] = rb + u * stride < c.r1 ? c.w.y[rb + u * stride] : (T)0;
-#pragma unroll
-        for (int i = 0; i < kMaxDots; i++) {
-          if (i <= j) {
-            const T ci = coef[i];
-            const T *Wi = c.w.Wb + (size_t)i * N;
-#pragma unroll
-            for (int u = 0; u < kU; u++)
-              if (rb + u * stride < c.r1) a[u] -= ci * Wi[rb + u * stride];
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < kU; u++)
-          if (rb + u * stride < c.r1) {
-            Wn[rb + u * stride] = a[u];
-            nacc[0] += a[u] * a[u];
-          }
-      }
+      T nacc[1] = {ph_update(c, j, coef)};
       __syncthreads();
-      apply_precond(c, grid, S, Wn, c.w.Z + (size_t)(j + 1) * N);
+      apply_precond(c, c.w.Wb + (size_t)(j + 1) * c.pv->ntot, c.w.Z + (size_t)(j + 1) * c.pv->ntot);
       group_reduce<kGrid>(grid, nacc, 1, S, iv.partials, parity);  // publishes Z_{j+1}
       if (threadIdx.x == 0) {
         const double hn = sqrt(S.red[0]);
@@ -658,29 +1192,7 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
       for (int i = 0; i < k; i++) coef[i] = (T)(S.y[i] * S.s[i]);
     }
     __syncthreads();
-    {
-      const int64_t stride = (int64_t)blockDim.x;
-      for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kU * stride) {
-        T a[kU];
-#pragma unroll
-        for (int u = 0; u < kU; u++) a[u] = 0;
-#pragma unroll
-        for (int i = 0; i < kMaxDots; i++) {
-          if (i < k) {
-            const T ci = coef[i];
-            const T *Zi = c.w.Z + (size_t)i * N;
-#pragma unroll
-            for (int u = 0; u < kU; u++)
-              if (rb + u * stride < c.r1) a[u] += ci * Zi[rb + u * stride];
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < kU; u++) {
-          const int64_t r = rb + u * stride;
-          if (r < c.r1 && !(pv.topo[r].flags & F_IDENT)) Vout[r] += (double)a[u];
-        }
-      }
-    }
+    ph_xupdate(c, k, coef, Vout);
     group_sync<kGrid>(grid);
   }
   if (threadIdx.x == 0 && (!kGrid || blockIdx.x == 0)) {
@@ -694,16 +1206,16 @@ __device__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared
 }
 
 template <typename T, bool kGrid>
-__global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView iv, int nsteps,
-                                                           int force, double *V0, double *V1,
-                                                           int cur) {
-  extern __shared__ __align__(16) double smem[];
-  Shared S = carve(smem, iv.m);
+__global__ void __launch_bounds__(kThreads, 3) implicit_steps(const PackView *pvp, const ImView *ivp,
+                                                           int nsteps, int force, double *V0,
+                                                           double *V1, int cur) {
+  const ImView &iv = *ivp;
+  Shared S = carve(dyn_smem(), iv.m);
   cg::grid_group grid = cg::this_grid();
   int parity = 0;
   Ctx<T, kGrid> c;
-  c.pv = pv;
-  c.iv = iv;
+  c.pv = pvp;
+  c.iv = ivp;
   c.w.Wb = (T *)iv.Wb;
   c.w.Z = (T *)iv.Z;
   c.w.y = (T *)iv.yv;
@@ -716,7 +1228,7 @@ __global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView i
     c.t1 = iv.cta_tile[blockIdx.x + 1];
     c.l0 = iv.work_lev ? iv.work_lev[blockIdx.x] : 0;
     c.l1 = iv.work_lev ? iv.work_lev[blockIdx.x + 1] : 0;
-    const InstDev in = pv.inst[0];
+    const InstDev in = pvp->inst[0];
     const int64_t inst_n = iv.inst_row[1] - iv.inst_row[0];
     for (int s = 0; s < nsteps; s++) {
       const int64_t i = in.base + s;
@@ -740,7 +1252,7 @@ __global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView i
       c.t1 = iv.inst_tile[inst + 1];
       c.l0 = iv.work_lev ? iv.work_lev[inst] : 0;
       c.l1 = iv.work_lev ? iv.work_lev[inst + 1] : 0;
-      const InstDev in = pv.inst[inst];
+      const InstDev in = pvp->inst[inst];
       int s = 0;
       for (; s < nsteps; s++) {
         const int64_t i = in.base + s;
@@ -762,34 +1274,36 @@ __global__ void __launch_bounds__(kThreads) implicit_steps(PackView pv, ImView i
 
 // ---------------------------------------------------------------- host side
 
+// Schedule of the exact tree preconditioner.  Segments are maximal runs of physical rows
+// each linked to the previous row (mother == j - 1), broken after every branch point and
+// at `cap` rows; a segment's parent row (the mother of its first row) is then always the
+// last row of its parent segment.  Level = number of segments above.  Each worker (one
+// CTA of the cooperative launch, or one instance of a batch) gets, per level (deepest
+// first), tiles of whole segments whose slots fit the shared-memory staging area; every
+// tile starts on a multiple of 4 slots (padding slots in between have row -1).
+struct TreeSchedule {
+  std::vector<int> seg_len, seg_c1, seg_c2, seg_prow, seg_soff;  // tile order
+  std::vector<int> tile_seg, tile_slot, slot_row, lev_tile, work_lev;
+  std::vector<uint8_t> slot_flag;
+};
+
 struct ImplicitState {
   ImView iv{};
+  PackView *d_pv = nullptr;  // device copies the kernel reads
+  ImView *d_iv = nullptr;
+  std::vector<uint8_t> rowf;
   std::vector<int2> pieces;
   std::vector<int> tiles, cta_row, cta_tile, inst_tile, order;
   std::vector<int64_t> inst_row;
+  TreeSchedule tree;
   int grid_blocks = 0;
   bool grid_mode = false;
+  int tile_rows = 0;
   size_t smem = 0;
 };
 
-static size_t smem_bytes(int m) { return ((shared_fixed_bytes(m) + 127) & ~(size_t)127) + kTileBytes; }
-
-size_t Engine::implicit_bytes() const {
-  const int64_t N = host.ntot;
-  const size_t tb = opt.precision == NRT_MIXED ? 4 : 8;
-  const int m = opt.restart;
-  size_t b = 0;
-  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  b += 6 * al(8 * N);                                   // cmdt, g64, wdx64, kdx64, inp64, diag
-  b += al(8 * N) + al(4 * N) + al(4 * N);               // rhs, diagf, gf
-  b += 2 * al(tb * N * (m + 1)) + 3 * al(tb * N);       // Wb, Z, y, pd, pc
-  b += al(8 * (N + 2)) + al(4 * (N + 2));               // pieces, tiles (upper bounds)
-  b += al(4 * 4100) * 2 + al(8 * (host.ninst + 1)) + al(4 * (host.ninst + 1)) + al(4 * host.ninst);
-  b += al(sizeof(double) * 2 * 4096 * kMaxDots);
-  b += al(sizeof(InstStat) * host.ninst) + al(64);
-  if (opt.precond == NRT_PRECOND_TREE)  // schedule arrays, factors, export slots (bounds)
-    b += 12 * al(4 * (N + 8)) + al(tb * N) + al(8 * N) + al(tb * N) + al(4 * (4096 + 8));
-  return b;
+static size_t smem_bytes(int m) {
+  return ((shared_fixed_bytes(m) + 127) & ~(size_t)127) + kTileBytes + kTileFlagBytes;
 }
 
 template <typename X>
@@ -808,17 +1322,6 @@ static int up(Arena &a, X *&dst, const X *src, size_t count, cudaStream_t st) {
     int _rc = (x);                  \
     if (_rc != NRT_OK) return _rc;  \
   } while (0)
-
-// Schedule of the exact tree preconditioner.  Segments are maximal runs of physical rows
-// each linked to the previous row (mother == j - 1), broken after every branch point and
-// at `cap` rows; a segment's parent row (the mother of its first row) is then always the
-// last row of its parent segment.  Level = number of segments above.  Each worker (one
-// CTA of the cooperative launch, or one instance of a batch) gets, per level (deepest
-// first), tiles of whole segments whose rows fit the shared-memory staging area.
-struct TreeSchedule {
-  std::vector<int> seg_len, seg_c1, seg_c2, seg_prow, seg_soff;  // tile order
-  std::vector<int> tile_seg, tile_slot, slot_row, lev_tile, work_lev;
-};
 
 static void build_tree_schedule(const HostPack &host, int cap, bool grid_mode, int ctas,
                                 TreeSchedule &T) {
@@ -892,6 +1395,15 @@ static void build_tree_schedule(const HostPack &host, int cap, bool grid_mode, i
   // Emit in (worker, level deepest first, tile) order; renumber segments accordingly.
   std::vector<int> newid(segs.size(), -1);
   std::vector<int> order;
+  auto pad = [&]() {
+    T.slot_row.push_back(-1);
+    T.slot_flag.push_back(SL_PAD | SL_FIRST | SL_LAST);
+  };
+  auto new_tile = [&]() {
+    while (T.slot_row.size() & 3) pad();
+    T.tile_seg.push_back((int)order.size());
+    T.tile_slot.push_back((int)T.slot_row.size());
+  };
   T.work_lev.assign(nwork + 1, 0);
   for (int w = 0; w < nwork; w++) {
     T.work_lev[w] = (int)T.lev_tile.size();
@@ -900,22 +1412,24 @@ static void build_tree_schedule(const HostPack &host, int cap, bool grid_mode, i
       int used = cap;  // forces a new tile for the first segment
       for (int s : lists[w][L]) {
         if (used + segs[s].len > cap) {
-          T.tile_seg.push_back((int)order.size());
-          T.tile_slot.push_back((int)T.slot_row.size());
+          new_tile();
           used = 0;
         }
         newid[s] = (int)order.size();
         order.push_back(s);
         T.seg_soff.push_back(used);
-        for (int k = 0; k < segs[s].len; k++) T.slot_row.push_back(segs[s].start + k);
+        for (int k = 0; k < segs[s].len; k++) {
+          T.slot_row.push_back(segs[s].start + k);
+          T.slot_flag.push_back((k == 0 ? SL_FIRST : 0) | (k == segs[s].len - 1 ? SL_LAST : 0));
+        }
         used += segs[s].len;
       }
     }
   }
   T.work_lev[nwork] = (int)T.lev_tile.size();
   T.lev_tile.push_back((int)T.tile_seg.size());
-  T.tile_seg.push_back((int)order.size());
-  T.tile_slot.push_back((int)T.slot_row.size());
+  new_tile();  // sentinel: end of the last tile
+  for (int k = 0; k < 16; k++) pad();  // 16-byte staging reads past the end
   for (int s : order) {
     const Seg &g = segs[s];
     T.seg_len.push_back(g.len);
@@ -938,7 +1452,11 @@ static void make_tiles(const std::vector<int2> &pieces, int pa, int pb, int tile
   }
 }
 
-int Engine::implicit_init() {
+static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Row structure, launch shape and preconditioner schedule; the exact device bytes the
+// implicit workspace takes from the arena.
+int Engine::implicit_plan(size_t &bytes) {
   im = new ImplicitState();
   ImplicitState &S = *im;
   const int64_t N = host.ntot;
@@ -947,24 +1465,36 @@ int Engine::implicit_init() {
   // numbering: mother < j, DR == j + 1 off terminals, terminals follow their mother.
   std::vector<char> is_term(N, 0);
   for (int64_t t : host.terms) is_term[t] = 1;
+  S.rowf.assign(N, R_IDENT);
   for (int32_t i = 0; i < ni; i++) {
     const int64_t o = host.off[i], n = host.num_elem[i];
     for (int64_t jl = 0; jl < n; jl++) {
       const int64_t j = o + jl;
       Topo &t = host.topo[j];
       t.flags &= ~(uint32_t)(F_UP | F_DOWNR | F_DOWNL | F_IDENT);
+      uint8_t rf = (t.flags & F_HH) ? R_HH : 0;
       const bool ident = jl == 0 || jl == n - 1 || is_term[j];
       if (ident) {
         t.flags |= F_IDENT;
+        S.rowf[j] = rf | R_IDENT;
         continue;
       }
-      if (jl != 1) t.flags |= F_UP;
-      if (!is_term[j + 1]) t.flags |= F_DOWNR;
-      if (t.flags & F_BRANCH) t.flags |= F_DOWNL;
+      if (jl != 1) {
+        t.flags |= F_UP;
+        rf |= R_UP;
+        if (t.mother != j - 1) rf |= R_FAR;
+      }
+      if (!is_term[j + 1]) {
+        t.flags |= F_DOWNR;
+        rf |= R_DOWNR;
+      }
+      if (t.flags & F_BRANCH) {
+        t.flags |= F_DOWNL;
+        rf |= R_DOWNL;
+      }
+      S.rowf[j] = rf;
     }
   }
-  NRT_CUDA(cudaMemcpyAsync((void *)pv.topo, host.topo.data(), sizeof(Topo) * N,
-                           cudaMemcpyHostToDevice, stream));
   // Segment pieces: maximal runs of consecutive physical rows linked to their
   // predecessor (mother == j - 1 with a mother column), cut at kMaxPiece rows.
   S.inst_row.assign(host.off.begin(), host.off.end());
@@ -989,7 +1519,7 @@ int Engine::implicit_init() {
   }
   const int np = (int)S.pieces.size();
   const size_t tb = opt.precision == NRT_MIXED ? 4 : 8;
-  const int tile_rows = (int)(kTileBytes / (4 * tb));
+  S.tile_rows = (int)(kTileBytes / (4 * tb));
   int dev_sms = 0;
   NRT_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, device));
   S.smem = smem_bytes(opt.restart);
@@ -1028,7 +1558,7 @@ int Engine::implicit_init() {
     S.cta_tile.assign(G + 1, 0);
     for (int c = 0; c < G; c++) {
       S.cta_tile[c] = (int)S.tiles.size();
-      make_tiles(S.pieces, cta_piece[c], cta_piece[c + 1], tile_rows, S.tiles);
+      make_tiles(S.pieces, cta_piece[c], cta_piece[c + 1], S.tile_rows, S.tiles);
     }
     S.cta_tile[G] = (int)S.tiles.size();
     S.grid_blocks = G;
@@ -1045,12 +1575,55 @@ int Engine::implicit_init() {
     S.inst_tile.assign(ni + 1, 0);
     for (int32_t i = 0; i < ni; i++) {
       S.inst_tile[i] = (int)S.tiles.size();
-      make_tiles(S.pieces, inst_piece[i], inst_piece[i + 1], tile_rows, S.tiles);
+      make_tiles(S.pieces, inst_piece[i], inst_piece[i + 1], S.tile_rows, S.tiles);
     }
     S.inst_tile[ni] = (int)S.tiles.size();
   }
   S.tiles.push_back(np);  // sentinel: end piece of the last tile
-  // device buffers
+  const bool tree = opt.precond == NRT_PRECOND_TREE;
+  if (tree) {
+    // staging slots: the substitution stages three T rows per slot
+    S.iv.tree_cap = (int)(kTileBytes / (3 * tb)) & ~3;
+    build_tree_schedule(host, S.iv.tree_cap, S.grid_mode, S.grid_blocks, S.tree);
+  }
+  // device bytes, in the order implicit_init takes them
+  const int m = opt.restart;
+  size_t b = 0;
+  b += al256(N);                                            // rowf
+  b += 5 * al256(8 * N);                                    // cmdt, g64, wdx64, kdx64, inp64
+  b += 2 * al256(8 * N);                                    // diag, rhs
+  b += al256(4 * N) + (mixed ? al256(4 * N) : 0);           // gf, diagf
+  b += 2 * al256(tb * N * (m + 1)) + 3 * al256(tb * N);     // Wb, Z, y, pd, pc
+  b += al256(sizeof(int2) * std::max<size_t>(1, S.pieces.size()));
+  b += al256(4 * S.tiles.size());
+  if (S.grid_mode)
+    b += al256(4 * S.cta_row.size()) + al256(4 * S.cta_tile.size());
+  else
+    b += al256(4 * S.inst_tile.size()) + al256(4 * S.order.size());
+  b += al256(8 * S.inst_row.size()) + al256(4) + al256(sizeof(double) * 2 * 4096 * kMaxDots);
+  b += al256(sizeof(InstStat) * ni) + al256(sizeof(PackView)) + al256(sizeof(ImView));
+  if (tree) {
+    const TreeSchedule &T = S.tree;
+    const size_t ns = T.slot_row.size(), nseg = std::max<size_t>(1, T.seg_len.size());
+    b += al256(tb * N);                                     // cdiag
+    b += 5 * al256(4 * nseg);                               // seg_len, c1, c2, prow, soff
+    b += al256(4 * T.tile_seg.size()) + al256(4 * T.tile_slot.size()) + al256(4 * ns) + al256(ns);
+    b += al256(4 * T.lev_tile.size()) + al256(4 * T.work_lev.size());
+    b += 4 * al256(tb * ns);                                // sg, sinv, se, sy
+    b += 2 * al256(tb * nseg);                              // exp_d, exp_b
+  }
+  bytes = b + 4096;
+  return NRT_OK;
+}
+
+int Engine::implicit_init() {
+  ImplicitState &S = *im;
+  const int64_t N = host.ntot;
+  const int32_t ni = host.ninst;
+  const bool mixed = opt.precision == NRT_MIXED;
+  const size_t tb = mixed ? 4 : 8;
+  NRT_CUDA(cudaMemcpyAsync((void *)pv.topo, host.topo.data(), sizeof(Topo) * N,
+                           cudaMemcpyHostToDevice, stream));
   cudaStream_t st = stream;
   ImView &iv = S.iv;
   iv.ntot = N;
@@ -1060,7 +1633,9 @@ int Engine::implicit_init() {
   iv.tol = opt.tol;
   iv.max_iter = opt.max_iter;
   iv.ninst = ni;
-  iv.tile_rows = tile_rows;
+  iv.tile_rows = S.tile_rows;
+  uint8_t *pr;
+  TRYI(up(arena, pr, S.rowf.data(), N, st)); iv.rowf = pr;
   std::vector<double> cmdt(N), g64(N), w64(N), k64(N), inp(N);
   std::vector<float> gf(N);
   for (int64_t j = 0; j < N; j++) {
@@ -1114,11 +1689,12 @@ int Engine::implicit_init() {
   std::vector<InstStat> zero(ni, InstStat{0, 0, 0, 0.0});
   TRYI(up(arena, iv.stats, zero.data(), ni, st));
   iv.work_lev = nullptr;
+  iv.cdiag = nullptr;
+  std::vector<char> sgbuf;
   if (opt.precond == NRT_PRECOND_TREE) {
-    TreeSchedule T;
-    // staging slots: the factorisation stages two FP64 rows, a solve three T rows
-    iv.tree_cap = (int)(kTileBytes / std::max<size_t>(2 * sizeof(double), 3 * tb));
-    build_tree_schedule(host, iv.tree_cap, S.grid_mode, S.grid_blocks, T);
+    const TreeSchedule &T = S.tree;
+    const size_t ns = T.slot_row.size(), nseg = std::max<size_t>(1, T.seg_len.size());
+    iv.cdiag = arena.take(tb * N);
     TRYI(up(arena, pi, T.seg_len.data(), T.seg_len.size(), st)); iv.seg_len = pi;
     TRYI(up(arena, pi, T.seg_c1.data(), T.seg_c1.size(), st)); iv.seg_c1 = pi;
     TRYI(up(arena, pi, T.seg_c2.data(), T.seg_c2.size(), st)); iv.seg_c2 = pi;
@@ -1126,18 +1702,45 @@ int Engine::implicit_init() {
     TRYI(up(arena, pi, T.seg_soff.data(), T.seg_soff.size(), st)); iv.seg_soff = pi;
     TRYI(up(arena, pi, T.tile_seg.data(), T.tile_seg.size(), st)); iv.tile_seg = pi;
     TRYI(up(arena, pi, T.tile_slot.data(), T.tile_slot.size(), st)); iv.tile_slot = pi;
-    TRYI(up(arena, pi, T.slot_row.data(), T.slot_row.size(), st)); iv.slot_row = pi;
+    TRYI(up(arena, pi, T.slot_row.data(), ns, st)); iv.srow = pi;
+    uint8_t *pf8;
+    TRYI(up(arena, pf8, T.slot_flag.data(), ns, st)); iv.sflag = pf8;
     TRYI(up(arena, pi, T.lev_tile.data(), T.lev_tile.size(), st)); iv.lev_tile = pi;
     TRYI(up(arena, pi, T.work_lev.data(), T.work_lev.size(), st)); iv.work_lev = pi;
-    const size_t nseg = std::max<size_t>(1, T.seg_len.size());
-    iv.tinv = arena.take(tb * N);
+    // static per-slot conductance to the mother (0 on a row without that column)
+    sgbuf.assign(tb * ns, 0);
+    for (size_t k = 0; k < ns; k++) {
+      const int r = T.slot_row[k];
+      const double g = (r >= 0 && (host.topo[r].flags & F_UP)) ? host.gax[r] : 0.0;
+      if (mixed)
+        ((float *)sgbuf.data())[k] = (float)g;
+      else
+        ((double *)sgbuf.data())[k] = g;
+    }
+    void *sgd = arena.take(tb * ns);
+    iv.sinv = arena.take(tb * ns);
+    iv.se = arena.take(tb * ns);
+    iv.sy = arena.take(tb * ns);
+    iv.exp_d = arena.take(tb * nseg);
     iv.exp_b = arena.take(tb * nseg);
-    TRYI(up(arena, iv.exp_d, (const double *)nullptr, nseg, st));
-    if (!iv.tinv || !iv.exp_b) {
+    if (!iv.cdiag || !sgd || !iv.sinv || !iv.se || !iv.sy || !iv.exp_d || !iv.exp_b) {
       set_error("arena exhausted (tree preconditioner)");
       return NRT_ENOMEM;
     }
+    NRT_CUDA(cudaMemcpyAsync(sgd, sgbuf.data(), tb * ns, cudaMemcpyHostToDevice, st));
+    iv.sg = sgd;
+    NRT_CUDA(cudaMemsetAsync(iv.sinv, 0, tb * ns, st));
+    NRT_CUDA(cudaMemsetAsync(iv.se, 0, tb * ns, st));
+    NRT_CUDA(cudaMemsetAsync(iv.sy, 0, tb * ns, st));
   }
+  S.d_pv = (PackView *)arena.take(sizeof(PackView));
+  S.d_iv = (ImView *)arena.take(sizeof(ImView));
+  if (!S.d_pv || !S.d_iv) {
+    set_error("arena exhausted (views)");
+    return NRT_ENOMEM;
+  }
+  NRT_CUDA(cudaMemcpyAsync(S.d_pv, &pv, sizeof(PackView), cudaMemcpyHostToDevice, st));
+  NRT_CUDA(cudaMemcpyAsync(S.d_iv, &iv, sizeof(ImView), cudaMemcpyHostToDevice, st));
   NRT_CUDA(cudaStreamSynchronize(st));
   return NRT_OK;
 }
@@ -1146,8 +1749,8 @@ int Engine::implicit_init() {
 static int implicit_launch(Engine &e, int nsteps, int force) {
   ImplicitState &S = *e.im;
   NRT_CUDA(cudaMemsetAsync(S.iv.queue, 0, sizeof(int), e.stream));
-  PackView pv = e.pv;
-  ImView iv = S.iv;
+  const PackView *pv = S.d_pv;
+  const ImView *iv = S.d_iv;
   double *V0 = e.V[0], *V1 = e.V[1];
   int cur = e.cur;
   void *args[] = {&pv, &iv, &nsteps, &force, &V0, &V1, &cur};
@@ -1258,9 +1861,12 @@ int export_system(Engine &e, int input_active, int32_t *row_ptr, int32_t *col, d
   NRT_CUDA(cudaStreamSynchronize(e.stream));
   const int saved_iter = S.iv.max_iter;
   S.iv.max_iter = -1;  // assembly only
+  NRT_CUDA(cudaMemcpyAsync(S.d_iv, &S.iv, sizeof(ImView), cudaMemcpyHostToDevice, e.stream));
   int rc = implicit_launch(e, 1, input_active ? 1 : 0);
   S.iv.max_iter = saved_iter;
+  const cudaError_t ce = cudaMemcpyAsync(S.d_iv, &S.iv, sizeof(ImView), cudaMemcpyHostToDevice, e.stream);
   if (rc) return rc;
+  NRT_CUDA(ce);
   std::vector<double> diag(N), rh(N), g(N);
   NRT_CUDA(cudaMemcpyAsync(diag.data(), S.iv.diag, 8 * N, cudaMemcpyDeviceToHost, e.stream));
   NRT_CUDA(cudaMemcpyAsync(rh.data(), S.iv.rhs, 8 * N, cudaMemcpyDeviceToHost, e.stream));

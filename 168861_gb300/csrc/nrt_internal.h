@@ -23,6 +23,7 @@ enum : uint32_t {
   F_MO_TERM = 256u, // explicit: the mother is a terminal (element 1 next to the root)
   F_DR_TERM = 512u, // explicit: the DR neighbour is a terminal (zero flux)
   F_DOWNL = 1024u,  // implicit row has a column at DL
+  F_INP = 2048u,    // nonzero injected current
 };
 constexpr int INST_SHIFT = 12;
 
@@ -34,7 +35,10 @@ struct __align__(16) Topo {
   uint32_t flags;   // F_* | instance << INST_SHIFT
 };
 
-// HH parameters per element, SoA rows of Pack::hp (FP64) / Pack::hpf (FP32).
+// HH parameters, SoA rows of Pack::hp (FP64) / Pack::hpf (FP32).  Columns: one per
+// instance when every HH element of an instance has the same parameters; else one per
+// distinct parameter set ("class", indexed through hp_cls) when there are few of them;
+// else one per element.
 enum { HP_GNA, HP_GK, HP_GL, HP_ENA, HP_EK, HP_EL, HP_LSNA, HP_LSK, HP_REST, HP_DX, HP_DTMS, HP_ROWS };
 
 // Per-instance run state kept on the device.
@@ -81,8 +85,11 @@ struct PackView {
   const double *inp;   // injected current
   double *gate;        // [3][ntot] m, h, n (FP64 path)
   float *gatef;        // [3][ntot] (mixed path)
-  const double *hp;    // [HP_ROWS][ntot]
-  const float *hpf;    // [HP_ROWS][ntot]
+  const double *hp;    // [HP_ROWS][hp_ld]
+  const float *hpf;    // [HP_ROWS][hp_ld]
+  int64_t hp_ld;       // number of columns
+  int hp_inst;         // 1: column = instance
+  const uint32_t *hp_cls;  // column per element (class tables), or null
   const float *cdtf, *gaxf, *wdxf, *kdxf, *inpf;  // FP32 copies (mixed path)
   InstDev *inst;
 };
@@ -109,7 +116,10 @@ struct HostPack {
   std::vector<Topo> topo;
   std::vector<double> cdt, gax, wdx, kdx, inp, V0, V1;
   std::vector<double> gate;         // [3][ntot]
-  std::vector<double> hp;           // [HP_ROWS][ntot]
+  std::vector<double> hp;           // [HP_ROWS][hp_ld]
+  bool hp_inst = false;             // one HH parameter column per instance
+  std::vector<uint32_t> hp_cls;     // column per element when classes are used
+  int64_t hp_ld = 0;
   std::vector<double> c_m_dx, radx; // c_m dX and r_a dX per element (implicit assembly)
   std::vector<double> Wfull, Kfull; // W, K per element as given
   std::vector<InstDev> inst;
@@ -122,6 +132,11 @@ struct HostPack {
 };
 
 int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp);
+
+// Column of the HH parameter tables for element j of instance `inst`.
+__host__ __device__ inline int64_t hp_col(const PackView &p, int64_t j, uint32_t inst) {
+  return p.hp_cls ? (int64_t)p.hp_cls[j] : (p.hp_inst ? (int64_t)inst : j);
+}
 
 // Kernel launchers (explicit.cu).
 int launch_explicit_step(const PackView &pv, int precision, bool general, int k, int force,

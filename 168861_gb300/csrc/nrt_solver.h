@@ -41,7 +41,7 @@ struct Engine {
   int fixup();
   int get_stats(nrt_stats *st);
   // implicit.cu
-  size_t implicit_bytes() const;
+  int implicit_plan(size_t &bytes);
   int implicit_init();
   int implicit_step(int k, int force);
   void implicit_release();

@@ -169,18 +169,30 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def _varies(a) -> bool:
+    return len(a) > 1 and bool(np.any(a != a[0]))
+
+
 def algorithmic_bytes_explicit(probs, precision: str) -> float:
-    """Bytes per step that the explicit step must move (the per-compartment figures of the
-    design notes): V read+write, gates read+write, parent index, the per-compartment
-    coefficients dT/(c_m dX) and 1/(r_a dX), and the channel parameters that vary per
-    compartment (g_Na, g_K, G_L, E_Na, E_K, E_L, LS_Na, LS_K).  Passive compartments move
-    V, index, both coefficients and W dX, K dX."""
+    """Compulsory bytes per explicit step: per compartment the potential (FP64) read and
+    written, the gates read and written (FP64, or FP32 in mixed precision), the parent
+    index, the coefficients dT/(c_m dX) and 1/(r_a dX) only where the geometry varies
+    within a tree, and a channel parameter only where it varies within a tree (uniform
+    ones live in a per-tree table).  Passive compartments: potential, index, the
+    coefficients where they vary, and W dX, K dX where they vary."""
     fb = 8 if precision == "fp64" else 4
-    n_hh = sum(int(p.struct.num_hh) for p in probs)
-    n = sum(p.num_elem for p in probs)
-    hh = 16 + 6 * fb + 4 + 2 * fb + 8 * fb
-    pas = 16 + 4 + 2 * fb + 2 * fb
-    return n_hh * hh + (n - n_hh) * pas
+    total = 0.0
+    for p in probs:
+        a = p.arrays
+        n, n_hh = p.num_elem, int(p.struct.num_hh)
+        geo = 2 * fb if (_varies(a["c_m"] * a["dx"]) or _varies(a["r_a"] * a["dx"])) else 0
+        chan = sum(fb for k in ("g_Na", "g_K", "G_L", "E_Na", "E_K", "E_L", "ls_Na", "ls_K")
+                   if _varies(a[k]))
+        passive = np.ones(n, bool)
+        passive[a["hh_elem"]] = False
+        wk = 2 * fb if (_varies(a["W"][passive]) or _varies(a["K"][passive])) else 0
+        total += n_hh * (16 + 6 * fb + 4 + geo + chan) + (n - n_hh) * (16 + 4 + geo + wk)
+    return total
 
 
 def algorithmic_bytes_implicit(probs, iters_per_step: float) -> float:
