@@ -605,7 +605,7 @@ int nrt_snapshot(nrt_solver *s, double *potential) {
   NRT_CUDA(cudaMemcpyAsync(potential, e.V[e.cur], sizeof(double) * e.host.ntot,
                            cudaMemcpyDeviceToHost, e.stream));
   NRT_CUDA(cudaStreamSynchronize(e.stream));
-  return NRT_OK;
+  return nrt::implicit_check(e);
 }
 
 int nrt_run(nrt_solver *s, int64_t i_begin, int64_t i_end, double init_time, double end_input) {
@@ -639,7 +639,7 @@ int nrt_synchronize(nrt_solver *s) {
   if (!s) return nrt::fail(NRT_EINVAL, "null solver");
   NRT_CUDA(cudaSetDevice(s->eng.device));
   NRT_CUDA(cudaStreamSynchronize(s->eng.stream));
-  return NRT_OK;
+  return nrt::implicit_check(s->eng);
 }
 
 int nrt_get_stream(nrt_solver *s, void **stream) {
@@ -754,7 +754,7 @@ int nrt_batch_synchronize(nrt_batch *b) {
   if (!b) return nrt::fail(NRT_EINVAL, "null batch");
   NRT_CUDA(cudaSetDevice(b->eng.device));
   NRT_CUDA(cudaStreamSynchronize(b->eng.stream));
-  return NRT_OK;
+  return nrt::implicit_check(b->eng);
 }
 
 int nrt_batch_snapshot(nrt_batch *b, int32_t instance, double *potential) {
@@ -768,7 +768,7 @@ int nrt_batch_snapshot(nrt_batch *b, int32_t instance, double *potential) {
   NRT_CUDA(cudaMemcpyAsync(potential, e.V[e.cur] + o, sizeof(double) * e.host.num_elem[instance],
                            cudaMemcpyDeviceToHost, e.stream));
   NRT_CUDA(cudaStreamSynchronize(e.stream));
-  return NRT_OK;
+  return nrt::implicit_check(e);
 }
 
 int nrt_batch_remaining(nrt_batch *b, int64_t *remaining) {

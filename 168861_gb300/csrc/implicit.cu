@@ -61,7 +61,6 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kMaxPiece = 256;                 // longest segment piece one sweep handles
 constexpr int kMaxDots = kMaxRestart + 1;
 constexpr int kTileBytes = 48 * 1024;          // shared-memory staging for the sweeps
-constexpr int kTileFlagBytes = 4096;           // tree tiles: one flag byte per slot
 constexpr int kU = 4;                          // rows per thread in flight: SpMV + products
 constexpr int kV = 8;                          // rows per thread in flight: streaming passes
 constexpr int kA = 1;                          // rows per thread in flight: assembly
@@ -113,9 +112,10 @@ struct ImView {
   int *queue;                     // batch: next index into order
   double *partials;               // kGrid: 2 x gridDim x kMaxDots
   InstStat *stats;
+  int *err;                       // set when a bounded wait gives up (device fault report)
   // exact tree preconditioner (NRT_PRECOND_TREE).  Segments in tile order; per-slot
   // arrays in slot order (slots: the rows of a worker's segments, level by level, deepest
-  // level first; every tile starts on a multiple of 4 slots, padding slots have row -1).
+  // level first; every tile starts on a multiple of 16 slots, padding slots have row -1).
   void *cdiag;                    // T[ntot]: c_j, written by the assembly
   const int *seg_len, *seg_c1, *seg_c2, *seg_prow, *seg_soff;
   const int *tile_seg;            // segments of tree tile q: [tile_seg[q], tile_seg[q+1])
@@ -127,7 +127,7 @@ struct ImView {
   const void *sg;                 // T per slot: conductance to the mother (0 without a column)
   void *sinv, *se, *sy;           // T per slot: 1 / pivot, g / pivot, eliminated right side
   void *exp_d, *exp_b;            // T per segment: what it passes to its parent row
-  int tree_cap;                   // staging slots per tree tile (multiple of 4)
+  int tree_cap;                   // staging slots per tree tile (multiple of 16)
 };
 
 template <typename T>
@@ -138,13 +138,14 @@ struct Work {
 struct Shared {
   double *H, *cs, *sn, *g, *s, *y, *red, *warp;
   void *coef;      // T[kMaxDots]: update / solution coefficients
-  int *flag;
+  int *flag;       // [0] convergence, [1] queue slot, [2] tile barrier phase
+  uint64_t *bar;   // mbarrier of the tile bulk copies
   void *tile;      // staging area
 };
 
 __host__ __device__ inline size_t shared_fixed_bytes(int m) {
   return sizeof(double) * ((size_t)(m + 1) * m + 2 * m + 2 * (m + 1) + m + kMaxDots +
-                           kWarps * kMaxDots + kMaxDots) + 16;
+                           kWarps * kMaxDots + kMaxDots) + 32;
 }
 
 // The dynamic shared memory of the launch.
@@ -165,6 +166,7 @@ __device__ Shared carve(double *base, int m) {
   S.warp = S.red + kMaxDots;
   S.coef = (void *)(S.warp + kWarps * kMaxDots);
   S.flag = (int *)((double *)S.coef + kMaxDots);
+  S.bar = (uint64_t *)(S.flag + 4);
   S.tile = (void *)((char *)base + ((shared_fixed_bytes(m) + 127) & ~(size_t)127));
   return S;
 }
@@ -330,78 +332,134 @@ __device__ __forceinline__ void level_sync(cg::grid_group &grid) {
 
 enum : uint8_t { SL_FIRST = 1, SL_LAST = 2, SL_PAD = 4 };  // slot flags (ImView::sflag)
 
-// Contiguous copy of `count` T values from src[s0 ..] into shared memory in 16-byte
-// chunks (s0 is 4-aligned; the slot arrays are padded so the rounded tail stays in bounds).
-template <typename T>
-__device__ __forceinline__ void stage_contig(T *dst, const T *src, int s0, int count) {
-  const int n16 = (int)(((size_t)count * sizeof(T) + 15) >> 4);
-  const uint4 *s = reinterpret_cast<const uint4 *>(src + s0);
-  uint4 *d = reinterpret_cast<uint4 *>(dst);
-  for (int q = threadIdx.x; q < n16; q += 4 * blockDim.x) {
-    uint4 v[4];
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const int qq = q + u * blockDim.x;
-      if (qq < n16) v[u] = s[qq];
-    }
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const int qq = q + u * blockDim.x;
-      if (qq < n16) d[qq] = v[u];
+// ---- bulk (TMA) copies global -> shared, completed on an mbarrier
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// Orders this thread's earlier generic-proxy accesses before later bulk (async-proxy) ones.
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async;" ::: "memory");
+}
+
+// Waits for phase `phase` of the tile barrier; gives up after about two seconds of
+// clock (the copies it waits for are in bounds and always land, so giving up means a
+// device fault), raising the error word the host checks.
+__device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t phase, int *err) {
+  if (mbar_try_wait(bar, phase)) return;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, phase)) {
+    if (clock64() - t0 > 4000000000ll) {
+      atomicOr(err, 1);
+      return;
     }
   }
 }
 
-// dst[k] = src[srow[s0 + k]] (0 for padding slots).
+// Shared-memory tile of the tree preconditioner: three T rows, the slot flags and the
+// slot rows, `cap` slots each.
 template <typename T>
-__device__ __forceinline__ void stage_gather(T *dst, const int *srow, const T *src, int s0,
-                                             int count) {
-  for (int k = threadIdx.x; k < count; k += 8 * blockDim.x) {
-    int r[8];
-#pragma unroll
-    for (int u = 0; u < 8; u++) {
-      const int kk = k + u * blockDim.x;
-      r[u] = kk < count ? srow[s0 + kk] : -1;
-    }
+struct TreeTile {
+  T *a, *b, *d;
+  uint8_t *f;
+  int *r;
+};
+
+template <typename T>
+__device__ __forceinline__ TreeTile<T> tree_tile(const Shared &S, int cap) {
+  TreeTile<T> t;
+  t.a = (T *)S.tile;
+  t.b = t.a + cap;
+  t.d = t.b + cap;
+  t.r = (int *)(t.d + cap);
+  t.f = (uint8_t *)(t.r + cap);
+  return t;
+}
+
+// Bulk-copies slots [s0, s0 + cnt) of the slot rows, the slot flags and up to three T
+// arrays (null sources are skipped) into the tile, then waits for them.  s0 is a multiple
+// of 16 slots and the slot arrays are padded, so every copy starts 16-byte aligned and
+// its size rounded up to 16 bytes stays inside the arrays and the tile.
+template <typename T>
+__device__ __forceinline__ void tile_bulk_load(const ImView &iv, const Shared &S,
+                                               const TreeTile<T> &t, int s0, int cnt,
+                                               const T *x0, T *d0, const T *x1, T *d1,
+                                               const T *x2, T *d2) {
+  const uint32_t nt = ((uint32_t)cnt * sizeof(T) + 15u) & ~15u;
+  const uint32_t nr = ((uint32_t)cnt * 4u + 15u) & ~15u;
+  const uint32_t nf = ((uint32_t)cnt + 15u) & ~15u;
+  if (threadIdx.x == 0) {
+    fence_proxy_async();
+    const uint32_t total = nr + nf + (x0 ? nt : 0) + (x1 ? nt : 0) + (x2 ? nt : 0);
+    mbar_expect_tx(S.bar, total);
+    bulk_load(t.r, iv.srow + s0, nr, S.bar);
+    bulk_load(t.f, iv.sflag + s0, nf, S.bar);
+    if (x0) bulk_load(d0, x0 + s0, nt, S.bar);
+    if (x1) bulk_load(d1, x1 + s0, nt, S.bar);
+    if (x2) bulk_load(d2, x2 + s0, nt, S.bar);
+  }
+  const uint32_t ph = (uint32_t)S.flag[2];
+  mbar_wait(S.bar, ph, iv.err);
+  __syncthreads();
+  if (threadIdx.x == 0) S.flag[2] = (int)(ph ^ 1u);
+}
+
+// dst[k] = src[row of slot k] for the slots of the tile (0 for padding slots).
+template <typename T>
+__device__ __forceinline__ void tile_gather(T *dst, const int *rows, const T *src, int cnt) {
+  for (int k = threadIdx.x; k < cnt; k += 8 * blockDim.x) {
     T v[8];
 #pragma unroll
-    for (int u = 0; u < 8; u++) v[u] = r[u] >= 0 ? src[r[u]] : (T)0;
+    for (int u = 0; u < 8; u++) {
+      const int kk = k + u * blockDim.x;
+      const int r = kk < cnt ? rows[kk] : -1;
+      v[u] = r >= 0 ? src[r] : (T)0;
+    }
 #pragma unroll
     for (int u = 0; u < 8; u++) {
       const int kk = k + u * blockDim.x;
-      if (kk < count) dst[kk] = v[u];
+      if (kk < cnt) dst[kk] = v[u];
     }
   }
 }
 
-// Slot flags from src[s0 ..] in 4-byte words (s0 is a multiple of 4, so the words are
-// aligned; the flag array is padded past its last slot).
-__device__ __forceinline__ void stage_flags(uint8_t *dst, const uint8_t *src, int s0, int count) {
-  const int n4 = (count + 3) >> 2;
-  const uint32_t *s = reinterpret_cast<const uint32_t *>(src + s0);
-  uint32_t *d = reinterpret_cast<uint32_t *>(dst);
-  for (int q = threadIdx.x; q < n4; q += blockDim.x) d[q] = s[q];
-}
-
+// dst[s0 + k] = src[k] for the tile's slots.
 template <typename T>
 __device__ __forceinline__ void store_contig(T *dst, const T *src, int s0, int count) {
   for (int k = threadIdx.x; k < count; k += blockDim.x) dst[s0 + k] = src[k];
 }
 
-// dst[srow[s0 + k]] = src[k] for the real slots.
+// dst[row of slot k] = src[k] for the real slots of the tile.
 template <typename T>
-__device__ __forceinline__ void scatter_rows(T *dst, const int *srow, const T *src, int s0,
-                                             int count) {
-  for (int k = threadIdx.x; k < count; k += 4 * blockDim.x) {
-    int r[4];
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const int kk = k + u * blockDim.x;
-      r[u] = kk < count ? srow[s0 + kk] : -1;
-    }
-#pragma unroll
-    for (int u = 0; u < 4; u++)
-      if (r[u] >= 0) dst[r[u]] = src[k + u * blockDim.x];
+__device__ __forceinline__ void tile_scatter(T *dst, const int *rows, const T *src, int cnt) {
+  for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+    const int r = rows[k];
+    if (r >= 0) dst[r] = src[k];
   }
 }
 
@@ -614,19 +672,15 @@ __device__ __noinline__ void tree_factor(Ctx<T, kGrid> c) {
   const ImView &iv = *c.iv;
   cg::grid_group grid = cg::this_grid();
   Shared S = carve(dyn_smem(), iv.m);
-  T *sc = (T *)S.tile;
-  T *sgg = sc + iv.tree_cap;
-  T *sh = sgg + iv.tree_cap;
-  uint8_t *sf = (uint8_t *)(sh + iv.tree_cap);
+  const TreeTile<T> t = tree_tile<T>(S, iv.tree_cap);
   T *scratch = (T *)S.warp;
-  const T *cdiag = (const T *)iv.cdiag;
   T *exp_d = (T *)iv.exp_d;
   for (int e = c.l0; e < c.l1; e++) {
     for (int q = iv.lev_tile[e]; q < iv.lev_tile[e + 1]; q++) {
       const int s0 = iv.tile_slot[q], cnt = iv.tile_slot[q + 1] - s0;
-      stage_gather(sc, iv.srow, cdiag, s0, cnt);
-      stage_contig(sgg, (const T *)iv.sg, s0, cnt);
-      stage_flags(sf, iv.sflag, s0, cnt);
+      tile_bulk_load<T>(iv, S, t, s0, cnt, (const T *)iv.sg, t.b, nullptr, nullptr, nullptr,
+                        nullptr);
+      tile_gather(t.a, t.r, (const T *)iv.cdiag, cnt);  // c of every slot's row
       __syncthreads();
       for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {
         const int last = iv.seg_soff[s] + iv.seg_len[s] - 1;
@@ -634,14 +688,15 @@ __device__ __noinline__ void tree_factor(Ctx<T, kGrid> c) {
         T add = 0;
         if (c1 >= 0) add += exp_d[c1];
         if (c2 >= 0) add += exp_d[c2];
-        sc[last] += add;
+        t.a[last] += add;
       }
       __syncthreads();
-      tile_factor_scan(sc, sgg, sh, sf, cnt, scratch);
+      tile_factor_scan(t.a, t.b, t.d, t.f, cnt, scratch);
       for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x)
-        exp_d[s] = sh[iv.seg_soff[s]];  // 0 when the first row has no mother column
-      store_contig((T *)iv.sinv, sc, s0, cnt);
-      store_contig((T *)iv.se, sgg, s0, cnt);
+        exp_d[s] = t.d[iv.seg_soff[s]];  // 0 when the first row has no mother column
+      store_contig((T *)iv.sinv, t.a, s0, cnt);
+      store_contig((T *)iv.se, t.b, s0, cnt);
+      fence_proxy_async();  // the solves read sinv / se back with bulk copies
       __syncthreads();
     }
     level_sync<kGrid>(grid);
@@ -654,19 +709,16 @@ __device__ __noinline__ void tree_apply(Ctx<T, kGrid> c, const T *v, T *z) {
   const ImView &iv = *c.iv;
   cg::grid_group grid = cg::this_grid();
   Shared S = carve(dyn_smem(), iv.m);
-  T *sa = (T *)S.tile;
-  T *sb = sa + iv.tree_cap;
-  T *sd = sb + iv.tree_cap;
-  uint8_t *sf = (uint8_t *)(sd + iv.tree_cap);
+  const TreeTile<T> t = tree_tile<T>(S, iv.tree_cap);
   T *scratch = (T *)S.warp;
   T *exp_b = (T *)iv.exp_b;
   // elimination, deepest level first: y_k = v_k + e_{k+1} y_{k+1} inside a segment
   for (int e = c.l0; e < c.l1; e++) {
     for (int q = iv.lev_tile[e]; q < iv.lev_tile[e + 1]; q++) {
       const int s0 = iv.tile_slot[q], cnt = iv.tile_slot[q + 1] - s0;
-      stage_gather(sa, iv.srow, v, s0, cnt);
-      stage_contig(sb, (const T *)iv.se, s0, cnt);
-      stage_flags(sf, iv.sflag, s0, cnt);
+      tile_bulk_load<T>(iv, S, t, s0, cnt, (const T *)iv.se, t.b, nullptr, nullptr, nullptr,
+                        nullptr);
+      tile_gather(t.a, t.r, v, cnt);
       __syncthreads();
       for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {
         const int last = iv.seg_soff[s] + iv.seg_len[s] - 1;
@@ -674,15 +726,16 @@ __device__ __noinline__ void tree_apply(Ctx<T, kGrid> c, const T *v, T *z) {
         T add = 0;
         if (c1 >= 0) add += exp_b[c1];
         if (c2 >= 0) add += exp_b[c2];
-        sa[last] += add;
+        t.a[last] += add;
       }
       __syncthreads();
-      tile_affine_scan<T, true>(sa, cnt, SlotLink<T, true>{sb, sf}, scratch);
+      tile_affine_scan<T, true>(t.a, cnt, SlotLink<T, true>{t.b, t.f}, scratch);
       for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {
         const int o = iv.seg_soff[s];
-        exp_b[s] = sb[o] * sa[o];
+        exp_b[s] = t.b[o] * t.a[o];
       }
-      store_contig((T *)iv.sy, sa, s0, cnt);
+      store_contig((T *)iv.sy, t.a, s0, cnt);
+      fence_proxy_async();  // the substitution reads sy back with bulk copies
       __syncthreads();
     }
     level_sync<kGrid>(grid);
@@ -691,23 +744,20 @@ __device__ __noinline__ void tree_apply(Ctx<T, kGrid> c, const T *v, T *z) {
   for (int e = c.l1 - 1; e >= c.l0; e--) {
     for (int q = iv.lev_tile[e]; q < iv.lev_tile[e + 1]; q++) {
       const int s0 = iv.tile_slot[q], cnt = iv.tile_slot[q + 1] - s0;
-      stage_contig(sa, (const T *)iv.sy, s0, cnt);
-      stage_contig(sb, (const T *)iv.se, s0, cnt);
-      stage_contig(sd, (const T *)iv.sinv, s0, cnt);
-      stage_flags(sf, iv.sflag, s0, cnt);
-      __syncthreads();
-      for (int k = threadIdx.x; k < cnt; k += blockDim.x) sa[k] *= sd[k];
+      tile_bulk_load<T>(iv, S, t, s0, cnt, (const T *)iv.sy, t.a, (const T *)iv.se, t.b,
+                        (const T *)iv.sinv, t.d);
+      for (int k = threadIdx.x; k < cnt; k += blockDim.x) t.a[k] *= t.d[k];
       __syncthreads();
       for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {
         const int pr = iv.seg_prow[s];
         if (pr >= 0) {
           const int o = iv.seg_soff[s];
-          sa[o] += sb[o] * z[pr];
+          t.a[o] += t.b[o] * z[pr];
         }
       }
       __syncthreads();
-      tile_affine_scan<T, false>(sa, cnt, SlotLink<T, false>{sb, sf}, scratch);
-      scatter_rows(z, iv.srow, sa, s0, cnt);
+      tile_affine_scan<T, false>(t.a, cnt, SlotLink<T, false>{t.b, t.f}, scratch);
+      tile_scatter(z, t.r, t.a, cnt);
       __syncthreads();
     }
     level_sync<kGrid>(grid);
@@ -1213,6 +1263,11 @@ __global__ void __launch_bounds__(kThreads, 3) implicit_steps(const PackView *pv
   Shared S = carve(dyn_smem(), iv.m);
   cg::grid_group grid = cg::this_grid();
   int parity = 0;
+  if (threadIdx.x == 0) {
+    mbar_init(S.bar, 1);
+    S.flag[2] = 0;
+  }
+  __syncthreads();
   Ctx<T, kGrid> c;
   c.pv = pvp;
   c.iv = ivp;
@@ -1280,7 +1335,7 @@ __global__ void __launch_bounds__(kThreads, 3) implicit_steps(const PackView *pv
 // last row of its parent segment.  Level = number of segments above.  Each worker (one
 // CTA of the cooperative launch, or one instance of a batch) gets, per level (deepest
 // first), tiles of whole segments whose slots fit the shared-memory staging area; every
-// tile starts on a multiple of 4 slots (padding slots in between have row -1).
+// tile starts on a multiple of 16 slots (padding slots in between have row -1).
 struct TreeSchedule {
   std::vector<int> seg_len, seg_c1, seg_c2, seg_prow, seg_soff;  // tile order
   std::vector<int> tile_seg, tile_slot, slot_row, lev_tile, work_lev;
@@ -1302,9 +1357,7 @@ struct ImplicitState {
   size_t smem = 0;
 };
 
-static size_t smem_bytes(int m) {
-  return ((shared_fixed_bytes(m) + 127) & ~(size_t)127) + kTileBytes + kTileFlagBytes;
-}
+static size_t smem_bytes(int m) { return ((shared_fixed_bytes(m) + 127) & ~(size_t)127) + kTileBytes; }
 
 template <typename X>
 static int up(Arena &a, X *&dst, const X *src, size_t count, cudaStream_t st) {
@@ -1400,7 +1453,7 @@ static void build_tree_schedule(const HostPack &host, int cap, bool grid_mode, i
     T.slot_flag.push_back(SL_PAD | SL_FIRST | SL_LAST);
   };
   auto new_tile = [&]() {
-    while (T.slot_row.size() & 3) pad();
+    while (T.slot_row.size() & 15) pad();
     T.tile_seg.push_back((int)order.size());
     T.tile_slot.push_back((int)T.slot_row.size());
   };
@@ -1429,7 +1482,7 @@ static void build_tree_schedule(const HostPack &host, int cap, bool grid_mode, i
   T.work_lev[nwork] = (int)T.lev_tile.size();
   T.lev_tile.push_back((int)T.tile_seg.size());
   new_tile();  // sentinel: end of the last tile
-  for (int k = 0; k < 16; k++) pad();  // 16-byte staging reads past the end
+  for (int k = 0; k < 16; k++) pad();  // bulk copies round their size up to 16 bytes
   for (int s : order) {
     const Seg &g = segs[s];
     T.seg_len.push_back(g.len);
@@ -1582,8 +1635,8 @@ int Engine::implicit_plan(size_t &bytes) {
   S.tiles.push_back(np);  // sentinel: end piece of the last tile
   const bool tree = opt.precond == NRT_PRECOND_TREE;
   if (tree) {
-    // staging slots: the substitution stages three T rows per slot
-    S.iv.tree_cap = (int)(kTileBytes / (3 * tb)) & ~3;
+    // staging slots: three T rows, the slot row and the slot flag per slot
+    S.iv.tree_cap = (int)(kTileBytes / (3 * tb + 5)) & ~15;
     build_tree_schedule(host, S.iv.tree_cap, S.grid_mode, S.grid_blocks, S.tree);
   }
   // device bytes, in the order implicit_init takes them
@@ -1600,7 +1653,7 @@ int Engine::implicit_plan(size_t &bytes) {
     b += al256(4 * S.cta_row.size()) + al256(4 * S.cta_tile.size());
   else
     b += al256(4 * S.inst_tile.size()) + al256(4 * S.order.size());
-  b += al256(8 * S.inst_row.size()) + al256(4) + al256(sizeof(double) * 2 * 4096 * kMaxDots);
+  b += al256(8 * S.inst_row.size()) + 2 * al256(4) + al256(sizeof(double) * 2 * 4096 * kMaxDots);
   b += al256(sizeof(InstStat) * ni) + al256(sizeof(PackView)) + al256(sizeof(ImView));
   if (tree) {
     const TreeSchedule &T = S.tree;
@@ -1685,6 +1738,8 @@ int Engine::implicit_init() {
   int64_t *pl;
   TRYI(up(arena, pl, S.inst_row.data(), S.inst_row.size(), st)); iv.inst_row = pl;
   TRYI(up(arena, iv.queue, (const int *)nullptr, 1, st));
+  TRYI(up(arena, iv.err, (const int *)nullptr, 1, st));
+  NRT_CUDA(cudaMemsetAsync(iv.err, 0, sizeof(int), st));
   TRYI(up(arena, iv.partials, (const double *)nullptr, (size_t)2 * 4096 * kMaxDots, st));
   std::vector<InstStat> zero(ni, InstStat{0, 0, 0, 0.0});
   TRYI(up(arena, iv.stats, zero.data(), ni, st));
@@ -1801,9 +1856,23 @@ int instance_stats(Engine &e, int64_t *iters, int32_t *last_iters, int32_t *nonc
   return NRT_OK;
 }
 
+// NRT_EDEVICE when a kernel's bounded wait gave up (the error word is set); synchronises.
+int implicit_check(Engine &e) {
+  if (!e.im) return NRT_OK;
+  int err = 0;
+  NRT_CUDA(cudaMemcpyAsync(&err, e.im->iv.err, sizeof(int), cudaMemcpyDeviceToHost, e.stream));
+  NRT_CUDA(cudaStreamSynchronize(e.stream));
+  if (err) {
+    set_error("implicit kernel: a bounded wait for its tile copies expired");
+    return NRT_EDEVICE;
+  }
+  return NRT_OK;
+}
+
 // Sum of non-converged steps over all instances (-1 on a device error).
 int64_t nonconverged_total(Engine &e) {
   if (!e.im) return 0;
+  if (implicit_check(e) != NRT_OK) return -1;
   std::vector<InstStat> s(e.host.ninst);
   if (cudaMemcpyAsync(s.data(), e.im->iv.stats, sizeof(InstStat) * e.host.ninst,
                       cudaMemcpyDeviceToHost, e.stream) != cudaSuccess ||

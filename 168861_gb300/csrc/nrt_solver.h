@@ -53,6 +53,7 @@ int implicit_advance(Engine &e, int64_t steps);
 int export_system(Engine &e, int input_active, int32_t *row_ptr, int32_t *col, double *val,
                   double *rhs, int32_t *nnz_out);
 int64_t nonconverged_total(Engine &e);
+int implicit_check(Engine &e);
 int instance_stats(Engine &e, int64_t *iters, int32_t *last_iters, int32_t *nonconv,
                    double *last_res);
 
