@@ -538,6 +538,8 @@ static int check_options(const nrt_options *o, std::string &why) {
   if (o->mode != NRT_EXPLICIT && o->mode != NRT_IMPLICIT_BE) return (why = "bad mode", NRT_EINVAL);
   if (o->precision != NRT_FP64 && o->precision != NRT_MIXED) return (why = "bad precision", NRT_EINVAL);
   if (o->krylov != NRT_GMRES && o->krylov != NRT_BICGSTAB) return (why = "bad krylov", NRT_EINVAL);
+  if (o->mode == NRT_IMPLICIT_BE && o->krylov == NRT_BICGSTAB && o->restart < 3)
+    return (why = "BiCGSTAB needs restart >= 3 (its eight work vectors share the GMRES basis)", NRT_EINVAL);
   if (o->precond < NRT_PRECOND_NONE || o->precond > NRT_PRECOND_TREE) return (why = "bad precond", NRT_EINVAL);
   if (o->restart < 1 || o->restart > nrt::kMaxRestart) return (why = "restart must be in [1, 32]", NRT_EINVAL);
   if (!(o->tol > 0)) return (why = "tol must be > 0", NRT_EINVAL);

@@ -86,7 +86,8 @@ struct InstStat {
 
 struct ImView {
   int64_t ntot;
-  int m;             // restart
+  int m;             // restart (GMRES) / iterations per refinement cycle (BiCGSTAB)
+  int krylov;        // NRT_GMRES or NRT_BICGSTAB
   int precond;
   int tol_mode;
   double tol;
@@ -1135,6 +1136,183 @@ __device__ __noinline__ void ph_xupdate(Ctx<T, kGrid> c, int k, const T *coef, d
   }
 }
 
+// ---- BiCGSTAB (right-preconditioned, on the correction equation of one refinement cycle)
+
+// p = r + beta (p - omega v); beta == 0 gives p = r.
+template <typename T, bool kGrid>
+__device__ __noinline__ void ph_bicg_dir(Ctx<T, kGrid> c, const T *r, T *p, const T *v, T beta,
+                                         T omega) {
+  const int64_t stride = blockDim.x;
+  for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kV * stride) {
+    T a[kV], b[kV], d[kV];
+#pragma unroll
+    for (int u = 0; u < kV; u++) {
+      const int64_t q = rb + u * stride;
+      const bool ok = q < c.r1;
+      a[u] = ok ? r[q] : (T)0;
+      b[u] = ok && beta != (T)0 ? p[q] : (T)0;
+      d[u] = ok && beta != (T)0 ? v[q] : (T)0;
+    }
+#pragma unroll
+    for (int u = 0; u < kV; u++) {
+      const int64_t q = rb + u * stride;
+      if (q < c.r1) p[q] = a[u] + beta * (b[u] - omega * d[u]);
+    }
+  }
+}
+
+// out = A x; returns the thread's parts of <out, d0> and <out, d1> (d1 may be null).
+template <typename T, bool kGrid>
+__device__ __noinline__ DotAcc<T> ph_matvec(Ctx<T, kGrid> c, const T *x, T *out, const T *d0,
+                                            const T *d1) {
+  const PackView &pv = *c.pv;
+  const ImView &iv = *c.iv;
+  const int64_t stride = blockDim.x;
+  const T *DT = sizeof(T) == 4 ? (const T *)(const void *)iv.diagf : (const T *)(const void *)iv.diag;
+  const T *GT = sizeof(T) == 4 ? (const T *)(const void *)iv.gf : (const T *)(const void *)iv.g64;
+  DotAcc<T> acc;
+#pragma unroll
+  for (int i = 0; i < kG; i++) acc.v[i] = 0;
+  for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kU * stride) {
+    T y[kU], e0[kU], e1[kU];
+    uint8_t fl[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int64_t q = rb + u * stride;
+      e0[u] = q < c.r1 ? d0[q] : (T)0;
+      e1[u] = q < c.r1 && d1 ? d1[q] : (T)0;
+    }
+    apply_rows<kU>(pv, iv, DT, GT, x, rb, stride, c.r1, y, fl);
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int64_t q = rb + u * stride;
+      if (q < c.r1) out[q] = y[u];
+      acc.v[0] += y[u] * e0[u];
+      acc.v[1] += y[u] * e1[u];
+    }
+  }
+  return acc;
+}
+
+// s = r - alpha v; returns the thread's part of ||s||^2.
+template <typename T, bool kGrid>
+__device__ __noinline__ T ph_bicg_s(Ctx<T, kGrid> c, const T *r, const T *v, T alpha, T *s) {
+  const int64_t stride = blockDim.x;
+  T acc = 0;
+  for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kV * stride) {
+    T a[kV], b[kV];
+#pragma unroll
+    for (int u = 0; u < kV; u++) {
+      const int64_t q = rb + u * stride;
+      a[u] = q < c.r1 ? r[q] : (T)0;
+      b[u] = q < c.r1 ? v[q] : (T)0;
+    }
+#pragma unroll
+    for (int u = 0; u < kV; u++) {
+      const int64_t q = rb + u * stride;
+      const T x = a[u] - alpha * b[u];
+      if (q < c.r1) s[q] = x;
+      acc += x * x;
+    }
+  }
+  return acc;
+}
+
+// V += alpha ph + omega sh (FP64 accumulation; identity rows keep their value) and
+// r = s - omega t; returns the thread's parts of ||r||^2 and <rh, r>.
+template <typename T, bool kGrid>
+__device__ __noinline__ DotAcc<T> ph_bicg_x(Ctx<T, kGrid> c, const T *ph, const T *sh,
+                                            const T *s, const T *t, T alpha, T omega, T *r,
+                                            const T *rh, double *Vout) {
+  const int64_t stride = blockDim.x;
+  const uint8_t *rowf = c.iv->rowf;
+  DotAcc<T> acc;
+#pragma unroll
+  for (int i = 0; i < kG; i++) acc.v[i] = 0;
+  for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kU * stride) {
+    T a[kU], b[kU], e[kU], f[kU], h[kU];
+    uint8_t fl[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int64_t q = rb + u * stride;
+      const bool ok = q < c.r1;
+      a[u] = ok ? ph[q] : (T)0;
+      b[u] = ok ? sh[q] : (T)0;
+      e[u] = ok ? s[q] : (T)0;
+      f[u] = ok ? t[q] : (T)0;
+      h[u] = ok ? rh[q] : (T)0;
+      fl[u] = ok ? rowf[q] : (uint8_t)R_IDENT;
+    }
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int64_t q = rb + u * stride;
+      const T rn = e[u] - omega * f[u];
+      if (q < c.r1) r[q] = rn;
+      if (!(fl[u] & R_IDENT)) Vout[q] += (double)(alpha * a[u] + omega * b[u]);
+      acc.v[0] += rn * rn;
+      acc.v[1] += rn * h[u];
+    }
+  }
+  return acc;
+}
+
+// One refinement cycle of BiCGSTAB on A d = r0 (r0 in W_0, ||r0|| = res), accumulating
+// d into V.  Stops at the cycle target, after iv.m iterations, at the budget, or on a
+// breakdown (the next cycle restarts from the true residual).
+template <typename T, bool kGrid>
+__device__ __forceinline__ void bicgstab_cycle(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared &S,
+                                               int &parity, double res, double cycle_target,
+                                               int budget, int &iters, double *Vout) {
+  const ImView &iv = *c.iv;
+  const int64_t N = c.pv->ntot;
+  T *rh = c.w.Wb, *r1 = c.w.Wb + N, *p = c.w.Wb + 2 * N, *v = c.w.Wb + 3 * N;
+  T *ph = c.w.Z, *sh = c.w.Z + N, *s = c.w.Z + 2 * N, *t = c.w.Z + 3 * N;
+  const T *r = rh;  // the first iteration reads r0 itself
+  double rho = res * res, rho_prev = 1.0, alpha = 1.0, omega = 1.0;
+  for (int it = 0; it < iv.m && iters < budget; it++) {
+    const double beta = it == 0 ? 0.0 : (rho / rho_prev) * (alpha / omega);
+    ph_bicg_dir(c, r, p, v, (T)beta, (T)omega);
+    group_sync<kGrid>(grid);
+    apply_precond(c, p, ph);
+    group_sync<kGrid>(grid);
+    {
+      DotAcc<T> acc = ph_matvec(c, ph, v, rh, (const T *)nullptr);
+      group_reduce<kGrid>(grid, acc.v, 1, S, iv.partials, parity);
+    }
+    const double rv = S.red[0];
+    if (rv == 0.0 || !(rv == rv) || !(rho == rho)) break;  // breakdown: restart from r0
+    alpha = rho / rv;
+    {
+      T acc[1] = {ph_bicg_s(c, r, v, (T)alpha, s)};
+      group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);
+    }
+    iters++;
+    if (sqrt(S.red[0]) <= cycle_target) {  // x += alpha ph completes the cycle
+      ph_bicg_x(c, ph, ph, s, s, (T)alpha, (T)0, r1, rh, Vout);
+      group_sync<kGrid>(grid);
+      break;
+    }
+    apply_precond(c, s, sh);
+    group_sync<kGrid>(grid);
+    {
+      DotAcc<T> acc = ph_matvec(c, sh, t, s, t);
+      group_reduce<kGrid>(grid, acc.v, 2, S, iv.partials, parity);
+    }
+    const double ts = S.red[0], tt = S.red[1];
+    omega = tt > 0.0 ? ts / tt : 0.0;
+    {
+      DotAcc<T> acc = ph_bicg_x(c, ph, sh, s, t, (T)alpha, (T)omega, r1, rh, Vout);
+      group_reduce<kGrid>(grid, acc.v, 2, S, iv.partials, parity);
+    }
+    r = r1;
+    const double rn = sqrt(S.red[0]);
+    rho_prev = rho;
+    rho = S.red[1];
+    if (rn <= cycle_target || omega == 0.0 || rho == 0.0) break;
+  }
+  group_sync<kGrid>(grid);  // V complete before the next true residual
+}
+
 // One backward-Euler step of one group (CTA or grid) for instance `inst`.
 template <typename T, bool kGrid>
 __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid,
@@ -1177,6 +1355,10 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
       break;
     }
     if (iters >= budget) break;
+    if (iv.krylov == NRT_BICGSTAB) {
+      bicgstab_cycle(c, grid, S, parity, res, fmax(target, inner_rel * res), budget, iters, Vout);
+      continue;
+    }
     apply_precond(c, c.w.Wb, c.w.Z);
     group_sync<kGrid>(grid);  // Z_0 of every row visible before the SpMV
     if (threadIdx.x == 0) {
@@ -1682,6 +1864,7 @@ int Engine::implicit_init() {
   iv.ntot = N;
   iv.m = opt.restart;
   iv.precond = opt.precond;
+  iv.krylov = opt.krylov;
   iv.tol_mode = opt.tol_mode;
   iv.tol = opt.tol;
   iv.max_iter = opt.max_iter;

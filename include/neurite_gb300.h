@@ -50,7 +50,9 @@ typedef enum nrt_precision {
 
 typedef enum nrt_krylov {
   NRT_GMRES = 0,          /* restarted GMRES(m), classical Gram-Schmidt */
-  NRT_BICGSTAB = 1        /* unpreconditioned-form BiCGSTAB, src/solverIm-gpu.cpp:725-843 */
+  NRT_BICGSTAB = 1        /* BiCGSTAB, src/solverIm-gpu.cpp:725-843; right-preconditioned by
+                             precond (NRT_PRECOND_NONE: the reference's form), at most
+                             `restart` (>= 3) iterations per FP64 refinement cycle */
 } nrt_krylov;
 
 typedef enum nrt_precond {

@@ -176,3 +176,46 @@ def test_tree_preconditioner_needs_few_iterations(gpu, pkg, model):
     st = s.stats()
     assert st.nonconverged_steps == 0
     assert st.krylov_iters <= 20 * 3
+
+
+@pytest.mark.parametrize("name", golden_names("i"))
+@pytest.mark.parametrize("precond", ["none", "segment", "tree"])
+def test_bicgstab_fp64_matches_exact_solution(gpu, pkg, orc, name, precond):
+    """BiCGSTAB, the reference GPU solver's method (src/solverIm-gpu.cpp:725-843); with
+    precond="none" it is the reference's unpreconditioned form."""
+    g = load_golden(name)
+    spec = g["spec"]
+    steps = int(g["numStepsT"]) - 2
+    s = pkg.SolverIm(problem(pkg, g), **tight(krylov="bicgstab", precond=precond, max_iter=20000))
+    s.run(1, 1 + steps, spec.init_time, spec.end_input)
+    d = orc.derive(spec)
+    Vo, _, _, _ = orc.implicit_run(spec, d, float(g["dT"]), 1, 1 + steps, linsolve=0)
+    assert np.abs(s.snapshot() - Vo).max() < TOL_FP64
+    st = s.stats()
+    assert st.nonconverged_steps == 0 and st.krylov_iters > 0
+    s.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_bicgstab_batch_and_cooperative(gpu, pkg, orc, model, precision):
+    """BiCGSTAB with the tree preconditioner in a batch and on the whole-GPU launch."""
+    opts = tight(krylov="bicgstab", precond="tree") if precision == "fp64" else dict(
+        precision="mixed", krylov="bicgstab", restart=20, tol=1e-10, tol_mode="rel", precond="tree")
+    tol = TOL_FP64 if precision == "fp64" else TOL_MIXED
+    specs = [model.random_tree(seed=s, n_target=n, dt=2.5e-5, tspan=1e-3)
+             for s, n in [(11, 2500), (12, 800), (13, 7000)]]
+    probs = [pkg.ProblemArrays.from_spec(sp, pkg.derive(sp)) for sp in specs]
+    b = pkg.Batch(probs, mode=1, **opts)
+    b.set_runs([(1, 21, sp.init_time, sp.end_input) for sp in specs])
+    b.advance(20)
+    for k, sp in enumerate(specs):
+        Vo, _, _, _ = orc.implicit_run(sp, orc.derive(sp), sp.dt_abs, 1, 21, linsolve=0)
+        assert np.abs(b.snapshot(k) - Vo).max() < tol
+    assert b.stats().nonconverged_steps == 0
+    b.close()
+    spec = model.random_binary_tree(depth=7, seed=3, dt=2.5e-5, tspan=5e-3)
+    s = pkg.SolverIm(pkg.ProblemArrays.from_spec(spec, pkg.derive(spec)), **opts)
+    s.run(1, 11, spec.init_time, spec.end_input)
+    Vo, _, _, _ = orc.implicit_run(spec, orc.derive(spec), spec.dt_abs, 1, 11, linsolve=0)
+    assert np.abs(s.snapshot() - Vo).max() < tol
+    s.close()
