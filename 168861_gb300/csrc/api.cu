@@ -368,6 +368,7 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   pv.hp_ld = host.hp_ld;
   pv.hp_inst = host.hp_inst ? 1 : 0;
   pv.hp_cls = nullptr;
+  pv.hh_dense = 2 * (int64_t)host.hh_local.size() >= N ? 1 : 0;
   if (!host.hp_cls.empty()) {
     uint32_t *pc = nullptr;
     TRY(upload(arena, pc, host.hp_cls.data(), N, st));

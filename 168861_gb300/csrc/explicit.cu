@@ -108,27 +108,47 @@ __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, in
                                                            float *__restrict__ Fout) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= p.ntot) return;
+  const int64_t N = p.ntot;
+  // Loads that do not depend on the topology record go out together with it: the
+  // element's own state and its neighbours j-1 and j+1 (the mother and DR of nearly
+  // every element in the reference numbering), so most elements wait for one round trip.
+  const int64_t jm = j > 0 ? j - 1 : j, jp = j + 1 < N ? j + 1 : j;
   const Topo tj = p.topo[j];
-  const InstDev in = p.inst[tj.flags >> INST_SHIFT];
+  const float f0 = Fin[j], fm = Fin[jm], fp = Fin[jp];
+  const float g0 = p.gaxf[j], gp = p.gaxf[jp];
+  const double v64 = Vin[j];
+  const float cdt = p.cdtf[j];
+  const uint32_t cls = p.hp_cls ? p.hp_cls[j] : 0u;
+  float m0 = 0.f, h0 = 0.f, n0 = 0.f;
+  if (p.hh_dense) {
+    m0 = p.gatef[j];
+    h0 = p.gatef[N + j];
+    n0 = p.gatef[2 * N + j];
+  }
+  const uint32_t inst = tj.flags >> INST_SHIFT;
+  const InstDev in = p.inst[inst];
   const int64_t i = in.base + k;
   if (i >= in.iend) {
-    Vout[j] = Vin[j];
-    Fout[j] = Fin[j];
+    Vout[j] = v64;
+    Fout[j] = f0;
     return;
   }
-  const int64_t N = p.ntot;
   const bool term = (tj.flags & F_TERM) != 0;
   if (term && !(tj.flags & F_HH)) return;
   const int64_t self = (kGeneral || !term) ? j : ghost_source(tj, j);
-  const float vf = Fin[self];
+  const float vf = self == j ? f0 : (self == jm ? fm : (self == jp ? fp : Fin[self]));
   float wdx, kdx;
   if (tj.flags & F_HH) {
+    if (!p.hh_dense) {
+      m0 = p.gatef[j];
+      h0 = p.gatef[N + j];
+      n0 = p.gatef[2 * N + j];
+    }
     const int64_t L = p.hp_ld;
-    const float *hp = p.hpf + hp_col(p, j, tj.flags >> INST_SHIFT);
+    const float *hp = p.hpf + (p.hp_cls ? (int64_t)cls : (p.hp_inst ? (int64_t)inst : j));
     const float dv = vf - hp[HP_REST * L];
-    GateStep32 g = hh_step32(dv + hp[HP_LSNA * L], dv + hp[HP_LSK * L], p.gatef[j],
-                             p.gatef[N + j], p.gatef[2 * N + j], hp[HP_DTMS * L],
-                             hp[HP_GNA * L], hp[HP_GK * L], hp[HP_GL * L],
+    GateStep32 g = hh_step32(dv + hp[HP_LSNA * L], dv + hp[HP_LSK * L], m0, h0, n0,
+                             hp[HP_DTMS * L], hp[HP_GNA * L], hp[HP_GK * L], hp[HP_GL * L],
                              hp[HP_ENA * L], hp[HP_EK * L], hp[HP_EL * L]);
     p.gatef[j] = g.m;
     p.gatef[N + j] = g.h;
@@ -145,11 +165,18 @@ __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, in
   float acc = 0.0f;
   if ((tj.flags & F_BRANCH) && (kGeneral || !(tj.flags & F_DL_TERM)))
     acc = (Fin[tj.dl] - vf) * p.gaxf[tj.dl];
-  if (kGeneral || !(tj.flags & F_DR_TERM)) acc = fmaf(Fin[tj.dr] - vf, p.gaxf[tj.dr], acc);
-  if (kGeneral || !(tj.flags & F_MO_TERM)) acc = fmaf(Fin[tj.mother] - vf, p.gaxf[j], acc);
+  if (kGeneral || !(tj.flags & F_DR_TERM)) {
+    const bool adj = tj.dr == jp && jp != j;
+    const float fd = adj ? fp : Fin[tj.dr], gd = adj ? gp : p.gaxf[tj.dr];
+    acc = fmaf(fd - vf, gd, acc);
+  }
+  if (kGeneral || !(tj.flags & F_MO_TERM)) {
+    const float fo = (tj.mother == jm && jm != j) ? fm : Fin[tj.mother];
+    acc = fmaf(fo - vf, g0, acc);
+  }
   acc = fmaf(wdx, vf, acc) + kdx;
   if (active && (tj.flags & F_INP)) acc += p.inpf[j];
-  const double vn = Vin[j] + (double)(p.cdtf[j] * acc);
+  const double vn = v64 + (double)(cdt * acc);
   Vout[j] = vn;
   Fout[j] = (float)vn;
 }

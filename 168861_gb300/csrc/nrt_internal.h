@@ -90,6 +90,7 @@ struct PackView {
   int64_t hp_ld;       // number of columns
   int hp_inst;         // 1: column = instance
   const uint32_t *hp_cls;  // column per element (class tables), or null
+  int hh_dense;        // most elements are HH: the step loads gates before the topology
   const float *cdtf, *gaxf, *wdxf, *kdxf, *inpf;  // FP32 copies (mixed path)
   InstDev *inst;
 };
