@@ -86,7 +86,7 @@ struct InstStat {
 
 struct ImView {
   int64_t ntot;
-  int m;             // restart (GMRES) / iterations per refinement cycle (BiCGSTAB)
+  int m;             // GMRES restart (BiCGSTAB: sizes the shared work vectors only)
   int krylov;        // NRT_GMRES or NRT_BICGSTAB
   int precond;
   int tol_mode;
@@ -1257,8 +1257,9 @@ __device__ __noinline__ DotAcc<T> ph_bicg_x(Ctx<T, kGrid> c, const T *ph, const 
 }
 
 // One refinement cycle of BiCGSTAB on A d = r0 (r0 in W_0, ||r0|| = res), accumulating
-// d into V.  Stops at the cycle target, after iv.m iterations, at the budget, or on a
-// breakdown (the next cycle restarts from the true residual).
+// d into V.  Stops at the cycle target, at the budget, or on a breakdown (the next cycle
+// restarts from the true residual).  Every pass through the loop counts against the
+// budget, so repeated breakdowns still end the step.
 template <typename T, bool kGrid>
 __device__ __forceinline__ void bicgstab_cycle(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared &S,
                                                int &parity, double res, double cycle_target,
@@ -1269,7 +1270,7 @@ __device__ __forceinline__ void bicgstab_cycle(Ctx<T, kGrid> &c, cg::grid_group 
   T *ph = c.w.Z, *sh = c.w.Z + N, *s = c.w.Z + 2 * N, *t = c.w.Z + 3 * N;
   const T *r = rh;  // the first iteration reads r0 itself
   double rho = res * res, rho_prev = 1.0, alpha = 1.0, omega = 1.0;
-  for (int it = 0; it < iv.m && iters < budget; it++) {
+  for (int it = 0; iters < budget; it++) {
     const double beta = it == 0 ? 0.0 : (rho / rho_prev) * (alpha / omega);
     ph_bicg_dir(c, r, p, v, (T)beta, (T)omega);
     group_sync<kGrid>(grid);
@@ -1280,7 +1281,10 @@ __device__ __forceinline__ void bicgstab_cycle(Ctx<T, kGrid> &c, cg::grid_group 
       group_reduce<kGrid>(grid, acc.v, 1, S, iv.partials, parity);
     }
     const double rv = S.red[0];
-    if (rv == 0.0 || !(rv == rv) || !(rho == rho)) break;  // breakdown: restart from r0
+    if (rv == 0.0 || !(rv == rv) || !(rho == rho)) {  // breakdown: restart from r0
+      iters++;
+      break;
+    }
     alpha = rho / rv;
     {
       T acc[1] = {ph_bicg_s(c, r, v, (T)alpha, s)};
@@ -1354,7 +1358,7 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
       converged = true;
       break;
     }
-    if (iters >= budget) break;
+    if (iters >= budget || !(res == res)) break;  // budget spent, or the state is not finite
     if (iv.krylov == NRT_BICGSTAB) {
       bicgstab_cycle(c, grid, S, parity, res, fmax(target, inner_rel * res), budget, iters, Vout);
       continue;

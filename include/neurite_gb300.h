@@ -51,8 +51,8 @@ typedef enum nrt_precision {
 typedef enum nrt_krylov {
   NRT_GMRES = 0,          /* restarted GMRES(m), classical Gram-Schmidt */
   NRT_BICGSTAB = 1        /* BiCGSTAB, src/solverIm-gpu.cpp:725-843; right-preconditioned by
-                             precond (NRT_PRECOND_NONE: the reference's form), at most
-                             `restart` (>= 3) iterations per FP64 refinement cycle */
+                             precond (NRT_PRECOND_NONE: the reference's form); restarts only
+                             for FP64 refinement (mixed) or a breakdown; needs restart >= 3 */
 } nrt_krylov;
 
 typedef enum nrt_precond {

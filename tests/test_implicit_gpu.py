@@ -182,10 +182,13 @@ def test_tree_preconditioner_needs_few_iterations(gpu, pkg, model):
 @pytest.mark.parametrize("precond", ["none", "segment", "tree"])
 def test_bicgstab_fp64_matches_exact_solution(gpu, pkg, orc, name, precond):
     """BiCGSTAB, the reference GPU solver's method (src/solverIm-gpu.cpp:725-843); with
-    precond="none" it is the reference's unpreconditioned form."""
+    precond="none" it is the reference's unpreconditioned form, which needs hundreds of
+    iterations per step on these stiff trees, so that case runs a few steps only."""
     g = load_golden(name)
     spec = g["spec"]
     steps = int(g["numStepsT"]) - 2
+    if precond == "none":
+        steps = min(steps, 5)
     s = pkg.SolverIm(problem(pkg, g), **tight(krylov="bicgstab", precond=precond, max_iter=20000))
     s.run(1, 1 + steps, spec.init_time, spec.end_input)
     d = orc.derive(spec)
