@@ -525,7 +525,7 @@ int nrt_options_default(nrt_options *o) {
   o->mode = NRT_EXPLICIT;
   o->precision = NRT_FP64;
   o->krylov = NRT_GMRES;
-  o->precond = NRT_PRECOND_SEGMENT;
+  o->precond = NRT_PRECOND_TREE;
   o->restart = 30;
   o->tol_mode = NRT_TOL_ABS;
   o->tol = 1e-14;  // RANGE_ERROR, inc/configuration.h:16

@@ -116,7 +116,7 @@ class ProblemArrays:
 
 
 def make_options(mode: int, precision: str = "fp64", krylov: str = "gmres",
-                 precond: str = "segment", restart: int = 30, tol: float = 1e-14,
+                 precond: str = "tree", restart: int = 30, tol: float = 1e-14,
                  tol_mode: str = "abs", max_iter: int = 0, use_graphs: bool = True,
                  device: int = -1, schedule: int = 0) -> _lib.Options:
     lib = _lib.load()

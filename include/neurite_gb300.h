@@ -125,7 +125,7 @@ typedef struct nrt_stats {
 
 typedef struct nrt_solver nrt_solver;
 
-/* Fills the defaults: explicit, FP64, GMRES(30), segment preconditioner, absolute
+/* Fills the defaults: explicit, FP64, GMRES(30), exact tree preconditioner, absolute
  * tolerance 1e-14 (RANGE_ERROR, inc/configuration.h:16), max_iter 0, device -1. */
 int nrt_options_default(nrt_options *opt);
 

@@ -149,7 +149,7 @@ class SolverExGB300 : public neurite_gb300::SolverGB300 {
 };
 
 // Replaces `new SolverImGPU(...)` (src/neurite.cpp:193-194).  Default: plain FP64,
-// segment-preconditioned GMRES(30), ||r||_2 <= 1e-14 (the reference's RANGE_ERROR test).
+// tree-preconditioned GMRES(30), ||r||_2 <= 1e-14 (the reference's RANGE_ERROR test).
 class SolverImGB300 : public neurite_gb300::SolverGB300 {
  public:
   SolverImGB300(TYPE dT, TYPE **potential, int num_term, int *ind_terminals, TYPE input_val,
