@@ -4,6 +4,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <thread>
+#include <atomic>
 #include <memory>
 #include <new>
 #include <string>
@@ -110,10 +112,71 @@ static int validate_problem(const nrt_problem *p, bool strict, std::string &why)
 
 // ------------------------------------------------------------------ packing
 
+// Runs f(i) for every i in [0, n) on the host's cores, handing out indices one at a time
+// (instances differ in size by orders of magnitude).
+template <class F>
+static void parallel_for(int32_t n, F f) {
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = std::max(1u, std::min(nt, 64u));
+  nt = (unsigned)std::max<int32_t>(1, std::min<int32_t>((int32_t)nt, n));
+  std::atomic<int32_t> next(0);
+  auto work = [&]() {
+    for (;;) {
+      const int32_t i = next.fetch_add(1);
+      if (i >= n) break;
+      f(i);
+    }
+  };
+  std::vector<std::thread> th;
+  for (unsigned t = 1; t < nt; t++) th.emplace_back(work);
+  work();
+  for (std::thread &t : th) t.join();
+}
+
+namespace {
+
+// One HH parameter set in HP_* row order.
+struct HHKey {
+  double v[HP_ROWS];
+  bool operator==(const HHKey &o) const { return memcmp(v, o.v, sizeof(v)) == 0; }
+};
+struct HHKeyHash {
+  size_t operator()(const HHKey &k) const {
+    uint64_t h = 1469598103934665603ull;  // FNV-1a over the bytes
+    const unsigned char *b = (const unsigned char *)k.v;
+    for (size_t q = 0; q < sizeof(k.v); q++) h = (h ^ b[q]) * 1099511628211ull;
+    return (size_t)h;
+  }
+};
+
+HHKey hh_key(const nrt_problem &p, int32_t k) {
+  HHKey key;
+  key.v[HP_GNA] = p.g_Na[k];
+  key.v[HP_GK] = p.g_K[k];
+  key.v[HP_GL] = p.G_L[k];
+  key.v[HP_ENA] = p.E_Na[k];
+  key.v[HP_EK] = p.E_K[k];
+  key.v[HP_EL] = p.E_L[k];
+  key.v[HP_LSNA] = p.ls_Na[k];
+  key.v[HP_LSK] = p.ls_K[k];
+  key.v[HP_REST] = p.rest[k];
+  key.v[HP_DX] = p.dx[p.hh_elem[k]];
+  key.v[HP_DTMS] = p.dT * 1000;  // src/solverEx-cpu.cpp:96
+  return key;
+}
+
+}  // namespace
+
 int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
   hp.ninst = count;
   hp.off.assign(count + 1, 0);
-  for (int32_t i = 0; i < count; i++) hp.off[i + 1] = hp.off[i] + probs[i].num_elem;
+  hp.hh_off.assign(count + 1, 0);
+  std::vector<int64_t> term_off(count + 1, 0);
+  for (int32_t i = 0; i < count; i++) {
+    hp.off[i + 1] = hp.off[i] + probs[i].num_elem;
+    hp.hh_off[i + 1] = hp.hh_off[i] + probs[i].num_hh;
+    term_off[i + 1] = term_off[i] + probs[i].num_term;
+  }
   const int64_t N = hp.ntot = hp.off[count];
   if (N >= ((int64_t)1 << 31)) return fail(NRT_EINVAL, "total elements exceed 2^31");
   if (count >= (1 << (32 - INST_SHIFT))) return fail(NRT_EINVAL, "too many instances");
@@ -122,14 +185,16 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
   hp.V0.resize(N); hp.V1.resize(N);
   hp.c_m_dx.resize(N); hp.radx.resize(N); hp.Wfull.resize(N); hp.Kfull.resize(N);
   hp.gate.assign(3 * N, 0.0);
-  hp.hp.assign((size_t)HP_ROWS * N, 0.0);
   hp.inst.resize(count);
   hp.num_elem.resize(count);
-  hp.hh_off.assign(count + 1, 0);
-  hp.hh_local.clear();
-  hp.terms.clear();
-  hp.fusable = true;
-  for (int32_t i = 0; i < count; i++) {
+  hp.hh_local.resize(hp.hh_off[count]);
+  hp.terms.resize(term_off[count]);
+  // Per instance: everything element-indexed, plus the instance's distinct HH parameter
+  // sets in order of first appearance and each HH element's index among them.
+  std::vector<char> fusable(count, 1), invariant(count, 1);
+  std::vector<std::vector<HHKey>> local_keys(count);
+  std::vector<uint32_t> cls(N, 0);
+  parallel_for(count, [&](int32_t i) {
     const nrt_problem &p = probs[i];
     const int64_t o = hp.off[i];
     const int32_t n = p.num_elem;
@@ -138,6 +203,7 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
     for (int32_t q = 0; q < p.num_term; q++) is_term[p.terminals[q]] = 1;
     std::vector<char> is_hh(n, 0);
     for (int32_t k = 0; k < p.num_hh; k++) is_hh[p.hh_elem[k]] = 1;
+    auto src_of = [&](int32_t t_) { return t_ == p.terminals[0] ? t_ + 1 : p.mother[t_]; };
     for (int32_t j = 0; j < n; j++) {
       Topo t;
       t.mother = (int32_t)(o + (p.mother[j] >= 0 ? p.mother[j] : j));
@@ -150,16 +216,15 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
       if (j == p.terminals[0]) f |= F_ROOT;
       if (p.input[j] != 0.0) f |= F_INP;
       // Flux through a terminal neighbour is zero when that terminal copies this element.
-      auto src_of = [&](int32_t t_) { return t_ == p.terminals[0] ? t_ + 1 : p.mother[t_]; };
       if (!is_term[j]) {
         if (p.branching[j] && is_term[p.dl[j]]) {
-          if (src_of(p.dl[j]) == j) f |= F_DL_TERM; else hp.fusable = false;
+          if (src_of(p.dl[j]) == j) f |= F_DL_TERM; else fusable[i] = 0;
         }
         if (is_term[p.dr[j]]) {
-          if (src_of(p.dr[j]) == j) f |= F_DR_TERM; else hp.fusable = false;
+          if (src_of(p.dr[j]) == j) f |= F_DR_TERM; else fusable[i] = 0;
         }
         if (p.mother[j] >= 0 && is_term[p.mother[j]]) {
-          if (src_of(p.mother[j]) == j) f |= F_MO_TERM; else hp.fusable = false;
+          if (src_of(p.mother[j]) == j) f |= F_MO_TERM; else fusable[i] = 0;
         }
       }
       t.flags = f | ((uint32_t)i << INST_SHIFT);
@@ -179,29 +244,33 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
     }
     for (int32_t q = 0; q < p.num_term; q++) {
       const int32_t t = p.terminals[q];
-      hp.terms.push_back(o + t);
+      hp.terms[term_off[i] + q] = o + t;
       const int32_t src = (q == 0 || t == p.terminals[0]) ? t + 1 : p.mother[t];
-      if (p.V0[t] != p.V0[src]) hp.invariant = false;
+      if (p.V0[t] != p.V0[src]) invariant[i] = 0;
     }
+    std::vector<HHKey> &keys = local_keys[i];
+    uint32_t prev = UINT32_MAX;
     for (int32_t k = 0; k < p.num_hh; k++) {
       const int64_t e = o + p.hh_elem[k];
-      hp.hh_local.push_back(p.hh_elem[k]);
+      hp.hh_local[hp.hh_off[i] + k] = p.hh_elem[k];
       hp.gate[e] = p.m[k];
       hp.gate[N + e] = p.h[k];
       hp.gate[2 * N + e] = p.n[k];
-      hp.hp[HP_GNA * N + e] = p.g_Na[k];
-      hp.hp[HP_GK * N + e] = p.g_K[k];
-      hp.hp[HP_GL * N + e] = p.G_L[k];
-      hp.hp[HP_ENA * N + e] = p.E_Na[k];
-      hp.hp[HP_EK * N + e] = p.E_K[k];
-      hp.hp[HP_EL * N + e] = p.E_L[k];
-      hp.hp[HP_LSNA * N + e] = p.ls_Na[k];
-      hp.hp[HP_LSK * N + e] = p.ls_K[k];
-      hp.hp[HP_REST * N + e] = p.rest[k];
-      hp.hp[HP_DX * N + e] = p.dx[p.hh_elem[k]];
-      hp.hp[HP_DTMS * N + e] = p.dT * 1000;  // src/solverEx-cpu.cpp:96
+      const HHKey key = hh_key(p, k);
+      if (prev == UINT32_MAX || !(key == keys[prev])) {
+        prev = UINT32_MAX;
+        for (size_t c = 0; c < keys.size() && c < 64; c++)
+          if (keys[c] == key) {
+            prev = (uint32_t)c;
+            break;
+          }
+        if (prev == UINT32_MAX) {
+          prev = (uint32_t)keys.size();
+          keys.push_back(key);
+        }
+      }
+      cls[e] = prev;
     }
-    hp.hh_off[i + 1] = (int64_t)hp.hh_local.size();
     InstDev in;
     in.base = 0;
     in.iend = INT64_MAX;
@@ -210,79 +279,63 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
     in.t1 = -1;
     set_window(in);
     hp.inst[i] = in;
-  }
-  // One parameter column per instance when every HH element of each instance carries
-  // the same parameters (then the step reads them from a small, cached table).
+  });
+  hp.fusable = std::all_of(fusable.begin(), fusable.end(), [](char c) { return c != 0; });
+  hp.invariant = std::all_of(invariant.begin(), invariant.end(), [](char c) { return c != 0; });
+  // HH parameter columns.  One per instance when every HH element of each instance
+  // carries the same parameters; else one per distinct set (class), merged across
+  // instances in instance order, while there are at most N/4 sets; else one per element.
   hp.hp_inst = true;
-  for (int32_t i = 0; i < count && hp.hp_inst; i++) {
-    const int64_t a = hp.hh_off[i], b = hp.hh_off[i + 1];
-    for (int64_t k = a + 1; k < b && hp.hp_inst; k++) {
-      const int64_t e0 = hp.off[i] + hp.hh_local[a], e = hp.off[i] + hp.hh_local[k];
-      for (int r = 0; r < HP_ROWS; r++)
-        if (memcmp(&hp.hp[(size_t)r * N + e0], &hp.hp[(size_t)r * N + e], sizeof(double)) != 0) {
-          hp.hp_inst = false;
-          break;
-        }
-    }
-  }
+  for (int32_t i = 0; i < count; i++)
+    if (local_keys[i].size() > 1) hp.hp_inst = false;
   if (hp.hp_inst) {
-    std::vector<double> tab((size_t)HP_ROWS * count, 0.0);
-    for (int32_t i = 0; i < count; i++) {
-      if (hp.hh_off[i + 1] == hp.hh_off[i]) continue;
-      const int64_t e0 = hp.off[i] + hp.hh_local[hp.hh_off[i]];
-      for (int r = 0; r < HP_ROWS; r++) tab[(size_t)r * count + i] = hp.hp[(size_t)r * N + e0];
-    }
-    hp.hp.swap(tab);
+    hp.hp.assign((size_t)HP_ROWS * count, 0.0);
+    for (int32_t i = 0; i < count; i++)
+      if (!local_keys[i].empty())
+        for (int r = 0; r < HP_ROWS; r++) hp.hp[(size_t)r * count + i] = local_keys[i][0].v[r];
     hp.hp_ld = count;
     return NRT_OK;
   }
-  // Otherwise: distinct parameter sets (consecutive elements mostly share one).
-  struct Key {
-    double v[HP_ROWS];
-    bool operator==(const Key &o) const { return memcmp(v, o.v, sizeof(v)) == 0; }
-  };
-  struct KeyHash {
-    size_t operator()(const Key &k) const {
-      uint64_t h = 1469598103934665603ull;
-      const unsigned char *b = (const unsigned char *)k.v;
-      for (size_t q = 0; q < sizeof(k.v); q++) h = (h ^ b[q]) * 1099511628211ull;
-      return (size_t)h;
-    }
-  };
-  std::unordered_map<Key, uint32_t, KeyHash> ids;
-  std::vector<uint32_t> cls(N, 0);
-  std::vector<Key> keys;
-  Key prev{};
-  uint32_t prev_id = UINT32_MAX;
-  for (int32_t i = 0; i < count; i++) {
-    for (int64_t k = hp.hh_off[i]; k < hp.hh_off[i + 1]; k++) {
-      const int64_t e = hp.off[i] + hp.hh_local[k];
-      Key key;
-      for (int r = 0; r < HP_ROWS; r++) key.v[r] = hp.hp[(size_t)r * N + e];
-      if (prev_id == UINT32_MAX || !(key == prev)) {
-        auto it = ids.find(key);
-        if (it == ids.end()) {
-          it = ids.emplace(key, (uint32_t)keys.size()).first;
-          keys.push_back(key);
-        }
-        prev = key;
-        prev_id = it->second;
+  std::unordered_map<HHKey, uint32_t, HHKeyHash> ids;
+  std::vector<HHKey> keys;
+  std::vector<std::vector<uint32_t>> remap(count);
+  bool few = true;
+  for (int32_t i = 0; i < count && few; i++) {
+    for (const HHKey &k : local_keys[i]) {
+      auto it = ids.find(k);
+      if (it == ids.end()) {
+        it = ids.emplace(k, (uint32_t)keys.size()).first;
+        keys.push_back(k);
       }
-      cls[e] = prev_id;
+      remap[i].push_back(it->second);
     }
-    if ((int64_t)keys.size() * 4 > N) break;
+    few = (int64_t)keys.size() * 4 <= N;
   }
-  if ((int64_t)keys.size() * 4 > N || keys.empty()) {
-    hp.hp_ld = N;
+  if (few) {
+    parallel_for(count, [&](int32_t i) {
+      for (int64_t k = hp.hh_off[i]; k < hp.hh_off[i + 1]; k++) {
+        const int64_t e = hp.off[i] + hp.hh_local[k];
+        cls[e] = remap[i][cls[e]];
+      }
+    });
+    const size_t nc = keys.size();
+    hp.hp.assign((size_t)HP_ROWS * nc, 0.0);
+    for (size_t c = 0; c < nc; c++)
+      for (int r = 0; r < HP_ROWS; r++) hp.hp[(size_t)r * nc + c] = keys[c].v[r];
+    hp.hp_cls.swap(cls);
+    hp.hp_ld = (int64_t)nc;
     return NRT_OK;
   }
-  const size_t nc = keys.size();
-  std::vector<double> tab((size_t)HP_ROWS * nc);
-  for (size_t c = 0; c < nc; c++)
-    for (int r = 0; r < HP_ROWS; r++) tab[(size_t)r * nc + c] = keys[c].v[r];
-  hp.hp.swap(tab);
-  hp.hp_cls.swap(cls);
-  hp.hp_ld = (int64_t)nc;
+  hp.hp.assign((size_t)HP_ROWS * N, 0.0);
+  parallel_for(count, [&](int32_t i) {
+    const nrt_problem &p = probs[i];
+    for (int32_t k = 0; k < p.num_hh; k++) {
+      const int64_t e = hp.off[i] + p.hh_elem[k];
+      const HHKey key = hh_key(p, k);
+      for (int r = 0; r < HP_ROWS; r++) hp.hp[(size_t)r * N + e] = key.v[r];
+    }
+  });
+  hp.hp_ld = N;
   return NRT_OK;
 }
 
