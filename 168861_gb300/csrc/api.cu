@@ -112,27 +112,6 @@ static int validate_problem(const nrt_problem *p, bool strict, std::string &why)
 
 // ------------------------------------------------------------------ packing
 
-// Runs f(i) for every i in [0, n) on the host's cores, handing out indices one at a time
-// (instances differ in size by orders of magnitude).
-template <class F>
-static void parallel_for(int32_t n, F f) {
-  unsigned nt = std::thread::hardware_concurrency();
-  nt = std::max(1u, std::min(nt, 64u));
-  nt = (unsigned)std::max<int32_t>(1, std::min<int32_t>((int32_t)nt, n));
-  std::atomic<int32_t> next(0);
-  auto work = [&]() {
-    for (;;) {
-      const int32_t i = next.fetch_add(1);
-      if (i >= n) break;
-      f(i);
-    }
-  };
-  std::vector<std::thread> th;
-  for (unsigned t = 1; t < nt; t++) th.emplace_back(work);
-  work();
-  for (std::thread &t : th) t.join();
-}
-
 namespace {
 
 // One HH parameter set in HP_* row order.
@@ -431,8 +410,13 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   pv.inst = inst;
   if (mixed) {
     auto f32 = [&](const std::vector<double> &v) {
-      hostf.emplace_back(v.begin(), v.end());
-      return hostf.back().data();
+      hostf.emplace_back(v.size());
+      float *d = hostf.back().data();
+      const double *src = v.data();
+      parallel_ranges((int64_t)v.size(), [&](int64_t a, int64_t b) {
+        for (int64_t q = a; q < b; q++) d[q] = (float)src[q];
+      });
+      return d;
     };
     hostf.reserve(8);
     float *p;

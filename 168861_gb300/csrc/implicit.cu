@@ -1705,7 +1705,7 @@ int Engine::implicit_plan(size_t &bytes) {
   std::vector<char> is_term(N, 0);
   for (int64_t t : host.terms) is_term[t] = 1;
   S.rowf.assign(N, R_IDENT);
-  for (int32_t i = 0; i < ni; i++) {
+  parallel_for(ni, [&](int64_t i) {
     const int64_t o = host.off[i], n = host.num_elem[i];
     for (int64_t jl = 0; jl < n; jl++) {
       const int64_t j = o + jl;
@@ -1733,7 +1733,7 @@ int Engine::implicit_plan(size_t &bytes) {
       }
       S.rowf[j] = rf;
     }
-  }
+  });
   // Segment pieces: maximal runs of consecutive physical rows linked to their
   // predecessor (mother == j - 1 with a mother column), cut at kMaxPiece rows.
   S.inst_row.assign(host.off.begin(), host.off.end());
@@ -1878,14 +1878,16 @@ int Engine::implicit_init() {
   TRYI(up(arena, pr, S.rowf.data(), N, st)); iv.rowf = pr;
   std::vector<double> cmdt(N), g64(N), w64(N), k64(N), inp(N);
   std::vector<float> gf(N);
-  for (int64_t j = 0; j < N; j++) {
-    cmdt[j] = host.c_m_dx[j] / host.inst[host.topo[j].flags >> INST_SHIFT].dT;
-    g64[j] = host.gax[j];
-    gf[j] = (float)host.gax[j];
-    w64[j] = host.wdx[j];
-    k64[j] = host.kdx[j];
-    inp[j] = host.inp[j];
-  }
+  parallel_ranges(N, [&](int64_t a, int64_t b) {
+    for (int64_t j = a; j < b; j++) {
+      cmdt[j] = host.c_m_dx[j] / host.inst[host.topo[j].flags >> INST_SHIFT].dT;
+      g64[j] = host.gax[j];
+      gf[j] = (float)host.gax[j];
+      w64[j] = host.wdx[j];
+      k64[j] = host.kdx[j];
+      inp[j] = host.inp[j];
+    }
+  });
   double *p;
   TRYI(up(arena, p, cmdt.data(), N, st)); iv.cmdt = p;
   TRYI(up(arena, p, g64.data(), N, st)); iv.g64 = p;

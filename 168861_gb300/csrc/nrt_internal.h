@@ -3,7 +3,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+#include <atomic>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "neurite_gb300.h"
@@ -71,6 +74,34 @@ inline void set_window(InstDev &in) {
   while (below(i1 + 1)) i1++;
   in.ion = i0;
   in.ioff = i1;
+}
+
+// Runs f(i) for every i in [0, n) on the host's cores, handing out indices one at a time
+// (instances differ in size by orders of magnitude).
+template <class F>
+void parallel_for(int64_t n, F f) {
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = std::max(1u, std::min(nt, 64u));
+  nt = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)nt, n));
+  std::atomic<int64_t> next(0);
+  auto work = [&]() {
+    for (;;) {
+      const int64_t i = next.fetch_add(1);
+      if (i >= n) break;
+      f(i);
+    }
+  };
+  std::vector<std::thread> th;
+  for (unsigned t = 1; t < nt; t++) th.emplace_back(work);
+  work();
+  for (std::thread &t : th) t.join();
+}
+
+// f(a, b) over [0, n) in chunks of about 1M.
+template <class F>
+void parallel_ranges(int64_t n, F f) {
+  const int64_t chunk = 1 << 20, nc = (n + chunk - 1) / chunk;
+  parallel_for(nc, [&](int64_t c) { f(c * chunk, std::min(n, (c + 1) * chunk)); });
 }
 
 // Device-side view passed by value to the kernels.
