@@ -1260,11 +1260,15 @@ __device__ __noinline__ DotAcc<T> ph_bicg_x(Ctx<T, kGrid> c, const T *ph, const 
 // d into V.  Stops at the cycle target, at the budget, or on a breakdown (the next cycle
 // restarts from the true residual).  Every pass through the loop counts against the
 // budget, so repeated breakdowns still end the step.
+// Not inlined, so that the GMRES path's register allocation does not carry it.
+// Returns {parity, iters}.
 template <typename T, bool kGrid>
-__device__ __forceinline__ void bicgstab_cycle(Ctx<T, kGrid> &c, cg::grid_group &grid, Shared &S,
-                                               int &parity, double res, double cycle_target,
-                                               int budget, int &iters, double *Vout) {
+__device__ __noinline__ int2 bicgstab_cycle(Ctx<T, kGrid> c, int parity, double res,
+                                            double cycle_target, int budget, int iters,
+                                            double *Vout) {
   const ImView &iv = *c.iv;
+  cg::grid_group grid = cg::this_grid();
+  Shared S = carve(dyn_smem(), iv.m);
   const int64_t N = c.pv->ntot;
   T *rh = c.w.Wb, *r1 = c.w.Wb + N, *p = c.w.Wb + 2 * N, *v = c.w.Wb + 3 * N;
   T *ph = c.w.Z, *sh = c.w.Z + N, *s = c.w.Z + 2 * N, *t = c.w.Z + 3 * N;
@@ -1315,6 +1319,7 @@ __device__ __forceinline__ void bicgstab_cycle(Ctx<T, kGrid> &c, cg::grid_group 
     if (rn <= cycle_target || omega == 0.0 || rho == 0.0) break;
   }
   group_sync<kGrid>(grid);  // V complete before the next true residual
+  return make_int2(parity, iters);
 }
 
 // One backward-Euler step of one group (CTA or grid) for instance `inst`.
@@ -1360,7 +1365,10 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
     }
     if (iters >= budget || !(res == res)) break;  // budget spent, or the state is not finite
     if (iv.krylov == NRT_BICGSTAB) {
-      bicgstab_cycle(c, grid, S, parity, res, fmax(target, inner_rel * res), budget, iters, Vout);
+      const int2 pi = bicgstab_cycle(c, parity, res, fmax(target, inner_rel * res), budget,
+                                     iters, Vout);
+      parity = pi.x;
+      iters = pi.y;
       continue;
     }
     apply_precond(c, c.w.Wb, c.w.Z);
