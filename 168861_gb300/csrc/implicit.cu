@@ -878,24 +878,32 @@ struct DotAcc {
   T v[kG];
 };
 
-// Assembly: gates (from V^n), W, K, diagonal, c, right-hand side and the initial guess
-// (V^n extrapolated from V^{n-1}, which Vout holds); returns the thread's part of ||b||^2.
+// The initial guess of a step: V^n extrapolated from V^{n-1} (which Vout holds until the
+// first solution update writes it).
+__device__ __forceinline__ double x0_of(const double *Vin, const double *Vout, int64_t j) {
+  return 2.0 * Vin[j] - Vout[j];
+}
+
+// Assembly: gates (from V^n), W, K, diagonal, c and right-hand side, fused with the first
+// true residual r = b - A x0 (into W_0).  Nothing writes V here, so the neighbours' x0 are
+// formed from V^n and V^{n-1} directly (a row's columns are never identity rows).  Returns
+// the thread's parts of ||b||^2 and ||r||^2.
 template <typename T, bool kGrid>
-__device__ __noinline__ double ph_assemble(Ctx<T, kGrid> c, const double *Vin, double *Vout,
-                                           int active, int inst) {
+__device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
+                                            const double *Vout, int active, int inst) {
   const PackView &pv = *c.pv;
   const ImView &iv = *c.iv;
   const int64_t N = pv.ntot, stride = blockDim.x;
   T *cdiag = (T *)iv.cdiag;
-  double bacc = 0;
+  double bacc = 0, racc = 0;
   for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kA * stride) {
     uint8_t f[kA];
-    double v[kA], vo[kA], cm[kA], gj[kA], gn[kA], inp[kA];
+    double v[kA], vo[kA], cm[kA], gj[kA], gn[kA], inp[kA], xm[kA], xp[kA];
 #pragma unroll
     for (int u = 0; u < kA; u++) {
       const int64_t r = rb + u * stride;
       const bool ok = r < c.r1;
-      const int64_t rp = r + 1 < N ? r + 1 : r;
+      const int64_t rp = r + 1 < N ? r + 1 : r, rm = r > 0 ? r - 1 : r;
       f[u] = ok ? iv.rowf[r] : (uint8_t)R_IDENT;
       v[u] = ok ? Vin[r] : 0.0;
       vo[u] = ok ? Vout[r] : 0.0;
@@ -903,6 +911,8 @@ __device__ __noinline__ double ph_assemble(Ctx<T, kGrid> c, const double *Vin, d
       gj[u] = ok ? iv.g64[r] : 0.0;
       gn[u] = ok ? iv.g64[rp] : 0.0;
       inp[u] = ok && active ? iv.inp64[r] : 0.0;
+      xm[u] = ok ? x0_of(Vin, Vout, rm) : 0.0;
+      xp[u] = ok ? x0_of(Vin, Vout, rp) : 0.0;
     }
 #pragma unroll
     for (int u = 0; u < kA; u++) {
@@ -944,11 +954,20 @@ __device__ __noinline__ double ph_assemble(Ctx<T, kGrid> c, const double *Vin, d
       }
       if (f[u] & R_IDENT) {
         c.w.y[r] = 0;
+        c.w.Wb[r] = 0;
         continue;
       }
       const double cj = cm[u] - wdx;
-      double d = cj;
-      if (f[u] & R_DOWNL) d += iv.g64[pv.topo[r].dl];
+      double d = cj, gl = 0.0, xl = 0.0, xmo = xm[u];
+      if (f[u] & (R_DOWNL | R_FAR)) {
+        const Topo t = pv.topo[r];
+        if (f[u] & R_DOWNL) {
+          gl = iv.g64[t.dl];
+          xl = x0_of(Vin, Vout, t.dl);
+          d += gl;
+        }
+        if (f[u] & R_FAR) xmo = x0_of(Vin, Vout, t.mother);
+      }
       if (f[u] & R_DOWNR) d += gn[u];
       if (f[u] & R_UP) d += gj[u];
       iv.diag[r] = d;
@@ -958,10 +977,25 @@ __device__ __noinline__ double ph_assemble(Ctx<T, kGrid> c, const double *Vin, d
       if (active) b += inp[u];
       iv.rhs[r] = b;
       bacc += b * b;
-      Vout[r] = 2.0 * v[u] - vo[u];
+      // r = b - A x0, in the order of row_apply: diagonal, mother, DR, DL
+      double ax = d * (2.0 * v[u] - vo[u]);
+      if (f[u] & R_UP) ax -= gj[u] * xmo;
+      if (f[u] & R_DOWNR) ax -= gn[u] * xp[u];
+      if (f[u] & R_DOWNL) ax -= gl * xl;
+      const double rr = b - ax;
+      c.w.Wb[r] = (T)rr;
+      racc += rr * rr;
     }
   }
-  return bacc;
+  return make_double2(bacc, racc);
+}
+
+// Vout = x0 for the rows of this group (when a step ends before any solution update).
+template <typename T, bool kGrid>
+__device__ __noinline__ void ph_x0(Ctx<T, kGrid> c, const double *Vin, double *Vout) {
+  const uint8_t *rowf = c.iv->rowf;
+  for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x)
+    if (!(rowf[j] & R_IDENT)) Vout[j] = x0_of(Vin, Vout, j);
 }
 
 // True residual r = b - A x in FP64 into W_0 (identity rows 0); returns the thread's
@@ -1101,9 +1135,11 @@ __device__ __noinline__ T ph_update(Ctx<T, kGrid> c, int j, const T *coef) {
   return nacc;
 }
 
-// V += sum_{i < k} coef_i Z_i (identity rows keep their value).
+// V += sum_{i < k} coef_i Z_i (identity rows keep their value).  With Vin non-null this is
+// the step's first update and V starts from x0 = 2 Vin - V.
 template <typename T, bool kGrid>
-__device__ __noinline__ void ph_xupdate(Ctx<T, kGrid> c, int k, const T *coef, double *Vout) {
+__device__ __noinline__ void ph_xupdate(Ctx<T, kGrid> c, int k, const T *coef, double *Vout,
+                                        const double *Vin) {
   const int64_t N = c.pv->ntot, stride = blockDim.x;
   const uint8_t *rowf = c.iv->rowf;
   for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kV * stride) {
@@ -1131,7 +1167,10 @@ __device__ __noinline__ void ph_xupdate(Ctx<T, kGrid> c, int k, const T *coef, d
 #pragma unroll
     for (int u = 0; u < kV; u++) {
       const int64_t r = rb + u * stride;
-      if (!(fl[u] & R_IDENT)) Vout[r] += (double)a[u];
+      if (!(fl[u] & R_IDENT)) {
+        const double base = Vin ? x0_of(Vin, Vout, r) : Vout[r];
+        Vout[r] = base + (double)a[u];
+      }
     }
   }
 }
@@ -1331,8 +1370,8 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
   const ImView &iv = *c.iv;
   const int m = iv.m;
   T *coef = (T *)S.coef;
-  // ---- assembly
-  const double bacc = ph_assemble(c, Vin, Vout, active ? 1 : 0, inst);
+  // ---- assembly, fused with the first true residual (W_0); V still holds V^{n-1}
+  const double2 br = ph_assemble(c, Vin, Vout, active ? 1 : 0, inst);
   __syncthreads();
   if (iv.precond == NRT_PRECOND_SEGMENT) {
     factor_pieces(c);
@@ -1340,11 +1379,12 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
     level_sync<kGrid>(grid);  // c of every row visible before the elimination
     tree_factor(c);
   }
-  double target = iv.tol;
+  double target = iv.tol, res0 = 0;
   {
-    double acc[1] = {bacc};
-    group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);  // also publishes x0
+    double acc[2] = {br.x, br.y};
+    group_reduce<kGrid>(grid, acc, 2, S, iv.partials, parity);  // also publishes W_0
     if (iv.tol_mode == NRT_TOL_REL) target = iv.tol * sqrt(S.red[0]);
+    res0 = sqrt(S.red[1]);
     if (!kGrid) __syncthreads();
   }
   const int budget = iv.max_iter > 0 ? iv.max_iter : (iv.max_iter < 0 ? 0 : (int)inst_n);
@@ -1352,19 +1392,27 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
   int iters = 0;
   double res = 0;
   bool converged = false;
-  for (;;) {
+  bool x0_pending = true;  // V holds V^{n-1} until the first solution update
+  for (int cycle = 0;; cycle++) {
     // ---- cycle start: true residual r = b - A x in FP64, W_0 = r, Z_0 = M^-1 r
-    {
+    if (cycle == 0) {
+      res = res0;
+    } else {
       double acc[1] = {ph_residual(c, Vout)};
       group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);
+      res = sqrt(S.red[0]);
     }
-    res = sqrt(S.red[0]);
     if (res <= target) {
       converged = true;
       break;
     }
     if (iters >= budget || !(res == res)) break;  // budget spent, or the state is not finite
     if (iv.krylov == NRT_BICGSTAB) {
+      if (x0_pending) {
+        ph_x0(c, Vin, Vout);
+        x0_pending = false;
+        group_sync<kGrid>(grid);
+      }
       const int2 pi = bicgstab_cycle(c, parity, res, fmax(target, inner_rel * res), budget,
                                      iters, Vout);
       parity = pi.x;
@@ -1436,9 +1484,11 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
       for (int i = 0; i < k; i++) coef[i] = (T)(S.y[i] * S.s[i]);
     }
     __syncthreads();
-    ph_xupdate(c, k, coef, Vout);
+    ph_xupdate(c, k, coef, Vout, x0_pending ? Vin : (const double *)nullptr);
+    x0_pending = false;
     group_sync<kGrid>(grid);
   }
+  if (x0_pending) ph_x0(c, Vin, Vout);  // converged (or out of budget) at x0 itself
   if (threadIdx.x == 0 && (!kGrid || blockIdx.x == 0)) {
     InstStat &st = iv.stats[inst];
     st.iters += iters;
