@@ -1447,11 +1447,9 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
         coef[threadIdx.x] = (T)(h * S.s[threadIdx.x]);
       }
       __syncthreads();
-      // w = y - sum_i h_ij s_i W_i -> W_{j+1}; ||w||^2; then Z_{j+1} = M^-1 w
+      // w = y - sum_i h_ij s_i W_i -> W_{j+1}; ||w||^2
       T nacc[1] = {ph_update(c, j, coef)};
-      __syncthreads();
-      apply_precond(c, c.w.Wb + (size_t)(j + 1) * c.pv->ntot, c.w.Z + (size_t)(j + 1) * c.pv->ntot);
-      group_reduce<kGrid>(grid, nacc, 1, S, iv.partials, parity);  // publishes Z_{j+1}
+      group_reduce<kGrid>(grid, nacc, 1, S, iv.partials, parity);  // publishes W_{j+1}
       if (threadIdx.x == 0) {
         const double hn = sqrt(S.red[0]);
         S.s[j + 1] = hn > 0 ? 1.0 / hn : 0.0;
@@ -1472,7 +1470,10 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
       __syncthreads();
       k = j + 1;
       iters++;
-      if (S.flag[0] || iters >= budget) break;
+      if (S.flag[0] || iters >= budget || k >= m) break;
+      // Z_{j+1} = M^-1 W_{j+1}, only when another Arnoldi step will use it
+      apply_precond(c, c.w.Wb + (size_t)(j + 1) * c.pv->ntot, c.w.Z + (size_t)(j + 1) * c.pv->ntot);
+      group_sync<kGrid>(grid);  // Z_{j+1} of every row visible before the next SpMV
     }
     // ---- x += sum_i y_i s_i Z_i
     if (threadIdx.x == 0) {
