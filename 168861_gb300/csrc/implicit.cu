@@ -896,14 +896,24 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
   const int64_t N = pv.ntot, stride = blockDim.x;
   T *cdiag = (T *)iv.cdiag;
   double bacc = 0, racc = 0;
+  // gates of this precision (the mixed path keeps them in FP32)
+  T *gate = sizeof(T) == 4 ? (T *)(void *)pv.gatef : (T *)(void *)pv.gate;
   for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kA * stride) {
     uint8_t f[kA];
     double v[kA], vo[kA], cm[kA], gj[kA], gn[kA], inp[kA], xm[kA], xp[kA];
+    int64_t hc[kA];
+    T g0[kA], g1[kA], g2[kA];
+    // every load that does not depend on the row's flags goes out in this first round
 #pragma unroll
     for (int u = 0; u < kA; u++) {
       const int64_t r = rb + u * stride;
       const bool ok = r < c.r1;
       const int64_t rp = r + 1 < N ? r + 1 : r, rm = r > 0 ? r - 1 : r;
+      hc[u] = ok && pv.hp_cls ? (int64_t)pv.hp_cls[r] : (pv.hp_inst ? (int64_t)inst : r);
+      const bool gl = ok && pv.hh_dense;
+      g0[u] = gl ? gate[r] : (T)0;
+      g1[u] = gl ? gate[N + r] : (T)0;
+      g2[u] = gl ? gate[2 * N + r] : (T)0;
       f[u] = ok ? iv.rowf[r] : (uint8_t)R_IDENT;
       v[u] = ok ? Vin[r] : 0.0;
       vo[u] = ok ? Vout[r] : 0.0;
@@ -920,30 +930,35 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
       if (r >= c.r1) continue;
       double wdx, kdx;
       if (f[u] & R_HH) {
-        const int64_t L = pv.hp_ld, hc = hp_col(pv, r, (uint32_t)inst);
-        if (pv.hpf) {
-          const float *hp = pv.hpf + hc;
+        const int64_t L = pv.hp_ld;
+        if (!pv.hh_dense) {
+          g0[u] = gate[r];
+          g1[u] = gate[N + r];
+          g2[u] = gate[2 * N + r];
+        }
+        if (sizeof(T) == 4) {
+          const float *hp = pv.hpf + hc[u];
           const float dv = (float)(v[u] - (double)hp[HP_REST * L]);
-          GateStep32 g = hh_step32(dv + hp[HP_LSNA * L], dv + hp[HP_LSK * L], pv.gatef[r],
-                                   pv.gatef[N + r], pv.gatef[2 * N + r], hp[HP_DTMS * L],
+          GateStep32 g = hh_step32(dv + hp[HP_LSNA * L], dv + hp[HP_LSK * L], (float)g0[u],
+                                   (float)g1[u], (float)g2[u], hp[HP_DTMS * L],
                                    hp[HP_GNA * L], hp[HP_GK * L], hp[HP_GL * L],
                                    hp[HP_ENA * L], hp[HP_EK * L], hp[HP_EL * L]);
-          pv.gatef[r] = g.m;
-          pv.gatef[N + r] = g.h;
-          pv.gatef[2 * N + r] = g.n;
+          gate[r] = (T)g.m;
+          gate[N + r] = (T)g.h;
+          gate[2 * N + r] = (T)g.n;
           const double dx = (double)hp[HP_DX * L];
           wdx = (double)g.W * dx;
           kdx = (double)g.K * dx;
         } else {
-          const double *hp = pv.hp + hc;
-          GateStep64 g = hh_step64(v[u], pv.gate[r], pv.gate[N + r], pv.gate[2 * N + r],
+          const double *hp = pv.hp + hc[u];
+          GateStep64 g = hh_step64(v[u], (double)g0[u], (double)g1[u], (double)g2[u],
                                    hp[HP_LSNA * L], hp[HP_LSK * L], hp[HP_REST * L],
                                    hp[HP_DTMS * L], hp[HP_GNA * L], hp[HP_GK * L],
                                    hp[HP_GL * L], hp[HP_ENA * L], hp[HP_EK * L],
                                    hp[HP_EL * L]);
-          pv.gate[r] = g.m;
-          pv.gate[N + r] = g.h;
-          pv.gate[2 * N + r] = g.n;
+          gate[r] = (T)g.m;
+          gate[N + r] = (T)g.h;
+          gate[2 * N + r] = (T)g.n;
           const double dx = hp[HP_DX * L];
           wdx = g.W * dx;
           kdx = g.K * dx;
