@@ -895,7 +895,11 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
   const ImView &iv = *c.iv;
   const int64_t N = pv.ntot, stride = blockDim.x;
   T *cdiag = (T *)iv.cdiag;
-  double bacc = 0, racc = 0;
+  // ||b|| needs a few digits only and its terms are far from FP32's range limits: it
+  // accumulates in T.  Residual entries near convergence are tiny (their squares leave
+  // FP32's normal range), so ||r|| stays in FP64.
+  T bacc = 0;
+  double racc = 0;
   // gates of this precision (the mixed path keeps them in FP32)
   T *gate = sizeof(T) == 4 ? (T *)(void *)pv.gatef : (T *)(void *)pv.gate;
   for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kA * stride) {
@@ -946,9 +950,9 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
           gate[r] = (T)g.m;
           gate[N + r] = (T)g.h;
           gate[2 * N + r] = (T)g.n;
-          const double dx = (double)hp[HP_DX * L];
-          wdx = (double)g.W * dx;
-          kdx = (double)g.K * dx;
+          const float dx = hp[HP_DX * L];
+          wdx = (double)(g.W * dx);  // FP32 inputs: the product in FP32 loses nothing
+          kdx = (double)(g.K * dx);
         } else {
           const double *hp = pv.hp + hc[u];
           GateStep64 g = hh_step64(v[u], (double)g0[u], (double)g1[u], (double)g2[u],
@@ -991,7 +995,7 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
       double b = cm[u] * v[u] + kdx;
       if (active) b += inp[u];
       iv.rhs[r] = b;
-      bacc += b * b;
+      bacc += (T)b * (T)b;
       // r = b - A x0, in the order of row_apply: diagonal, mother, DR, DL
       double ax = d * (2.0 * v[u] - vo[u]);
       if (f[u] & R_UP) ax -= gj[u] * xmo;
@@ -1002,7 +1006,7 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
       racc += rr * rr;
     }
   }
-  return make_double2(bacc, racc);
+  return make_double2((double)bacc, racc);
 }
 
 // Vout = x0 for the rows of this group (when a step ends before any solution update).
