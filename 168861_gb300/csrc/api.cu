@@ -194,6 +194,9 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
       if (is_term[j]) f |= F_TERM;
       if (j == p.terminals[0]) f |= F_ROOT;
       if (p.input[j] != 0.0) f |= F_INP;
+      if (p.branching[j] || is_term[j] || j == p.terminals[0] || p.mother[j] != j - 1 ||
+          p.dr[j] != j + 1)
+        f |= F_XTOPO;
       // Flux through a terminal neighbour is zero when that terminal copies this element.
       if (!is_term[j]) {
         if (p.branching[j] && is_term[p.dl[j]]) {
@@ -370,6 +373,7 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
                  al(8 * host.terms.size() + 8);
   const size_t hpn = (size_t)HP_ROWS * host.hp_ld;
   if (!host.hp_cls.empty()) bytes += al(4 * N);
+  if (mixed && opt.mode == NRT_EXPLICIT) bytes += al(4 * N);  // flags of the compact step
   if (mixed)
     bytes += 7 * al(4 * N) + al(4 * 3 * N) + al(4 * hpn);
   else
@@ -401,6 +405,17 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   pv.hp_inst = host.hp_inst ? 1 : 0;
   pv.hp_cls = nullptr;
   pv.hh_dense = 2 * (int64_t)host.hh_local.size() >= N ? 1 : 0;
+  pv.eflags = nullptr;
+  if (mixed && opt.mode == NRT_EXPLICIT) {
+    std::vector<uint32_t> fl(N);
+    parallel_ranges(N, [&](int64_t a, int64_t b) {
+      for (int64_t j = a; j < b; j++) fl[j] = host.topo[j].flags;
+    });
+    uint32_t *pf = nullptr;
+    TRY(upload(arena, pf, fl.data(), N, st));
+    pv.eflags = pf;
+    NRT_CUDA(cudaStreamSynchronize(st));  // fl is a local buffer
+  }
   if (!host.hp_cls.empty()) {
     uint32_t *pc = nullptr;
     TRY(upload(arena, pc, host.hp_cls.data(), N, st));

@@ -113,7 +113,10 @@ __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, in
   // element's own state and its neighbours j-1 and j+1 (the mother and DR of nearly
   // every element in the reference numbering), so most elements wait for one round trip.
   const int64_t jm = j > 0 ? j - 1 : j, jp = j + 1 < N ? j + 1 : j;
-  const Topo tj = p.topo[j];
+  // The flags word alone (4 B) stands for the 16-byte topology record unless a neighbour
+  // is not adjacent (F_XTOPO), which only branch points, DL children, terminals and the
+  // root are.
+  const uint32_t fl = p.eflags ? p.eflags[j] : 0u;
   const float f0 = Fin[j], fm = Fin[jm], fp = Fin[jp];
   const float g0 = p.gaxf[j], gp = p.gaxf[jp];
   const double v64 = Vin[j];
@@ -124,6 +127,15 @@ __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, in
     m0 = p.gatef[j];
     h0 = p.gatef[N + j];
     n0 = p.gatef[2 * N + j];
+  }
+  Topo tj;
+  if (!p.eflags || (fl & F_XTOPO)) {
+    tj = p.topo[j];
+  } else {
+    tj.mother = (int32_t)jm;
+    tj.dr = (int32_t)jp;
+    tj.dl = (int32_t)j;
+    tj.flags = fl;
   }
   const uint32_t inst = tj.flags >> INST_SHIFT;
   const InstDev in = p.inst[inst];

@@ -13,7 +13,7 @@
 
 namespace nrt {
 
-// Per-element flag bits (low 12 bits of Topo::flags; the instance id sits above).
+// Per-element flag bits (low 13 bits of Topo::flags; the instance id sits above).
 enum : uint32_t {
   F_HH = 1u,        // Hodgkin_Huxley element (gates evolve)
   F_BRANCH = 2u,    // branching point: has a DL child
@@ -27,8 +27,10 @@ enum : uint32_t {
   F_DR_TERM = 512u, // explicit: the DR neighbour is a terminal (zero flux)
   F_DOWNL = 1024u,  // implicit row has a column at DL
   F_INP = 2048u,    // nonzero injected current
+  F_XTOPO = 4096u,  // a neighbour is not j-1 / j+1 (or the element is a branch point,
+                    // terminal or the root): the step needs the full topology record
 };
-constexpr int INST_SHIFT = 12;
+constexpr int INST_SHIFT = 13;
 
 // Topology of one element, global (packed) indices.  16 bytes, loaded as one int4.
 struct __align__(16) Topo {
@@ -121,6 +123,7 @@ struct PackView {
   int64_t hp_ld;       // number of columns
   int hp_inst;         // 1: column = instance
   const uint32_t *hp_cls;  // column per element (class tables), or null
+  const uint32_t *eflags;  // Topo::flags alone (mixed explicit step), or null
   int hh_dense;        // most elements are HH: the step loads gates before the topology
   const float *cdtf, *gaxf, *wdxf, *kdxf, *inpf;  // FP32 copies (mixed path)
   InstDev *inst;
