@@ -92,6 +92,7 @@ struct MicroBatch {
 };
 
 constexpr double kTickMs = 10.0;   // target device time of one tick per resident batch
+constexpr int32_t kWideRows = 20000;  // implicit requests this large step on the whole GPU
 
 // Device footprint of one tree in a batch (the arena sizes of the engine, rounded up).
 size_t estimate_bytes(const nrt_problem &p, const nrt_options &o) {
@@ -123,10 +124,12 @@ struct nrt_server {
   double busy = 0;
 
   void loop();
-  MicroBatch *admit(bool implicit, std::vector<Request *> &batch);
+  MicroBatch *admit(bool implicit, std::vector<Request *> &batch, bool wide = false);
 };
 
-MicroBatch *nrt_server::admit(bool implicit, std::vector<Request *> &batch) {
+// `wide`: one large implicit request on the cooperative whole-GPU launch (its steps take a
+// fraction of the time one CTA needs; it shares the SMs with the resident batches).
+MicroBatch *nrt_server::admit(bool implicit, std::vector<Request *> &batch, bool wide) {
   std::vector<nrt_problem> probs;
   std::vector<nrt_instance_run> runs;
   for (Request *r : batch) {
@@ -134,7 +137,9 @@ MicroBatch *nrt_server::admit(bool implicit, std::vector<Request *> &batch) {
     runs.push_back(r->run);
   }
   MicroBatch *mb = new MicroBatch();
-  int rc = nrt_batch_create(probs.data(), (int32_t)probs.size(), &opt[implicit ? 1 : 0], &mb->b);
+  nrt_options o = opt[implicit ? 1 : 0];
+  if (wide) o.schedule = 0;
+  int rc = nrt_batch_create(probs.data(), (int32_t)probs.size(), &o, &mb->b);
   if (rc == NRT_OK) rc = nrt_batch_set_runs(mb->b, runs.data());
   std::lock_guard<std::mutex> lk(mu);
   if (rc != NRT_OK) {
@@ -201,6 +206,19 @@ void nrt_server::loop() {
         }
       }
       if (stop && pending.empty() && active.empty() && take[0].empty() && take[1].empty()) break;
+    }
+    {  // large implicit requests each get their own whole-GPU micro-batch
+      std::vector<Request *> narrow;
+      for (Request *r : take[1]) {
+        if (r->prob.p.num_elem >= kWideRows) {
+          std::vector<Request *> one(1, r);
+          MicroBatch *mb = admit(true, one, true);
+          if (mb) active.push_back(mb);
+        } else {
+          narrow.push_back(r);
+        }
+      }
+      take[1].swap(narrow);
     }
     for (int k = 0; k < 2; k++)
       if (!take[k].empty()) {

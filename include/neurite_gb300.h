@@ -237,7 +237,10 @@ int nrt_batch_destroy(nrt_batch *b);
  *
  * A request is one tree (copied at submit) with its loop range and stimulus window;
  * `implicit` selects the backward-Euler engine.  The server's two option sets (explicit,
- * implicit) fix precision and solver settings for all requests of that kind. */
+ * implicit) fix precision and solver settings for all requests of that kind.  Implicit
+ * requests of 20,000 elements or more each get a batch of their own on the cooperative
+ * whole-GPU launch (their steps take a fraction of the time one CTA would need); smaller
+ * ones share block-per-instance batches. */
 typedef struct nrt_server nrt_server;
 
 typedef struct nrt_server_config {
