@@ -17,7 +17,10 @@ def _requests(pkg, model):
         dT = pkg.step_size(spec, d)
         reqs.append((pkg.ProblemArrays.from_spec(spec, d, dT), False,
                      (1, 1 + 300 + 150 * k, spec.init_time, spec.end_input)))
-    for seed, n, steps in [(21, 1200, 30), (22, 5000, 12), (23, 2500, 45), (24, 800, 20)]:
+    # (25, 30000): above the server's whole-GPU threshold, so it steps on the cooperative
+    # launch while the others share block-per-instance batches
+    for seed, n, steps in [(21, 1200, 30), (22, 5000, 12), (23, 2500, 45), (24, 800, 20),
+                           (25, 30000, 15)]:
         spec = model.random_tree(seed=seed, n_target=n, dt=2.5e-5, tspan=2e-3)
         reqs.append((pkg.ProblemArrays.from_spec(spec, pkg.derive(spec)), True,
                      (1, 1 + steps, spec.init_time, spec.end_input)))
