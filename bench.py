@@ -70,10 +70,30 @@ def tree_population(count: int, seed: int):
     return [(seed * 7919 + i, int(sizes[i])) for i in range(count)]
 
 
+def shard(population, rank: int, world: int):
+    """Round-robin split of the tree population over ranks: trees are independent, so a
+    rank steps its own share with no data exchange (replicas only, weak scaling)."""
+    return population[rank::world]
+
+
+def combine_ranks(dist, device, ms: float, e2e_s: float, n_elem: int, alg_bytes: float):
+    """Job-wide figures from the per-rank ones: the slowest rank's device time and
+    end-to-end time, the element count and algorithmic bytes summed over ranks.  With
+    `dist` None (one process) the inputs come back unchanged."""
+    if dist is None:
+        return ms, e2e_s, float(n_elem), float(alg_bytes)
+    import torch
+    t = torch.tensor([ms, e2e_s], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    s = torch.tensor([float(n_elem), float(alg_bytes)], device=device, dtype=torch.float64)
+    dist.all_reduce(s)
+    return float(t[0]), float(t[1]), float(s[0]), float(s[1])
+
+
 def build_batch_problems(workload: str, count: int, seed: int, rank: int, world: int):
     pkg = importlib.import_module("168861_gb300")
     model = pkg.model
-    pop = tree_population(count, seed)[rank::world]
+    pop = shard(tree_population(count, seed), rank, world)
     probs, runs = [], []
     n_elem = 0
     for tseed, size in pop:
@@ -321,26 +341,19 @@ def run_ours(args, rank: int, world: int):
         krylov = {"iters_per_tree_step_mean": float(per.mean()), "iters_per_tree_step_max": float(per.max()),
                   "nonconverged_steps": int(ist["nonconverged"].sum()),
                   "max_last_residual": float(ist["last_residual"].max())}
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        tot = torch.tensor([float(n_elem)], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tot)
-        n_all = float(tot.item())
-    else:
-        n_all = float(n_elem)
-    value = n_all * K / (ms / 1e3)
-    e2e_value = n_all * K / e2e_s
     if implicit:
         alg = algorithmic_bytes_implicit(probs, krylov["iters_per_tree_step_mean"])
     else:
         alg = algorithmic_bytes_explicit(probs, precision)
+    ms, e2e_s, n_all, alg_all = combine_ranks(dist, "cuda", ms, e2e_s, n_elem, alg)
+    value = n_all * K / (ms / 1e3)
+    e2e_value = n_all * K / e2e_s
     peak, peak_kind = measured_peaks()
-    achieved = alg * K / (ms / 1e3) / 1e9
+    # per GPU: the job's algorithmic bytes over the slowest rank's time, divided by N
+    achieved = alg_all * K / (ms / 1e3) / 1e9 / world
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-            "algorithmic_bytes_per_step": alg}
+            "algorithmic_bytes_per_step": alg_all}
     # our kernels launched in the timed region: one persistent launch + one loop-index
     # update per 64-step chunk (implicit); 64 step launches + 1 update per graph (explicit)
     launches = 2 * math.ceil(K / 64) if implicit else K + math.ceil(K / 64)
@@ -408,9 +421,15 @@ def serve_requests(count: int, seed: int):
 def run_serve(args, rank: int, world: int):
     import torch
     pkg = importlib.import_module("168861_gb300")
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     count = args.trees or 64
-    reqs = serve_requests(count, args.seed)
+    # each rank serves its own share of the arrival stream (one server per GPU)
+    reqs = shard(serve_requests(count, args.seed), rank, world)
     ex = dict(precision="mixed")
     im = dict(precision="mixed", restart=20, tol=1e-10, tol_mode="rel", precond=args.precond,
               max_iter=1000)
@@ -436,6 +455,19 @@ def run_serve(args, rank: int, world: int):
     st = srv.stats()
     srv.close()
     work = float(st.compartment_steps)
+    p50, p99, pmax = st.p50_ms, st.p99_ms, st.max_ms
+    h2d = sum(sum(a.nbytes for a in r[1].arrays.values()) for r in reqs)
+    d2h = sum(r[1].num_elem * 8 for r in reqs)
+    if dist:
+        t = torch.tensor([wall, p50, p99, pmax], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        s_ = torch.tensor([work, float(h2d), float(d2h)], device="cuda", dtype=torch.float64)
+        dist.all_reduce(s_)
+        wall, p50, p99, pmax = (float(x) for x in t)
+        work, h2d, d2h = (float(x) for x in s_)
+        dist.destroy_process_group()
+    if rank != 0:
+        return
     line = {"metric": "serve compartment-steps/s", "value": work / wall,
             "unit": "compartment-steps/s", "n_gpus": world, "steps": count, "warmup": 2,
             "ms_per_step": wall * 1e3 / count, "higher_is_better": True, "scaling": "weak",
@@ -443,13 +475,11 @@ def run_serve(args, rank: int, world: int):
             "config": {"workload": "serve", "requests": count, "arrivals": "Poisson 2000/s",
                        "mix": "50% explicit 1 cm axon (mixed), 50% implicit random tree 1e3-1e5 "
                               "(mixed GMRES(20)+FP64 refinement)", "sim_time_ms": "U(10,100)"},
-            "p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "max_ms": st.max_ms,
+            "p50_ms": p50, "p99_ms": p99, "max_ms": pmax,
             "batches": int(st.batches_created), "completed": int(st.completed),
             "clocks": clk.summary(),
             "e2e": {"value": work / wall, "unit": "compartment-steps/s",
-                    "h2d_bytes_per_step": sum(sum(a.nbytes for a in r[1].arrays.values())
-                                              for r in reqs) / count,
-                    "d2h_bytes_per_step": sum(r[1].num_elem * 8 for r in reqs) / count}}
+                    "h2d_bytes_per_step": h2d / count, "d2h_bytes_per_step": d2h / count}}
     print(json.dumps(line), flush=True)
 
 
