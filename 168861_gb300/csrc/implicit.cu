@@ -1549,13 +1549,19 @@ __global__ void __launch_bounds__(kThreads, 3) implicit_steps(const PackView *pv
     c.l1 = iv.work_lev ? iv.work_lev[blockIdx.x + 1] : 0;
     const InstDev in = pvp->inst[0];
     const int64_t inst_n = iv.inst_row[1] - iv.inst_row[0];
-    for (int s = 0; s < nsteps; s++) {
+    int s = 0;
+    for (; s < nsteps; s++) {
       const int64_t i = in.base + s;
       if (i >= in.iend) break;
       const bool active = force >= 0 ? force != 0
                                      : (i >= in.ion && i <= in.ioff);
       implicit_one_step<T, kGrid>(c, grid, S, parity, ((cur + s) & 1) ? V1 : V0,
                                   ((cur + s + 1) & 1) ? V1 : V0, active, inst_n, 0);
+    }
+    if ((nsteps - s) & 1) {  // the run ended inside the launch: each CTA moves its rows
+      double *dst = ((cur + nsteps) & 1) ? V1 : V0;
+      const double *src = ((cur + s) & 1) ? V1 : V0;
+      for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x) dst[j] = src[j];
     }
   } else {
     for (;;) {

@@ -112,6 +112,21 @@ def test_implicit_large_tree_cooperative(gpu, pkg, orc, model, precond):
     assert np.abs(s.snapshot() - Vo).max() < TOL_FP64
 
 
+@pytest.mark.parametrize("steps,advance", [(15, 16), (15, 64), (14, 17)])
+def test_cooperative_run_ending_inside_a_launch(gpu, pkg, orc, model, steps, advance):
+    """A one-tree batch on the cooperative launch whose run ends before the launch's step
+    count leaves its latest V where the host expects it."""
+    spec = model.random_tree(seed=25, n_target=30000, dt=2.5e-5, tspan=2e-3)
+    p = pkg.ProblemArrays.from_spec(spec, pkg.derive(spec))
+    b = pkg.Batch([p], mode=1, **tight())
+    b.set_runs([(1, 1 + steps, spec.init_time, spec.end_input)])
+    b.advance(advance)
+    assert (b.remaining() == 0).all()
+    Vo, _, _, _ = orc.implicit_run(spec, orc.derive(spec), spec.dt_abs, 1, 1 + steps, linsolve=0)
+    assert np.abs(b.snapshot(0) - Vo).max() < TOL_FP64
+    b.close()
+
+
 def test_implicit_mixed_precision(gpu, pkg, orc):
     g = load_golden("im_ytree_d3")
     spec = g["spec"]
