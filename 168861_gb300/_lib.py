@@ -72,6 +72,13 @@ class InstanceRun(ctypes.Structure):
                 ("init_time", ctypes.c_double), ("end_input", ctypes.c_double)]
 
 
+class RecordConfig(ctypes.Structure):
+    _fields_ = [("num_probes", ctypes.c_int32), ("instance", _i32p), ("element", _i32p),
+                ("origin", ctypes.c_int64), ("interval", ctypes.c_int64),
+                ("capacity", ctypes.c_int64), ("threshold", ctypes.c_double),
+                ("max_spikes", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+
+
 # Every symbol include/neurite_gb300.h declares.
 EXPORTS = (
     "nrt_options_default", "nrt_create", "nrt_update", "nrt_calculate", "nrt_snapshot", "nrt_run",
@@ -82,6 +89,8 @@ EXPORTS = (
     "nrt_batch_instance_stats",
     "nrt_server_create", "nrt_server_submit", "nrt_server_result", "nrt_server_drain",
     "nrt_server_get_stats", "nrt_server_destroy", "nrt_solve_csr_static",
+    "nrt_measurement_point", "nrt_record", "nrt_batch_record", "nrt_record_read",
+    "nrt_batch_record_read",
 )
 
 _lib = None
@@ -133,6 +142,12 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "nrt_server_drain": [vp],
         "nrt_server_get_stats": [vp, ctypes.POINTER(ServerStats)],
         "nrt_server_destroy": [vp],
+        "nrt_measurement_point": [ctypes.c_int32, _f64p, ctypes.c_double,
+                                  ctypes.POINTER(ctypes.c_int32)],
+        "nrt_record": [vp, ctypes.POINTER(RecordConfig)],
+        "nrt_batch_record": [vp, ctypes.POINTER(RecordConfig)],
+        "nrt_record_read": [vp, _i64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int32), _f64p],
+        "nrt_batch_record_read": [vp, _i64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int32), _f64p],
         "nrt_solve_csr_static": [ctypes.c_int32, vp, vp, vp, vp, vp, ctypes.c_int32,
                                  ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp,
                                  ctypes.POINTER(ctypes.c_int32), _f64p],

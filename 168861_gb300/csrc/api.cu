@@ -465,6 +465,7 @@ Engine::~Engine() {
     if (graph_exec[q]) cudaGraphExecDestroy(graph_exec[q]);
   if (stream) cudaStreamSynchronize(stream);
   implicit_release();
+  record_release();
   arena.release();
   if (stream) cudaStreamDestroy(stream);
 }
@@ -501,6 +502,7 @@ int Engine::advance(int64_t steps) {
   int64_t left = steps;
   while (left > 0 && (steps_done == 0 && !host.invariant)) {  // exact first step
     TRY(step(0, -1));
+    if (rec) TRY(launch_record_step(rec_view_host(), pv.inst, 0, V[cur], stream));
     TRY(launch_advance_base(pv.inst, pv.ninst, 1, stream));
     left--;
   }
@@ -510,10 +512,13 @@ int Engine::advance(int64_t steps) {
       cudaGraph_t g;
       NRT_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
       int rc = NRT_OK;
-      for (int k = 0; k < kChunk && rc == NRT_OK; k++)
+      for (int k = 0; k < kChunk && rc == NRT_OK; k++) {
         rc = launch_explicit_step(pv, opt.precision, false, k, -1, V[(cur + k) & 1],
                                   V[(cur + k + 1) & 1], Vf[(cur + k) & 1], Vf[(cur + k + 1) & 1],
                                   stream);
+        if (rc == NRT_OK && rec)
+          rc = launch_record_step(rec_view_host(), pv.inst, k, V[(cur + k + 1) & 1], stream);
+      }
       if (rc == NRT_OK) rc = launch_advance_base(pv.inst, pv.ninst, kChunk, stream);
       cudaError_t e = cudaStreamEndCapture(stream, &g);
       if (rc != NRT_OK) return rc;
@@ -531,6 +536,7 @@ int Engine::advance(int64_t steps) {
   }
   while (left > 0) {
     TRY(step(0, -1));
+    if (rec) TRY(launch_record_step(rec_view_host(), pv.inst, 0, V[cur], stream));
     TRY(launch_advance_base(pv.inst, pv.ninst, 1, stream));
     left--;
   }
@@ -853,6 +859,37 @@ int nrt_batch_instance_stats(nrt_batch *b, int64_t *iters, int32_t *last_iters,
 int nrt_batch_destroy(nrt_batch *b) {
   delete b;
   return NRT_OK;
+}
+
+int nrt_record(nrt_solver *s, const nrt_record_config *cfg) {
+  if (!s || !cfg) return nrt::fail(NRT_EINVAL, "null argument");
+  if (cfg->instance)
+    for (int32_t p = 0; p < cfg->num_probes; p++)
+      if (cfg->instance[p] != 0) return nrt::fail(NRT_EINVAL, "a solver has only instance 0");
+  NRT_CUDA(cudaSetDevice(s->eng.device));
+  return s->eng.record_config(cfg);
+}
+
+int nrt_batch_record(nrt_batch *b, const nrt_record_config *cfg) {
+  if (!b || !cfg) return nrt::fail(NRT_EINVAL, "null argument");
+  NRT_CUDA(cudaSetDevice(b->eng.device));
+  return b->eng.record_config(cfg);
+}
+
+int nrt_record_read(nrt_solver *s, int64_t *num_samples, double *times, double *values,
+                    int32_t *num_spikes, double *spike_times) {
+  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+  NRT_CUDA(cudaSetDevice(s->eng.device));
+  int rc = s->eng.record_read(num_samples, times, values, num_spikes, spike_times);
+  return rc ? rc : nrt::implicit_check(s->eng);
+}
+
+int nrt_batch_record_read(nrt_batch *b, int64_t *num_samples, double *times, double *values,
+                          int32_t *num_spikes, double *spike_times) {
+  if (!b) return nrt::fail(NRT_EINVAL, "null batch");
+  NRT_CUDA(cudaSetDevice(b->eng.device));
+  int rc = b->eng.record_read(num_samples, times, values, num_spikes, spike_times);
+  return rc ? rc : nrt::implicit_check(b->eng);
 }
 
 }  // extern "C"

@@ -118,3 +118,22 @@ extern "C" int nrt_derive(int32_t n, const int32_t *ispec, const double *dspec, 
   if (num_hh_out) *num_hh_out = num_hh;
   return NRT_OK;
 }
+
+// src/init.cpp:339-358: walk the elements accumulating dX until the distance is reached;
+// the reference treats "not reached" and "reached at element 0" alike (its index stays 0)
+// and then measures at the middle element.
+extern "C" int nrt_measurement_point(int32_t n, const double *dx, double dist_mes,
+                                     int32_t *point) {
+  if (n < 1 || !dx || !point) return NRT_EINVAL;
+  double acc = 0;
+  int32_t k_at = 0;
+  for (int32_t k = 0; k < n; k++) {
+    acc = acc + dx[k];
+    if (acc >= dist_mes) {
+      k_at = k;
+      break;
+    }
+  }
+  *point = k_at == 0 ? n / 2 : k_at;
+  return NRT_OK;
+}

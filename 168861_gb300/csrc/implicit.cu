@@ -51,6 +51,7 @@
 
 #include "hh.cuh"
 #include "nrt_solver.h"
+#include "record.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -1519,10 +1520,21 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
   group_sync<kGrid>(grid);  // V^{n+1} complete before the next step reads it
 }
 
+// Recording at the probes of instance `inst` after the step at loop index i (V is that
+// step's output, complete in this CTA's view).  Each thread keeps the same probes for the
+// whole launch.
+__device__ __noinline__ void ph_record(const RecView *rp, int inst, int64_t i, const double *V,
+                                       double dT) {
+  const RecView r = *rp;
+  const int a = r.p0[inst], b = r.p0[inst + 1];
+  for (int p = a + threadIdx.x; p < b; p += blockDim.x) record_probe(r, p, i, V[r.src[p]], dT);
+}
+
 template <typename T, bool kGrid>
 __global__ void __launch_bounds__(kThreads, 3) implicit_steps(const PackView *pvp, const ImView *ivp,
                                                            int nsteps, int force, double *V0,
-                                                           double *V1, int cur) {
+                                                           double *V1, int cur,
+                                                           const RecView *rec) {
   const ImView &iv = *ivp;
   Shared S = carve(dyn_smem(), iv.m);
   cg::grid_group grid = cg::this_grid();
@@ -1557,6 +1569,7 @@ __global__ void __launch_bounds__(kThreads, 3) implicit_steps(const PackView *pv
                                      : (i >= in.ion && i <= in.ioff);
       implicit_one_step<T, kGrid>(c, grid, S, parity, ((cur + s) & 1) ? V1 : V0,
                                   ((cur + s + 1) & 1) ? V1 : V0, active, inst_n, 0);
+      if (rec && blockIdx.x == 0) ph_record(rec, 0, i, ((cur + s + 1) & 1) ? V1 : V0, in.dT);
     }
     if ((nsteps - s) & 1) {  // the run ended inside the launch: each CTA moves its rows
       double *dst = ((cur + nsteps) & 1) ? V1 : V0;
@@ -1586,6 +1599,7 @@ __global__ void __launch_bounds__(kThreads, 3) implicit_steps(const PackView *pv
                                        : (i >= in.ion && i <= in.ioff);
         implicit_one_step<T, kGrid>(c, grid, S, parity, ((cur + s) & 1) ? V1 : V0,
                                     ((cur + s + 1) & 1) ? V1 : V0, active, c.r1 - c.r0, inst);
+        if (rec) ph_record(rec, inst, i, ((cur + s + 1) & 1) ? V1 : V0, in.dT);
       }
       if ((nsteps - s) & 1) {  // finished early: put its latest V where the others' is
         double *dst = ((cur + nsteps) & 1) ? V1 : V0;
@@ -2081,7 +2095,9 @@ static int implicit_launch(Engine &e, int nsteps, int force) {
   const ImView *iv = S.d_iv;
   double *V0 = e.V[0], *V1 = e.V[1];
   int cur = e.cur;
-  void *args[] = {&pv, &iv, &nsteps, &force, &V0, &V1, &cur};
+  // the drop-in per-call loop (force >= 0) has no device loop index: it is not recorded
+  const RecView *rec = force < 0 ? e.record_view() : nullptr;
+  void *args[] = {&pv, &iv, &nsteps, &force, &V0, &V1, &cur, &rec};
   const bool mixed = e.opt.precision == NRT_MIXED;
   if (S.grid_mode) {
     const void *k = mixed ? (const void *)implicit_steps<float, true> : (const void *)implicit_steps<double, true>;

@@ -129,6 +129,26 @@ struct PackView {
   InstDev *inst;
 };
 
+// Device-side recording at probes (record.cu, record.cuh).  Probes are sorted by
+// instance: those of instance q are [p0[q], p0[q+1]).
+struct RecView {
+  int32_t nprobe;
+  int32_t max_spikes;
+  int64_t origin;      // loop index at which the sample counter starts
+  int64_t interval;    // sample when (i - origin + 1) % (interval + 1) == 0
+  int64_t cap;         // samples kept per probe
+  double thresh;       // spike threshold
+  const int64_t *src;  // global element read for each probe
+  const int32_t *inst; // instance of each probe
+  const int32_t *p0;   // [ninst + 1]
+  int64_t *nsamp;      // samples taken per probe
+  int32_t *nspike;     // crossings found per probe
+  int64_t *prev_i;     // loop index of the last value seen
+  double *prev_v;      // the last value seen
+  double *val;         // [nprobe][cap]
+  double *spk;         // [nprobe][max_spikes]
+};
+
 struct DeviceBuffer {
   void *ptr = nullptr;
   size_t bytes = 0;
@@ -180,5 +200,8 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
 int launch_terminal_fixup(const Topo *topo, const int64_t *terms, int64_t nterm, double *V,
                           float *Vf, cudaStream_t st);
 int launch_advance_base(InstDev *inst, int32_t ninst, int64_t steps, cudaStream_t st);
+// Recording after explicit step k (record.cu); V is that step's output.
+int launch_record_step(const RecView &r, const InstDev *inst, int k, const double *V,
+                       cudaStream_t st);
 
 }  // namespace nrt

@@ -17,6 +17,7 @@ struct Arena {
 };
 
 struct ImplicitState;  // implicit.cu
+struct RecState;       // record.cu
 
 struct Engine {
   nrt_options opt{};
@@ -34,6 +35,7 @@ struct Engine {
   cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};  // one per starting buffer parity
   std::vector<std::vector<float>> hostf;  // staging for FP32 uploads
   ImplicitState *im = nullptr;
+  RecState *rec = nullptr;                // recording at probes, or null
 
   int init(const nrt_problem *probs, int32_t count, const nrt_options *o);
   int step(int k, int force);
@@ -45,6 +47,16 @@ struct Engine {
   int implicit_init();
   int implicit_step(int k, int force);
   void implicit_release();
+  // record.cu
+  int record_config(const nrt_record_config *c);
+  int record_read(int64_t *num_samples, double *times, double *values, int32_t *num_spikes,
+                  double *spike_times);
+  const RecView *record_view() const;  // device copy for the implicit kernel, or null
+  const RecView &rec_view_host() const;  // host copy (device pointers) for kernel arguments
+  int upload_and_init(RecState *R, const std::vector<int64_t> &src,
+                      const std::vector<int64_t> &raw, const std::vector<int32_t> &sinst,
+                      const std::vector<int32_t> &p0);
+  void record_release();
   ~Engine();
 };
 

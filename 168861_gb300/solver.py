@@ -69,6 +69,73 @@ def step_size(spec, d: Derived) -> float:
     return spec.dt_abs if spec.dt_abs > 0 else d.dT_crit * spec.dtf
 
 
+def measurement_point(dx, dist_mes: float) -> int:
+    """The reference's measurement point (src/init.cpp:339-358) for per-element lengths
+    dx (after the strain scaling) and a distance: nrt_measurement_point."""
+    lib = _lib.load()
+    d = np.ascontiguousarray(dx, dtype=np.float64)
+    out = ctypes.c_int32(0)
+    check(lib.nrt_measurement_point(len(d), _p(d, ctypes.c_double), float(dist_mes),
+                                    ctypes.byref(out)), "nrt_measurement_point")
+    return out.value
+
+
+@dataclasses.dataclass
+class Recording:
+    """What device-side recording kept, per probe in configuration order: the samples
+    (times i*dT and values) and the spike times.  num_samples / num_spikes count every
+    sample and crossing, also those past the kept capacity."""
+    times: list
+    values: list
+    num_samples: np.ndarray
+    spikes: list
+    num_spikes: np.ndarray
+
+    def trace_text(self, probe: int = 0) -> str:
+        """One probe's samples in the reference's trace format (src/neurite.cpp:248:
+        "%.20f %.20f" of time and potential, one line per sample)."""
+        return "".join("%.20f %.20f\n" % (t, v)
+                       for t, v in zip(self.times[probe], self.values[probe]))
+
+
+class _Recorder:
+    """nrt_record / nrt_record_read (and the batch forms) for a handle."""
+
+    def _record(self, fn, instances, elements, origin, interval, capacity, threshold,
+                max_spikes):
+        el = np.ascontiguousarray(elements, dtype=np.int32)
+        cfg = _lib.RecordConfig()
+        cfg.num_probes = len(el)
+        self._rec_keep = [el]
+        cfg.element = _p(el, ctypes.c_int32)
+        if instances is not None:
+            ins = np.ascontiguousarray(instances, dtype=np.int32)
+            self._rec_keep.append(ins)
+            cfg.instance = _p(ins, ctypes.c_int32)
+        cfg.origin = int(origin)
+        cfg.interval = int(interval)
+        cfg.capacity = int(capacity)
+        cfg.threshold = float(threshold)
+        cfg.max_spikes = int(max_spikes)
+        check(fn(self.h, ctypes.byref(cfg)), fn.__name__)
+        self._rec_shape = (len(el), int(capacity), int(max_spikes))
+
+    def _read(self, fn) -> Recording:
+        P, cap, ms = getattr(self, "_rec_shape", (0, 0, 0))
+        ns = np.zeros(P, np.int64)
+        nk = np.zeros(P, np.int32)
+        t = np.zeros((P, max(cap, 1)))
+        v = np.zeros((P, max(cap, 1)))
+        sp = np.zeros((P, max(ms, 1)))
+        check(fn(self.h, _p(ns, ctypes.c_int64), _p(t, ctypes.c_double), _p(v, ctypes.c_double),
+                 _p(nk, ctypes.c_int32), _p(sp, ctypes.c_double)), fn.__name__)
+        kept = np.minimum(ns, cap)
+        ks = np.minimum(nk, ms)
+        return Recording([t[p, :kept[p]].copy() for p in range(P)],
+                         [v[p, :kept[p]].copy() for p in range(P)], ns,
+                         [sp[p, :ks[p]].copy() for p in range(P)], nk)
+
+
 class ProblemArrays:
     """Keeps the numpy arrays of one nrt_problem alive and exposes the C struct."""
 
@@ -136,7 +203,7 @@ def make_options(mode: int, precision: str = "fp64", krylov: str = "gmres",
     return o
 
 
-class Solver:
+class Solver(_Recorder):
     """inc/solver.h:12-24 over the C ABI."""
 
     mode = _lib.NRT_EXPLICIT
@@ -170,6 +237,17 @@ class Solver:
 
     def synchronize(self) -> None:
         check(self.lib.nrt_synchronize(self.h), "nrt_synchronize")
+
+    def record(self, elements, interval: int = 0, origin: int = 1, capacity: int = 4096,
+               threshold: float = 0.0, max_spikes: int = 64) -> None:
+        """Records V at `elements` on the device during run(): a sample every
+        interval + 1 loop iterations counted from `origin` (the reference driver's rule),
+        and upward crossings of `threshold` (V).  Replaces any earlier recording."""
+        self._record(self.lib.nrt_record, None, elements, origin, interval, capacity,
+                     threshold, max_spikes)
+
+    def recording(self) -> Recording:
+        return self._read(self.lib.nrt_record_read)
 
     def stream(self) -> int:
         """The handle's cudaStream_t as an integer (for timing events on it)."""
@@ -233,7 +311,7 @@ class SolverIm(Solver):
     mode = _lib.NRT_IMPLICIT_BE
 
 
-class Batch:
+class Batch(_Recorder):
     """Many independent trees advanced together (one launch per step for all of them)."""
 
     def __init__(self, problems: list[ProblemArrays], mode: int = _lib.NRT_EXPLICIT, **opts):
@@ -259,6 +337,16 @@ class Batch:
 
     def synchronize(self) -> None:
         check(self.lib.nrt_batch_synchronize(self.h), "nrt_batch_synchronize")
+
+    def record(self, probes, interval: int = 0, origin: int = 1, capacity: int = 4096,
+               threshold: float = 0.0, max_spikes: int = 64) -> None:
+        """As Solver.record, for probes given as (instance, element) pairs."""
+        pr = np.asarray(probes, dtype=np.int32).reshape(-1, 2)
+        self._record(self.lib.nrt_batch_record, pr[:, 0], pr[:, 1], origin, interval, capacity,
+                     threshold, max_spikes)
+
+    def recording(self) -> Recording:
+        return self._read(self.lib.nrt_batch_record_read)
 
     def stream(self) -> int:
         v = ctypes.c_void_p()

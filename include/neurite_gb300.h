@@ -229,6 +229,58 @@ int nrt_batch_instance_stats(nrt_batch *b, int64_t *iters, int32_t *last_iters,
 int nrt_batch_destroy(nrt_batch *b);
 
 /* ----------------------------------------------------------------------------------
+ * Recording at measurement points, on the device.
+ *
+ * The reference's driver copies the whole potential to the host every interval + 1 loop
+ * iterations and prints one element of it (src/neurite.cpp:238-249: a snapshot when
+ * `++GL_cont > interval`, then `fprintf(study, "%.20f %.20f\n", time_run,
+ * potential[1][dist_mes_points])`); src/init.cpp:339-358 picks that element.  Here probes
+ * are read on the device after every step of nrt_run / nrt_batch_advance, so a time loop
+ * needs no copy of V:
+ *   - samples follow the same counter: loop index i is sampled when i - origin + 1 is a
+ *     positive multiple of interval + 1 (origin 1 gives the reference's loop);
+ *   - spikes are upward crossings of `threshold` between consecutive steps (value before
+ *     < threshold <= value after), timed by linear interpolation between (i-1) dT and i dT.
+ *     The value at configuration time counts as the value before loop index `origin`.
+ * Steps taken through nrt_update / nrt_calculate are not recorded: that loop snapshots on
+ * the host, as the reference's does.  A probe on a terminal reads what the reference's
+ * snapshot shows there (the copy of its source element, explicit mode). */
+typedef struct nrt_record_config {
+  int32_t num_probes;            /* 0 stops recording */
+  const int32_t *instance;       /* batch: instance of each probe; NULL -> instance 0 */
+  const int32_t *element;        /* element of each probe, local to its instance */
+  int64_t origin;                /* loop index at which the counter starts (reference: 1) */
+  int64_t interval;              /* the reference's `interval` (>= 0) */
+  int64_t capacity;              /* samples kept per probe; later ones are counted only */
+  double threshold;              /* spike threshold, V */
+  int32_t max_spikes;            /* spike times kept per probe; later ones counted only */
+  int32_t reserved[3];
+} nrt_record_config;
+
+/* The reference's measurement point for a distance (src/init.cpp:339-358): the first
+ * element k at which dx[0] + ... + dx[k] >= dist_mes; n/2 when there is none or it is
+ * element 0.  dx is the per-element length after the strain scaling (nrt_problem.dx).
+ * Host only. */
+int nrt_measurement_point(int32_t n, const double *dx, double dist_mes, int32_t *point);
+
+/* Starts recording (replacing an earlier configuration and its data).  Allocates the
+ * recording's device buffers outside any time loop. */
+int nrt_record(nrt_solver *s, const nrt_record_config *cfg);
+int nrt_batch_record(nrt_batch *b, const nrt_record_config *cfg);
+
+/* Copies the recording to host memory (synchronises), probes in configuration order;
+ * any pointer may be NULL.  For probe p:
+ *   num_samples[p]                     samples taken (may exceed capacity);
+ *   times[p*capacity + k], values[...] sample k (k < min(num_samples[p], capacity)), the
+ *                                      time as the reference prints it: i * dT;
+ *   num_spikes[p]                      crossings found (may exceed max_spikes);
+ *   spike_times[p*max_spikes + k]      crossing k, s. */
+int nrt_record_read(nrt_solver *s, int64_t *num_samples, double *times, double *values,
+                    int32_t *num_spikes, double *spike_times);
+int nrt_batch_record_read(nrt_batch *b, int64_t *num_samples, double *times, double *values,
+                          int32_t *num_spikes, double *spike_times);
+
+/* ----------------------------------------------------------------------------------
  * Serving: a request loop (worker thread) that admits simulation requests by device
  * memory budget, packs the requests admitted together into one batch, keeps every
  * batch's state resident, advances all resident batches each tick on their own streams

@@ -158,6 +158,49 @@ class Oracle:
         return x
 
 
+# ---------------------------------------------------------------- recording
+
+def measurement_point(dX, dist_mes: float) -> int:
+    """The reference's measurement point (src/init.cpp:339-358): the first element k at
+    which the running sum of dX (after the strain scaling) reaches dist_mes.  Not found,
+    or found at element 0, gives int(numStepsX / 2)."""
+    temp = 0.0
+    point = 0
+    for k in range(len(dX)):
+        temp = temp + float(dX[k])
+        if temp >= dist_mes:
+            point = k
+            break
+    if point == 0:
+        point = len(dX) // 2
+    return point
+
+
+def recording(i_first: int, v_before, steps, origin: int, interval: int, thresh: float,
+              dT: float):
+    """What device-side recording keeps for one probe, from its value before loop index
+    i_first and after every step i_first, i_first + 1, ... (`steps`, one per loop index).
+
+    Samples follow the reference driver's counter (src/neurite.cpp:241-248: a snapshot when
+    `++GL_cont > interval`, the loop starting at i = origin): loop index i is sampled when
+    (i - origin + 1) is a positive multiple of interval + 1.  Spikes are upward crossings
+    of `thresh` between consecutive steps, timed by linear interpolation between
+    t = (i - 1) dT and i dT.  Returns ({slot: value}, [spike times])."""
+    samples, spikes = {}, []
+    prev = float(v_before)
+    for k, v in enumerate(steps):
+        i = i_first + k
+        v = float(v)
+        if prev < thresh <= v:
+            t0, t1 = (i - 1) * dT, i * dT
+            spikes.append(t0 + (thresh - prev) * (t1 - t0) / (v - prev))
+        q = i - origin + 1
+        if q > 0 and q % (interval + 1) == 0:
+            samples[q // (interval + 1) - 1] = v
+        prev = v
+    return samples, spikes
+
+
 # ---------------------------------------------------------------- reference harness I/O
 
 def spec_dT(spec, dT_crit: float) -> float:
@@ -205,6 +248,11 @@ def read_reference_output(path: str) -> dict:
             out[key] = float(nxt())
         elif key == "numStepsT":
             out[key] = int(nxt())
+        elif key == "measurement_points":
+            k = int(nxt())
+            rows = [(float(nxt()), int(nxt())) for _ in range(k)]
+            out["mp_dist"] = np.array([r[0] for r in rows])
+            out["mp_index"] = np.array([r[1] for r in rows], np.int32)
         elif key == "elem_params":
             n = int(nxt())
             out["eparam"] = np.array([float(nxt()) for _ in range(6 * n)]).reshape(n, 6).T.copy()

@@ -162,6 +162,22 @@ int main(int argc, char **argv) {
   TYPE dm = 0;
   mechanical_model_initialization(in, element, dm);
 
+  // src/neurite.cpp:153: the reference's measurement point (src/init.cpp:339-358) for a
+  // few distances: zero, the first element's dX, fractions of the total length, the
+  // total itself and twice it (never reached).
+  double total = 0;
+  for (int i = 0; i < N; i++) total += element[i]->get_dX();
+  std::vector<double> mp_dist;
+  mp_dist.push_back(0.0);
+  mp_dist.push_back(element[0]->get_dX());
+  mp_dist.push_back(element[0]->get_dX() + element[1]->get_dX());
+  const double frac[] = {0.1, 0.25, 0.5, 0.75, 0.999};
+  for (int q = 0; q < 5; q++) mp_dist.push_back(frac[q] * total);
+  mp_dist.push_back(total);
+  mp_dist.push_back(2.0 * total);
+  std::vector<int> mp_index;
+  for (size_t q = 0; q < mp_dist.size(); q++) mp_index.push_back(measurement_point(element, mp_dist[q]));
+
   // src/neurite.cpp:165-177 (neuriteInit replaced by the two potential buffers it allocates).
   potentialR = new TYPE[2 * N]();
   potential = new TYPE *[2];
@@ -183,6 +199,8 @@ int main(int argc, char **argv) {
   fprintf(o, "dT_crit %.17g\n", dT_crit);
   fprintf(o, "dT %.17g\n", dT);
   fprintf(o, "numStepsT %d\n", numStepsT);
+  fprintf(o, "measurement_points %d\n", (int)mp_dist.size());
+  for (size_t q = 0; q < mp_dist.size(); q++) fprintf(o, "%.17g %d\n", mp_dist[q], mp_index[q]);
   fprintf(o, "elem_params %d\n", N);  // c_m r_a dX W K critical_dT
   for (int i = 0; i < N; i++)
     fprintf(o, "%.17g %.17g %.17g %.17g %.17g %.17g\n", element[i]->get_c_m(),

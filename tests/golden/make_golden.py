@@ -8,7 +8,8 @@ It builds oracle/_ref/ref_harness (src/solverEx-cpu.cpp & co. compiled unmodifie
 oracle/Makefile and oracle/ref_harness.cpp) and oracle/_ref/ref_harness_im (plus
 src/solverIm-cpu.cpp with the RCI shim), runs them on each case below and stores, per
 case, the tree description and the reference outputs: derived parameters, critical and
-chosen dT, a probe trace and the final potential and gates.  The GPU tests and the oracle
+chosen dT, a probe trace, the final potential and gates, and the reference's measurement
+point (src/init.cpp:339-358) for a few distances along the tree.  The GPU tests and the oracle
 tests read only these .npz files, so nothing at test time needs the reference tree.
 """
 from __future__ import annotations
@@ -88,6 +89,7 @@ def main():
             "dT": np.array(out["dT"]), "numStepsT": np.array(out["numStepsT"]),
             "eparam": out["eparam"], "hh_elem": out["hh_elem"], "hparam": out["hparam"],
             "trace": out["trace"], "final_V": out["final_V"], "final_gates": out["final_gates"],
+            "mp_dist": out["mp_dist"], "mp_index": out["mp_index"],
         })
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrays)
         fin = out["final_V"]
