@@ -63,7 +63,7 @@ def test_explicit_recording_is_the_reference_trace(gpu, pkg, name):
         assert np.abs(r.values[c] - tr[:, 1 + c]).max() < TOL_FP64
     # the reference's trace file, written from the device samples
     line = r.trace_text(0).splitlines()[0].split()
-    assert float(line[0]) == tr[0, 0] * float(g["dT"])
+    assert line[0] == "%.20f" % (tr[0, 0] * float(g["dT"]))
     s.close()
 
 
