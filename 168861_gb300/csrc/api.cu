@@ -856,6 +856,13 @@ int nrt_batch_instance_stats(nrt_batch *b, int64_t *iters, int32_t *last_iters,
   return nrt::instance_stats(b->eng, iters, last_iters, nonconverged, last_residual);
 }
 
+int nrt_batch_pass_counts(nrt_batch *b, int64_t *residuals, int64_t *precond_applies,
+                          int64_t *xupdates, int64_t *basis_reads) {
+  if (!b) return nrt::fail(NRT_EINVAL, "null batch");
+  NRT_CUDA(cudaSetDevice(b->eng.device));
+  return nrt::pass_counts(b->eng, residuals, precond_applies, xupdates, basis_reads);
+}
+
 int nrt_batch_destroy(nrt_batch *b) {
   delete b;
   return NRT_OK;

@@ -76,6 +76,7 @@ enum : uint8_t {
   R_DOWNL = 8,   // column at DL
   R_FAR = 16,    // the mother is not j - 1 (first row of a DL child)
   R_HH = 32,     // Hodgkin_Huxley element
+  R_INP = 64,    // nonzero injected current
 };
 
 struct InstStat {
@@ -83,6 +84,10 @@ struct InstStat {
   int32_t last_iters;
   int32_t nonconv;
   double last_res;
+  // passes over the rows (GMRES), for bandwidth accounting: FP64 residuals after the one
+  // fused into the assembly, preconditioner applications, solution updates, and basis
+  // vectors read by the Arnoldi steps (sum of j + 1)
+  int64_t residuals, applies, xupdates, basis;
 };
 
 struct ImView {
@@ -925,7 +930,7 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
       cm[u] = ok ? iv.cmdt[r] : 0.0;
       gj[u] = ok ? iv.g64[r] : 0.0;
       gn[u] = ok ? iv.g64[rp] : 0.0;
-      inp[u] = ok && active ? iv.inp64[r] : 0.0;
+      inp[u] = 0.0;
       xm[u] = ok ? x0_of(Vin, Vout, rm) : 0.0;
       xp[u] = ok ? x0_of(Vin, Vout, rp) : 0.0;
     }
@@ -993,6 +998,7 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
       iv.diag[r] = d;
       if (iv.diagf) iv.diagf[r] = (float)d;
       if (cdiag) cdiag[r] = (T)cj;
+      if (active && (f[u] & R_INP)) inp[u] = iv.inp64[r];  // one row or a few per tree
       double b = cm[u] * v[u] + kdx;
       if (active) b += inp[u];
       iv.rhs[r] = b;
@@ -1409,7 +1415,7 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
   }
   const int budget = iv.max_iter > 0 ? iv.max_iter : (iv.max_iter < 0 ? 0 : (int)inst_n);
   const double inner_rel = sizeof(T) == 4 ? 1e-5 : 0.0;
-  int iters = 0;
+  int iters = 0, n_res = 0, n_app = 0, n_xup = 0, n_basis = 0;
   double res = 0;
   bool converged = false;
   bool x0_pending = true;  // V holds V^{n-1} until the first solution update
@@ -1421,6 +1427,7 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
       double acc[1] = {ph_residual(c, Vout)};
       group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);
       res = sqrt(S.red[0]);
+      n_res++;
     }
     if (res <= target) {
       converged = true;
@@ -1440,6 +1447,7 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
       continue;
     }
     apply_precond(c, c.w.Wb, c.w.Z);
+    n_app++;
     group_sync<kGrid>(grid);  // Z_0 of every row visible before the SpMV
     if (threadIdx.x == 0) {
       S.g[0] = res;
@@ -1490,9 +1498,11 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
       __syncthreads();
       k = j + 1;
       iters++;
+      n_basis += j + 1;
       if (S.flag[0] || iters >= budget || k >= m) break;
       // Z_{j+1} = M^-1 W_{j+1}, only when another Arnoldi step will use it
       apply_precond(c, c.w.Wb + (size_t)(j + 1) * c.pv->ntot, c.w.Z + (size_t)(j + 1) * c.pv->ntot);
+      n_app++;
       group_sync<kGrid>(grid);  // Z_{j+1} of every row visible before the next SpMV
     }
     // ---- x += sum_i y_i s_i Z_i
@@ -1506,6 +1516,7 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
     }
     __syncthreads();
     ph_xupdate(c, k, coef, Vout, x0_pending ? Vin : (const double *)nullptr);
+    n_xup++;
     x0_pending = false;
     group_sync<kGrid>(grid);
   }
@@ -1516,6 +1527,10 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
     st.last_iters = iters;
     st.last_res = res;
     if (!converged) st.nonconv += 1;
+    st.residuals += n_res;
+    st.applies += n_app;
+    st.xupdates += n_xup;
+    st.basis += n_basis;
   }
   group_sync<kGrid>(grid);  // V^{n+1} complete before the next step reads it
 }
@@ -1810,6 +1825,7 @@ int Engine::implicit_plan(size_t &bytes) {
       Topo &t = host.topo[j];
       t.flags &= ~(uint32_t)(F_UP | F_DOWNR | F_DOWNL | F_IDENT);
       uint8_t rf = (t.flags & F_HH) ? R_HH : 0;
+      if (host.inp[j] != 0.0) rf |= R_INP;
       const bool ident = jl == 0 || jl == n - 1 || is_term[j];
       if (ident) {
         t.flags |= F_IDENT;
@@ -2028,7 +2044,7 @@ int Engine::implicit_init() {
   TRYI(up(arena, iv.err, (const int *)nullptr, 1, st));
   NRT_CUDA(cudaMemsetAsync(iv.err, 0, sizeof(int), st));
   TRYI(up(arena, iv.partials, (const double *)nullptr, (size_t)2 * 4096 * kMaxDots, st));
-  std::vector<InstStat> zero(ni, InstStat{0, 0, 0, 0.0});
+  std::vector<InstStat> zero(ni, InstStat{0, 0, 0, 0.0, 0, 0, 0, 0});
   TRYI(up(arena, iv.stats, zero.data(), ni, st));
   iv.work_lev = nullptr;
   iv.cdiag = nullptr;
@@ -2130,7 +2146,7 @@ int implicit_advance(Engine &e, int64_t steps) {
 int instance_stats(Engine &e, int64_t *iters, int32_t *last_iters, int32_t *nonconv,
                    double *last_res) {
   const int32_t ni = e.host.ninst;
-  std::vector<InstStat> s(ni, InstStat{0, 0, 0, 0.0});
+  std::vector<InstStat> s(ni, InstStat{0, 0, 0, 0.0, 0, 0, 0, 0});
   if (e.im) {
     NRT_CUDA(cudaMemcpyAsync(s.data(), e.im->iv.stats, sizeof(InstStat) * ni,
                              cudaMemcpyDeviceToHost, e.stream));
@@ -2141,6 +2157,24 @@ int instance_stats(Engine &e, int64_t *iters, int32_t *last_iters, int32_t *nonc
     if (last_iters) last_iters[i] = s[i].last_iters;
     if (nonconv) nonconv[i] = s[i].nonconv;
     if (last_res) last_res[i] = s[i].last_res;
+  }
+  return NRT_OK;
+}
+
+int pass_counts(Engine &e, int64_t *residuals, int64_t *applies, int64_t *xupdates,
+                int64_t *basis) {
+  const int32_t ni = e.host.ninst;
+  std::vector<InstStat> s(ni, InstStat{0, 0, 0, 0.0, 0, 0, 0, 0});
+  if (e.im) {
+    NRT_CUDA(cudaMemcpyAsync(s.data(), e.im->iv.stats, sizeof(InstStat) * ni,
+                             cudaMemcpyDeviceToHost, e.stream));
+    NRT_CUDA(cudaStreamSynchronize(e.stream));
+  }
+  for (int32_t i = 0; i < ni; i++) {
+    if (residuals) residuals[i] = s[i].residuals;
+    if (applies) applies[i] = s[i].applies;
+    if (xupdates) xupdates[i] = s[i].xupdates;
+    if (basis) basis[i] = s[i].basis;
   }
   return NRT_OK;
 }

@@ -68,5 +68,7 @@ int64_t nonconverged_total(Engine &e);
 int implicit_check(Engine &e);
 int instance_stats(Engine &e, int64_t *iters, int32_t *last_iters, int32_t *nonconv,
                    double *last_res);
+int pass_counts(Engine &e, int64_t *residuals, int64_t *applies, int64_t *xupdates,
+                int64_t *basis);
 
 }  // namespace nrt

@@ -380,6 +380,15 @@ class Batch(_Recorder):
                                                 _p(lr, ctypes.c_double)), "nrt_batch_instance_stats")
         return dict(iters=it, last_iters=li, nonconverged=nc, last_residual=lr)
 
+    def pass_counts(self) -> dict:
+        """Per-instance counts of the implicit kernel's passes over the rows (GMRES):
+        residuals, applies, xupdates, basis."""
+        out = {k: np.zeros(self.count, np.int64) for k in ("residuals", "applies", "xupdates",
+                                                          "basis")}
+        check(self.lib.nrt_batch_pass_counts(self.h, *[_p(out[k], ctypes.c_int64) for k in out]),
+              "nrt_batch_pass_counts")
+        return out
+
     def close(self) -> None:
         if getattr(self, "h", None):
             self.lib.nrt_batch_destroy(self.h)

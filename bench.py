@@ -215,25 +215,53 @@ def algorithmic_bytes_explicit(probs, precision: str) -> float:
     return total
 
 
-def algorithmic_bytes_implicit(probs, iters_per_step: float) -> float:
-    """Bytes per step one backward-Euler step must move, mixed precision (FP32 Krylov
-    vectors, FP64 potential, right-hand side and diagonal), for `iters_per_step` GMRES
-    iterations at about two per refinement cycle:
-      assembly  gates r/w 24, V r 8 and x0 w 8, V^{n-1} r 8, b w 8, diagonal w 12,
-                8 channel parameters 32                                       = 100 B
-      factor    diagonal r 8, conductance r 8, 1/pivot w 4                      =  20 B
-      per cycle residual (rhs, x, diagonal, conductance, index; W_0 w)          =  40 B
-                preconditioner: two passes over 3 rows in, 1 out, + row map     =  40 B
-                x update (Z_i r, V r/w)                                         =  24 B
-      per iteration j of a cycle: SpMV (Z_j, diagonal, conductance, index, y w) =  20 B
-                Gram-Schmidt products and update: W_0..W_j read twice, y r, W_j+1 w
-                                                                 8 (j + 1) + 8 B
-                preconditioner                                                  =  40 B
-    """
-    n = sum(p.num_elem for p in probs)
-    cycles = iters_per_step / 2.0 + 1.0
-    per_it = 20 + 8 * 1.5 + 8 + 40
-    return n * (100 + 20 + cycles * (40 + 40 + 24) + iters_per_step * per_it)
+def _param_bytes(p, fb: int):
+    """Per-compartment parameter bytes the rule counts (where they vary within the tree):
+    (HH compartments, passive compartments)."""
+    a = p.arrays
+    geo = 2 * fb if (_varies(a["c_m"] * a["dx"]) or _varies(a["r_a"] * a["dx"])) else 0
+    chan = sum(fb for k in ("g_Na", "g_K", "G_L", "E_Na", "E_K", "E_L", "ls_Na", "ls_K")
+               if _varies(a[k]))
+    passive = np.ones(p.num_elem, bool)
+    passive[a["hh_elem"]] = False
+    wk = 2 * fb if (_varies(a["W"][passive]) or _varies(a["K"][passive])) else 0
+    return geo + chan, geo + wk
+
+
+def algorithmic_bytes_implicit(probs, steps: int, iters, counts):
+    """Bytes per implicit step (mixed precision), two ways, from the kernel's own counts of
+    its passes over the rows (`Batch.pass_counts`; per instance over `steps` steps).
+
+    rule: the compulsory-traffic rule for an implicit step, per compartment: assembly = HH
+      state (FP32 gates r/w 24) + V r 8 + b w 8 + diagonal w 8 + the parameters that vary
+      within the tree; plus, per Krylov iteration j, a CSR SpMV (36 B with FP32 values and
+      int32 indices at 3 nonzeros per row) and the orthogonalisation, 4 (2 (j + 1) + 1) B.
+      It counts no preconditioner and no refinement residual.
+
+    passes: what this kernel's passes must move per row, counted per pass:
+      assembly (HH 89 / passive 81 B: rowf 1, V^n 8, V^n-1 8, c_m dX/dT 8, 1/(r_a dX) 8,
+        class index 4, gates r/w 24 or W dX, K dX 16; writes diagonal 8 + 4, c 4, b 8, W_0 4),
+      tree factorisation 21 (slot row 4, flag 1, conductance 4, c 4; 1/pivot 4, e 4),
+      each later FP64 residual 37 (b 8, rowf 1, diagonal 8, conductance 8, x 8; W_0 4),
+      each preconditioner application 38 (two passes: slot rows and flags twice 10, e twice
+        8, 1/pivot 4, input 4, eliminated side 4 + 4, output 4),
+      each Arnoldi step j: SpMV 17 (rowf, diagonal, conductance, Z_j, y) + products and
+        update 8 (j + 1) + 8, and its share of the solution update 4,
+      each solution update 17 (rowf 1, V r/w 16), plus V^n 8 once per step for x0.
+    Neighbour values come from cache; topology records of branch rows and the
+    per-instance tables are left out of both.  Returns (rule, passes) in bytes per step."""
+    rule = passes = 0.0
+    for k, p in enumerate(probs):
+        n, n_hh = p.num_elem, int(p.struct.num_hh)
+        ph, pp = _param_bytes(p, 4)
+        asm_rule = n_hh * (24 + 24 + ph) + (n - n_hh) * (24 + pp)
+        I, B = float(iters[k]), float(counts["basis"][k])
+        rule += asm_rule + n * (36 * I + 4 * (2 * B + I)) / steps
+        asm = n_hh * 89 + (n - n_hh) * 81
+        per_run = (37 * counts["residuals"][k] + 38 * counts["applies"][k]
+                   + (17 + 8 + 4) * I + 8 * B + 17 * counts["xupdates"][k])
+        passes += asm + n * (21 + 8) + n * per_run / steps
+    return rule, passes
 
 
 def plain_fp64_single(pkg, torch):
@@ -321,6 +349,7 @@ def run_ours(args, rank: int, world: int):
     b.advance(W)
     b.synchronize()
     it0 = b.instance_stats()["iters"] if implicit else None
+    pc0 = b.pass_counts() if implicit else None
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     if dist:
@@ -337,12 +366,16 @@ def run_ours(args, rank: int, world: int):
     krylov = None
     if implicit:
         ist = b.instance_stats()
+        pc1 = b.pass_counts()
         per = (ist["iters"] - it0) / K
         krylov = {"iters_per_tree_step_mean": float(per.mean()), "iters_per_tree_step_max": float(per.max()),
                   "nonconverged_steps": int(ist["nonconverged"].sum()),
                   "max_last_residual": float(ist["last_residual"].max())}
+    passes = None
     if implicit:
-        alg = algorithmic_bytes_implicit(probs, krylov["iters_per_tree_step_mean"])
+        counts = {key: pc1[key] - pc0[key] for key in pc1}
+        alg, passes = algorithmic_bytes_implicit(probs, K, ist["iters"] - it0, counts)
+        krylov.update({key + "_per_tree_step": float(v.mean()) / K for key, v in counts.items()})
     else:
         alg = algorithmic_bytes_explicit(probs, precision)
     ms, e2e_s, n_all, alg_all = combine_ranks(dist, "cuda", ms, e2e_s, n_elem, alg)
@@ -354,6 +387,14 @@ def run_ours(args, rank: int, world: int):
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
             "algorithmic_bytes_per_step": alg_all}
+    roof_passes = None
+    if passes is not None:
+        # the same kernel time against the bytes its own passes must move (preconditioner
+        # and refinement residuals included), counted from the kernel's pass counters
+        _, _, _, passes_all = combine_ranks(dist, "cuda", ms, e2e_s, 0, passes)
+        a2 = passes_all * K / (ms / 1e3) / 1e9 / world
+        roof_passes = {"bound": "hbm", "achieved": a2, "peak": peak, "unit": "GB/s",
+                       "frac": a2 / peak, "bytes_per_step": passes_all}
     # our kernels launched in the timed region: one persistent launch + one loop-index
     # update per 64-step chunk (implicit); 64 step launches + 1 update per graph (explicit)
     launches = 2 * math.ceil(K / 64) if implicit else K + math.ceil(K / 64)
@@ -366,7 +407,8 @@ def run_ours(args, rank: int, world: int):
         "config": workload_config(wl, count, args.precond), "elements": n_all,
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d / K,
                 "d2h_bytes_per_step": d2h / K, "seconds": e2e_s},
-        "roofline": roof, "gpu_launches": launches, "clocks": clk.summary(),
+        "roofline": roof, "roofline_passes": roof_passes, "gpu_launches": launches,
+        "clocks": clk.summary(),
         "build_seconds": t_build,
         "krylov": krylov,
     }

@@ -226,6 +226,13 @@ int nrt_batch_get_stats(nrt_batch *b, nrt_stats *st);
  * any of which may be NULL. */
 int nrt_batch_instance_stats(nrt_batch *b, int64_t *iters, int32_t *last_iters,
                              int32_t *nonconverged, double *last_residual);
+/* Per-instance counts of the implicit kernel's passes over the rows since creation
+ * (GMRES): FP64 residuals after the one fused into each step's assembly, preconditioner
+ * applications, solution updates, and basis vectors read by the Arnoldi steps (the sum of
+ * j + 1 over steps j).  With the iteration count they give the bytes a step moved.  Arrays
+ * of `count` entries; any may be NULL.  No reference counterpart. */
+int nrt_batch_pass_counts(nrt_batch *b, int64_t *residuals, int64_t *precond_applies,
+                          int64_t *xupdates, int64_t *basis_reads);
 int nrt_batch_destroy(nrt_batch *b);
 
 /* ----------------------------------------------------------------------------------

@@ -249,3 +249,22 @@ def test_bicgstab_unpreconditioned_reports_budget(gpu, pkg):
     assert np.isfinite(s.snapshot()).all()
     assert s.stats().nonconverged_steps == 1
     s.close()
+
+
+def test_pass_counts_follow_the_gmres_structure(gpu, pkg, model):
+    """The kernel's pass counters (used for the bandwidth accounting): one preconditioner
+    application per Arnoldi step, one FP64 residual per solution update (every update is
+    followed by its residual check), and the basis reads of step j are j + 1."""
+    specs = [model.random_tree(seed=s, n_target=n, dt=2.5e-5, tspan=1e-3)
+             for s, n in [(41, 3000), (42, 12000)]]
+    b = pkg.Batch([pkg.ProblemArrays.from_spec(sp, pkg.derive(sp)) for sp in specs], mode=1,
+                  precision="mixed", restart=20, tol=1e-10, tol_mode="rel")
+    b.set_runs([(1, 21, sp.init_time, sp.end_input) for sp in specs])
+    b.advance(20)
+    it = b.instance_stats()["iters"]
+    pc = b.pass_counts()
+    b.close()
+    np.testing.assert_array_equal(pc["applies"], it)
+    np.testing.assert_array_equal(pc["residuals"], pc["xupdates"])
+    assert (pc["xupdates"] >= 20).all()            # at least one update per step
+    assert (pc["basis"] >= it).all() and (pc["basis"] <= it * (it + 1) // 2).all()
