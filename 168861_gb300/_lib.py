@@ -90,7 +90,8 @@ EXPORTS = (
     "nrt_server_create", "nrt_server_submit", "nrt_server_result", "nrt_server_drain",
     "nrt_server_get_stats", "nrt_server_destroy", "nrt_solve_csr_static",
     "nrt_measurement_point", "nrt_record", "nrt_batch_record", "nrt_record_read",
-    "nrt_batch_record_read", "nrt_batch_pass_counts",
+    "nrt_batch_record_read", "nrt_batch_pass_counts", "nrt_get_state", "nrt_set_state",
+    "nrt_batch_get_state", "nrt_batch_set_state",
 )
 
 _lib = None
@@ -145,6 +146,10 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "nrt_measurement_point": [ctypes.c_int32, _f64p, ctypes.c_double,
                                   ctypes.POINTER(ctypes.c_int32)],
         "nrt_batch_pass_counts": [vp, _i64p, _i64p, _i64p, _i64p],
+        "nrt_get_state": [vp, _f64p, _f64p, _f64p, _f64p, _f64p],
+        "nrt_set_state": [vp, _f64p, _f64p, _f64p, _f64p, _f64p],
+        "nrt_batch_get_state": [vp, ctypes.c_int32, _f64p, _f64p, _f64p, _f64p, _f64p],
+        "nrt_batch_set_state": [vp, ctypes.c_int32, _f64p, _f64p, _f64p, _f64p, _f64p],
         "nrt_record": [vp, ctypes.POINTER(RecordConfig)],
         "nrt_batch_record": [vp, ctypes.POINTER(RecordConfig)],
         "nrt_record_read": [vp, _i64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int32), _f64p],

@@ -472,7 +472,7 @@ Engine::~Engine() {
 
 // One loop iteration (update + calculate) for every instance, reading V[cur].
 int Engine::step(int k, int force) {
-  const bool general = !host.invariant && steps_done == 0;
+  const bool general = needs_general();
   if (opt.mode == NRT_IMPLICIT_BE) {
     TRY(implicit_step(k, force));
   } else {
@@ -484,7 +484,93 @@ int Engine::step(int k, int force) {
   }
   cur ^= 1;
   steps_done++;
+  general_next = false;
   terminals_dirty = opt.mode == NRT_EXPLICIT;
+  return NRT_OK;
+}
+
+// State of one instance: V (current buffer), the other buffer (the implicit step's
+// V^{n-1}, used for its initial guess), and the gates of its HH elements in HH order.
+int Engine::get_state(int32_t q, double *Vc, double *Vo, double *m, double *h, double *n) {
+  TRY(fixup());
+  const int64_t o = host.off[q], ne = host.num_elem[q], N = host.ntot;
+  if (Vc) NRT_CUDA(cudaMemcpyAsync(Vc, V[cur] + o, 8 * ne, cudaMemcpyDeviceToHost, stream));
+  if (Vo) NRT_CUDA(cudaMemcpyAsync(Vo, V[cur ^ 1] + o, 8 * ne, cudaMemcpyDeviceToHost, stream));
+  const int64_t h0 = host.hh_off[q], nh = host.hh_off[q + 1] - h0;
+  if ((m || h || n) && nh > 0) {
+    std::vector<double> g(3 * ne);
+    if (opt.precision == NRT_MIXED) {
+      std::vector<float> gf(3 * ne);
+      for (int c = 0; c < 3; c++)
+        NRT_CUDA(cudaMemcpyAsync(gf.data() + c * ne, pv.gatef + c * N + o, 4 * ne,
+                                 cudaMemcpyDeviceToHost, stream));
+      NRT_CUDA(cudaStreamSynchronize(stream));
+      for (int64_t k = 0; k < 3 * ne; k++) g[k] = gf[k];
+    } else {
+      for (int c = 0; c < 3; c++)
+        NRT_CUDA(cudaMemcpyAsync(g.data() + c * ne, pv.gate + c * N + o, 8 * ne,
+                                 cudaMemcpyDeviceToHost, stream));
+    }
+    NRT_CUDA(cudaStreamSynchronize(stream));
+    for (int64_t k = 0; k < nh; k++) {
+      const int64_t el = host.hh_local[h0 + k];
+      if (m) m[k] = g[el];
+      if (h) h[k] = g[ne + el];
+      if (n) n[k] = g[2 * ne + el];
+    }
+  }
+  NRT_CUDA(cudaStreamSynchronize(stream));
+  return NRT_OK;
+}
+
+int Engine::set_state(int32_t q, const double *Vc, const double *Vo, const double *m,
+                      const double *h, const double *n) {
+  NRT_CUDA(cudaStreamSynchronize(stream));
+  TRY(fixup());
+  const int64_t o = host.off[q], ne = host.num_elem[q], N = host.ntot;
+  const bool mixed_ex = opt.precision == NRT_MIXED && opt.mode == NRT_EXPLICIT;
+  std::vector<float> f(ne);
+  auto put_v = [&](int buf, const double *src) -> int {
+    NRT_CUDA(cudaMemcpyAsync(V[buf] + o, src, 8 * ne, cudaMemcpyHostToDevice, stream));
+    if (mixed_ex && Vf[buf]) {  // the FP32 shadow the explicit stencil reads
+      for (int64_t k = 0; k < ne; k++) f[k] = (float)src[k];
+      NRT_CUDA(cudaMemcpyAsync(Vf[buf] + o, f.data(), 4 * ne, cudaMemcpyHostToDevice, stream));
+      NRT_CUDA(cudaStreamSynchronize(stream));
+    }
+    return NRT_OK;
+  };
+  if (Vc) TRY(put_v(cur, Vc));
+  if (Vo) TRY(put_v(cur ^ 1, Vo));
+  const int64_t h0 = host.hh_off[q], nh = host.hh_off[q + 1] - h0;
+  const double *src[3] = {m, h, n};
+  for (int c = 0; c < 3; c++) {
+    if (!src[c] || nh == 0) continue;
+    // read-modify-write of the instance's column: passive elements keep their entries
+    if (opt.precision == NRT_MIXED) {
+      std::vector<float> g(ne);
+      NRT_CUDA(cudaMemcpyAsync(g.data(), pv.gatef + c * N + o, 4 * ne, cudaMemcpyDeviceToHost, stream));
+      NRT_CUDA(cudaStreamSynchronize(stream));
+      for (int64_t k = 0; k < nh; k++) g[host.hh_local[h0 + k]] = (float)src[c][k];
+      NRT_CUDA(cudaMemcpyAsync(pv.gatef + c * N + o, g.data(), 4 * ne, cudaMemcpyHostToDevice, stream));
+    } else {
+      std::vector<double> g(ne);
+      NRT_CUDA(cudaMemcpyAsync(g.data(), pv.gate + c * N + o, 8 * ne, cudaMemcpyDeviceToHost, stream));
+      NRT_CUDA(cudaStreamSynchronize(stream));
+      for (int64_t k = 0; k < nh; k++) g[host.hh_local[h0 + k]] = src[c][k];
+      NRT_CUDA(cudaMemcpyAsync(pv.gate + c * N + o, g.data(), 8 * ne, cudaMemcpyHostToDevice, stream));
+    }
+    NRT_CUDA(cudaStreamSynchronize(stream));
+  }
+  // explicit: a terminal that does not copy its source breaks the fused step's invariant;
+  // the next step then runs in the general form, as a first step from such a state does
+  if (Vc && opt.mode == NRT_EXPLICIT) {
+    for (int64_t t : host.terms) {
+      if (t < o || t >= o + ne) continue;
+      const Topo &tp = host.topo[t];
+      const int64_t s = (tp.flags & F_ROOT) ? t + 1 : (int64_t)tp.mother;
+      if (Vc[t - o] != Vc[s - o]) general_next = true;
+    }
+  }
   return NRT_OK;
 }
 
@@ -500,7 +586,7 @@ int Engine::fixup() {
 int Engine::advance(int64_t steps) {
   if (opt.mode == NRT_IMPLICIT_BE) return implicit_advance(*this, steps);
   int64_t left = steps;
-  while (left > 0 && (steps_done == 0 && !host.invariant)) {  // exact first step
+  while (left > 0 && needs_general()) {  // exact first step
     TRY(step(0, -1));
     if (rec) TRY(launch_record_step(rec_view_host(), pv.inst, 0, V[cur], stream));
     TRY(launch_advance_base(pv.inst, pv.ninst, 1, stream));
@@ -866,6 +952,37 @@ int nrt_batch_pass_counts(nrt_batch *b, int64_t *residuals, int64_t *precond_app
 int nrt_batch_destroy(nrt_batch *b) {
   delete b;
   return NRT_OK;
+}
+
+int nrt_get_state(nrt_solver *s, double *V, double *V_other, double *m, double *h, double *n) {
+  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+  NRT_CUDA(cudaSetDevice(s->eng.device));
+  int rc = s->eng.get_state(0, V, V_other, m, h, n);
+  return rc ? rc : nrt::implicit_check(s->eng);
+}
+
+int nrt_set_state(nrt_solver *s, const double *V, const double *V_other, const double *m,
+                  const double *h, const double *n) {
+  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+  NRT_CUDA(cudaSetDevice(s->eng.device));
+  return s->eng.set_state(0, V, V_other, m, h, n);
+}
+
+int nrt_batch_get_state(nrt_batch *b, int32_t instance, double *V, double *V_other, double *m,
+                        double *h, double *n) {
+  if (!b) return nrt::fail(NRT_EINVAL, "null batch");
+  if (instance < 0 || instance >= b->eng.pv.ninst) return nrt::fail(NRT_EINVAL, "instance out of range");
+  NRT_CUDA(cudaSetDevice(b->eng.device));
+  int rc = b->eng.get_state(instance, V, V_other, m, h, n);
+  return rc ? rc : nrt::implicit_check(b->eng);
+}
+
+int nrt_batch_set_state(nrt_batch *b, int32_t instance, const double *V, const double *V_other,
+                        const double *m, const double *h, const double *n) {
+  if (!b) return nrt::fail(NRT_EINVAL, "null batch");
+  if (instance < 0 || instance >= b->eng.pv.ninst) return nrt::fail(NRT_EINVAL, "instance out of range");
+  NRT_CUDA(cudaSetDevice(b->eng.device));
+  return b->eng.set_state(instance, V, V_other, m, h, n);
 }
 
 int nrt_record(nrt_solver *s, const nrt_record_config *cfg) {

@@ -32,6 +32,7 @@ struct Engine {
   int64_t *terms = nullptr;
   int64_t steps_done = 0;
   bool terminals_dirty = false;
+  bool general_next = false;  // explicit: the next step runs in the general form
   cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};  // one per starting buffer parity
   std::vector<std::vector<float>> hostf;  // staging for FP32 uploads
   ImplicitState *im = nullptr;
@@ -41,6 +42,10 @@ struct Engine {
   int step(int k, int force);
   int advance(int64_t steps);
   int fixup();
+  bool needs_general() const { return general_next || (!host.invariant && steps_done == 0); }
+  int get_state(int32_t q, double *Vc, double *Vo, double *m, double *h, double *n);
+  int set_state(int32_t q, const double *Vc, const double *Vo, const double *m, const double *h,
+                const double *n);
   int get_stats(nrt_stats *st);
   // implicit.cu
   int implicit_plan(size_t &bytes);

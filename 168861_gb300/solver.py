@@ -98,6 +98,31 @@ class Recording:
                        for t, v in zip(self.times[probe], self.values[probe]))
 
 
+@dataclasses.dataclass
+class State:
+    """A tree's state (nrt_get_state): V, the other potential buffer, and the gates of its
+    HH elements in HH order."""
+    V: np.ndarray
+    V_other: np.ndarray
+    m: np.ndarray
+    h: np.ndarray
+    n: np.ndarray
+
+
+def _state_get(fn, h, args, ne, nh, where):
+    st = State(np.empty(ne), np.empty(ne), np.empty(nh), np.empty(nh), np.empty(nh))
+    g = [_p(x, ctypes.c_double) if len(x) else None for x in (st.m, st.h, st.n)]
+    check(fn(h, *args, _p(st.V, ctypes.c_double), _p(st.V_other, ctypes.c_double), *g), where)
+    return st
+
+
+def _state_set(fn, h, args, st: State, where):
+    arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+            for a in (st.V, st.V_other, st.m, st.h, st.n)]
+    ptr = [None if a is None or not len(a) else _p(a, ctypes.c_double) for a in arrs]
+    check(fn(h, *args, *ptr), where)
+
+
 class _Recorder:
     """nrt_record / nrt_record_read (and the batch forms) for a handle."""
 
@@ -238,6 +263,12 @@ class Solver(_Recorder):
     def synchronize(self) -> None:
         check(self.lib.nrt_synchronize(self.h), "nrt_synchronize")
 
+    def get_state(self) -> State:
+        return _state_get(self.lib.nrt_get_state, self.h, (), self.n, self.num_hh, "nrt_get_state")
+
+    def set_state(self, st: State) -> None:
+        _state_set(self.lib.nrt_set_state, self.h, (), st, "nrt_set_state")
+
     def record(self, elements, interval: int = 0, origin: int = 1, capacity: int = 4096,
                threshold: float = 0.0, max_spikes: int = 64) -> None:
         """Records V at `elements` on the device during run(): a sample every
@@ -337,6 +368,14 @@ class Batch(_Recorder):
 
     def synchronize(self) -> None:
         check(self.lib.nrt_batch_synchronize(self.h), "nrt_batch_synchronize")
+
+    def get_state(self, i: int) -> State:
+        p = self.problems[i]
+        return _state_get(self.lib.nrt_batch_get_state, self.h, (int(i),), p.num_elem,
+                          int(p.struct.num_hh), "nrt_batch_get_state")
+
+    def set_state(self, i: int, st: State) -> None:
+        _state_set(self.lib.nrt_batch_set_state, self.h, (int(i),), st, "nrt_batch_set_state")
 
     def record(self, probes, interval: int = 0, origin: int = 1, capacity: int = 4096,
                threshold: float = 0.0, max_spikes: int = 64) -> None:

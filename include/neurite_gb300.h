@@ -236,6 +236,31 @@ int nrt_batch_pass_counts(nrt_batch *b, int64_t *residuals, int64_t *precond_app
 int nrt_batch_destroy(nrt_batch *b);
 
 /* ----------------------------------------------------------------------------------
+ * State export / import, for checkpoints and for moving a tree between handles (serving
+ * preemption).  The reference exports V only (Solver::snapshot, inc/solver.h:21) and keeps
+ * its gates inside the Hodgkin_Huxley objects; no reference counterpart.
+ *
+ * The state of a tree is:
+ *   V        the latest potential (num_elem), as nrt_snapshot returns it;
+ *   V_other  the other potential buffer (num_elem): in implicit mode V^{n-1}, which the
+ *            next step's initial guess 2 V^n - V^{n-1} uses (the reference's prevT/currT
+ *            pair, src/neurite.cpp:165-170); in explicit mode scratch;
+ *   m, h, n  the gates of its HH elements (num_hh each, HH order).
+ * Any pointer may be NULL (that part is neither read nor written).  Restoring a state taken
+ * from a handle with the same tree and options continues the run exactly as the original
+ * would have (same arithmetic; mixed-precision gates are FP32 and round-trip exactly).  The
+ * loop index is the caller's: pass it to nrt_run or nrt_batch_set_runs.  In explicit mode a
+ * V whose terminals do not copy their source elements makes the next step take the
+ * reference's general form (as a first step from such a state does). */
+int nrt_get_state(nrt_solver *s, double *V, double *V_other, double *m, double *h, double *n);
+int nrt_set_state(nrt_solver *s, const double *V, const double *V_other, const double *m,
+                  const double *h, const double *n);
+int nrt_batch_get_state(nrt_batch *b, int32_t instance, double *V, double *V_other, double *m,
+                        double *h, double *n);
+int nrt_batch_set_state(nrt_batch *b, int32_t instance, const double *V, const double *V_other,
+                        const double *m, const double *h, const double *n);
+
+/* ----------------------------------------------------------------------------------
  * Recording at measurement points, on the device.
  *
  * The reference's driver copies the whole potential to the host every interval + 1 loop
