@@ -61,7 +61,7 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxPiece = 256;                 // longest segment piece one sweep handles
 constexpr int kMaxDots = kMaxRestart + 1;
-constexpr int kTileBytes = 48 * 1024;          // shared-memory staging for the sweeps
+constexpr int kTileBytes = 44 * 1024;          // shared-memory staging for the sweeps
 constexpr int kU = 4;                          // rows per thread in flight: SpMV + products
 constexpr int kV = 8;                          // rows per thread in flight: streaming passes
 constexpr int kA = 1;                          // rows per thread in flight: assembly
@@ -1201,127 +1201,6 @@ __device__ __noinline__ void ph_xupdate(Ctx<T, kGrid> c, int k, const T *coef, d
   }
 }
 
-// The solution update fused with the next cycle's FP64 residual, for one instance per CTA
-// (batch launches): V += sum_{i < k} coef_i Z_i, then r = b - A V into W_0.  Rows go in
-// chunks of kV * blockDim.  A chunk's new values are staged in shared memory first; a row's
-// neighbour then comes from there (same chunk), from V (an earlier chunk, already written)
-// or is updated on the fly from its old value (a later chunk) with the same arithmetic its
-// own thread will use.  Saves the residual's second pass over V.  Returns the thread's part
-// of ||r||^2.
-template <typename T>
-__device__ __forceinline__ double x_updated(const Ctx<T, false> &c, int k, const T *coef,
-                                            const double *Vout, const double *Vin, int64_t q) {
-  const int64_t N = c.pv->ntot;
-  T a = 0;
-  for (int i = 0; i < k; i++) a += coef[i] * c.w.Z[(size_t)i * N + q];
-  const double base = Vin ? x0_of(Vin, Vout, q) : Vout[q];
-  return base + (double)a;
-}
-
-template <typename T>
-__device__ __noinline__ double ph_xupdate_residual(Ctx<T, false> c, int k, const T *coef,
-                                                   double *Vout, const double *Vin) {
-  const PackView &pv = *c.pv;
-  const ImView &iv = *c.iv;
-  const int64_t N = pv.ntot, stride = blockDim.x, C = kV * stride;
-  Shared S = carve(dyn_smem(), iv.m);
-  double *xs = (double *)S.tile;  // kV * blockDim doubles (16 KB), free between the sweeps
-  double acc = 0;
-  for (int64_t cb = c.r0; cb < c.r1; cb += C) {
-    const int64_t ce = cb + C < c.r1 ? cb + C : c.r1;
-    // new values of this chunk's rows (identity rows keep theirs)
-    {
-      T a[kV];
-      uint8_t fl[kV];
-#pragma unroll
-      for (int u = 0; u < kV; u++) {
-        const int64_t r = cb + threadIdx.x + u * stride;
-        a[u] = 0;
-        fl[u] = r < ce ? iv.rowf[r] : (uint8_t)R_IDENT;
-      }
-#pragma unroll 1
-      for (int i = 0; i < k; i++) {
-        const T ci = coef[i];
-        const T *Zi = c.w.Z + (size_t)i * N;
-        T z[kV];
-#pragma unroll
-        for (int u = 0; u < kV; u++) {
-          const int64_t r = cb + threadIdx.x + u * stride;
-          z[u] = r < ce ? Zi[r] : (T)0;
-        }
-#pragma unroll
-        for (int u = 0; u < kV; u++) a[u] += ci * z[u];
-      }
-#pragma unroll
-      for (int u = 0; u < kV; u++) {
-        const int64_t r = cb + threadIdx.x + u * stride;
-        if (r >= ce) continue;
-        if (fl[u] & R_IDENT) {
-          xs[r - cb] = Vout[r];
-        } else {
-          const double base = Vin ? x0_of(Vin, Vout, r) : Vout[r];
-          xs[r - cb] = base + (double)a[u];
-        }
-      }
-    }
-    __syncthreads();  // the chunk's new values staged
-    auto xval = [&](int64_t q) -> double {
-      if (q < cb) return Vout[q];
-      if (q < ce) return xs[q - cb];
-      return x_updated(c, k, coef, Vout, Vin, q);
-    };
-#pragma unroll 1
-    for (int u0 = 0; u0 < kV; u0 += kR) {
-      // every independent load of the kR rows first
-      uint8_t f[kR];
-      double dg[kR], gm[kR], gp[kR], rh[kR];
-#pragma unroll
-      for (int u = 0; u < kR; u++) {
-        const int64_t r = cb + threadIdx.x + (u0 + u) * stride;
-        const bool ok = r < ce;
-        f[u] = ok ? iv.rowf[r] : (uint8_t)R_IDENT;
-        dg[u] = ok ? iv.diag[r] : 0.0;
-        gm[u] = ok ? iv.g64[r] : 0.0;
-        gp[u] = ok && r + 1 < N ? iv.g64[r + 1] : 0.0;
-        rh[u] = ok ? iv.rhs[r] : 0.0;
-      }
-#pragma unroll
-      for (int u = 0; u < kR; u++) {
-        const int64_t r = cb + threadIdx.x + (u0 + u) * stride;
-        if (r >= ce) continue;
-        if (f[u] & R_IDENT) {
-          c.w.Wb[r] = 0;
-          continue;
-        }
-        const double xr = xs[r - cb];
-        double mo = 0, xp = 0, xl = 0, gl = 0;
-        if (f[u] & (R_FAR | R_DOWNL)) {
-          const Topo t = pv.topo[r];
-          mo = (f[u] & R_FAR) ? xval(t.mother) : xval(r - 1);
-          if (f[u] & R_DOWNL) {
-            gl = iv.g64[t.dl];
-            xl = xval(t.dl);
-          }
-        } else if (f[u] & R_UP) {
-          mo = xval(r - 1);
-        }
-        if (f[u] & R_DOWNR) xp = xval(r + 1);
-        // (A x)_r in the order of apply_rows: diagonal, mother, DR, DL
-        double s = dg[u] * xr;
-        if (f[u] & R_UP) s -= gm[u] * mo;
-        if (f[u] & R_DOWNR) s -= gp[u] * xp;
-        if (f[u] & R_DOWNL) s -= gl * xl;
-        const double rr = rh[u] - s;
-        c.w.Wb[r] = (T)rr;
-        acc += rr * rr;
-        Vout[r] = xr;
-      }
-    }
-    __syncthreads();  // V of this chunk written before the next chunk reads it; xs reusable
-  }
-  return acc;
-}
-
 // ---- BiCGSTAB (right-preconditioned, on the correction equation of one refinement cycle)
 
 // p = r + beta (p - omega v); beta == 0 gives p = r.
@@ -1537,17 +1416,13 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
   const int budget = iv.max_iter > 0 ? iv.max_iter : (iv.max_iter < 0 ? 0 : (int)inst_n);
   const double inner_rel = sizeof(T) == 4 ? 1e-5 : 0.0;
   int iters = 0, n_res = 0, n_app = 0, n_xup = 0, n_basis = 0;
-  double res = 0, res_next = 0;
-  bool converged = false, have_res = false;
+  double res = 0;
+  bool converged = false;
   bool x0_pending = true;  // V holds V^{n-1} until the first solution update
   for (int cycle = 0;; cycle++) {
     // ---- cycle start: true residual r = b - A x in FP64, W_0 = r, Z_0 = M^-1 r
     if (cycle == 0) {
       res = res0;
-    } else if (have_res) {  // computed with the solution update
-      res = res_next;
-      have_res = false;
-      n_res++;
     } else {
       double acc[1] = {ph_residual(c, Vout)};
       group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);
@@ -1640,17 +1515,8 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
       for (int i = 0; i < k; i++) coef[i] = (T)(S.y[i] * S.s[i]);
     }
     __syncthreads();
-    if constexpr (!kGrid) {
-      // one instance per CTA: the update and the next residual in one pass
-      double acc[1] = {ph_xupdate_residual(c, k, coef, Vout,
-                                           x0_pending ? Vin : (const double *)nullptr)};
-      group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);
-      res_next = sqrt(S.red[0]);
-      have_res = true;
-    } else {
-      ph_xupdate(c, k, coef, Vout, x0_pending ? Vin : (const double *)nullptr);
-      group_sync<kGrid>(grid);
-    }
+    ph_xupdate(c, k, coef, Vout, x0_pending ? Vin : (const double *)nullptr);
+    group_sync<kGrid>(grid);
     n_xup++;
     x0_pending = false;
   }
@@ -1680,7 +1546,7 @@ __device__ __noinline__ void ph_record(const RecView *rp, int inst, int64_t i, c
 }
 
 template <typename T, bool kGrid>
-__global__ void __launch_bounds__(kThreads, 3) implicit_steps(const PackView *pvp, const ImView *ivp,
+__global__ void __launch_bounds__(kThreads, 4) implicit_steps(const PackView *pvp, const ImView *ivp,
                                                            int nsteps, int force, double *V0,
                                                            double *V1, int cur,
                                                            const RecView *rec) {

@@ -228,7 +228,7 @@ def _param_bytes(p, fb: int):
     return geo + chan, geo + wk
 
 
-def algorithmic_bytes_implicit(probs, steps: int, iters, counts, fused: bool = True):
+def algorithmic_bytes_implicit(probs, steps: int, iters, counts):
     """Bytes per implicit step (mixed precision), two ways, from the kernel's own counts of
     its passes over the rows (`Batch.pass_counts`; per instance over `steps` steps).
 
@@ -242,8 +242,7 @@ def algorithmic_bytes_implicit(probs, steps: int, iters, counts, fused: bool = T
       assembly (HH 89 / passive 81 B: rowf 1, V^n 8, V^n-1 8, c_m dX/dT 8, 1/(r_a dX) 8,
         class index 4, gates r/w 24 or W dX, K dX 16; writes diagonal 8 + 4, c 4, b 8, W_0 4),
       tree factorisation 21 (slot row 4, flag 1, conductance 4, c 4; 1/pivot 4, e 4),
-      each later FP64 residual 37 (b 8, rowf 1, diagonal 8, conductance 8, x 8; W_0 4), or
-        28 in batch launches, where it shares the solution update's pass (rowf and V once),
+      each later FP64 residual 37 (b 8, rowf 1, diagonal 8, conductance 8, x 8; W_0 4),
       each preconditioner application 38 (two passes: slot rows and flags twice 10, e twice
         8, 1/pivot 4, input 4, eliminated side 4 + 4, output 4),
       each Arnoldi step j: SpMV 17 (rowf, diagonal, conductance, Z_j, y) + products and
@@ -259,7 +258,7 @@ def algorithmic_bytes_implicit(probs, steps: int, iters, counts, fused: bool = T
         I, B = float(iters[k]), float(counts["basis"][k])
         rule += asm_rule + n * (36 * I + 4 * (2 * B + I)) / steps
         asm = n_hh * 89 + (n - n_hh) * 81
-        per_run = ((28 if fused else 37) * counts["residuals"][k] + 38 * counts["applies"][k]
+        per_run = (37 * counts["residuals"][k] + 38 * counts["applies"][k]
                    + (17 + 8 + 4) * I + 8 * B + 17 * counts["xupdates"][k])
         passes += asm + n * (21 + 8) + n * per_run / steps
     return rule, passes
@@ -375,9 +374,7 @@ def run_ours(args, rank: int, world: int):
     passes = None
     if implicit:
         counts = {key: pc1[key] - pc0[key] for key in pc1}
-        # more than one tree: block-per-instance launch, residuals fused with the update
-        alg, passes = algorithmic_bytes_implicit(probs, K, ist["iters"] - it0, counts,
-                                                 fused=len(probs) > 1)
+        alg, passes = algorithmic_bytes_implicit(probs, K, ist["iters"] - it0, counts)
         krylov.update({key + "_per_tree_step": float(v.mean()) / K for key, v in counts.items()})
     else:
         alg = algorithmic_bytes_explicit(probs, precision)
