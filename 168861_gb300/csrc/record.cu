@@ -79,6 +79,10 @@ int Engine::record_config(const nrt_record_config *c) {
     set_error("bad record configuration (negative size or null element array)");
     return NRT_EINVAL;
   }
+  if ((double)P * (double)(c->capacity + c->max_spikes) * 8.0 > 1e12) {  // sizes cannot wrap
+    set_error("recording buffers would exceed 1 TB");
+    return NRT_EINVAL;
+  }
   std::vector<int32_t> pin(P), pel(P);
   for (int32_t p = 0; p < P; p++) {
     const int32_t q = c->instance ? c->instance[p] : 0;
