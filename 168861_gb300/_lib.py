@@ -41,7 +41,7 @@ class Options(ctypes.Structure):
         ("precond", ctypes.c_int32), ("restart", ctypes.c_int32), ("tol_mode", ctypes.c_int32),
         ("tol", ctypes.c_double), ("max_iter", ctypes.c_int32), ("device", ctypes.c_int32),
         ("use_graphs", ctypes.c_int32), ("schedule", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 6),
+        ("tiled", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5),
     ]
 
 

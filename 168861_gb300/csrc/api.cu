@@ -370,7 +370,7 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   const bool mixed = opt.precision == NRT_MIXED;
   // Sizes: V x2, topo, coefficient rows, gates, HH rows, instances, terminals, implicit.
   size_t bytes = 2 * al(8 * N) + al(sizeof(Topo) * N) + al(sizeof(InstDev) * count) +
-                 al(8 * host.terms.size() + 8);
+                 al(8 * host.terms.size() + 8) + al(16);
   const size_t hpn = (size_t)HP_ROWS * host.hp_ld;
   if (!host.hp_cls.empty()) bytes += al(4 * N);
   if (mixed && opt.mode == NRT_EXPLICIT) bytes += al(4 * N);  // flags of the compact step
@@ -423,6 +423,12 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   }
   pv.topo = topo;
   pv.inst = inst;
+  int *err = nullptr;
+  TRY(upload(arena, err, (const int *)nullptr, 4, st));
+  NRT_CUDA(cudaMemsetAsync(err, 0, 16, st));
+  pv.err = err;
+  pv.tile_blocks = (mixed && opt.mode == NRT_EXPLICIT && opt.tiled != 0)
+                       ? explicit_tile_blocks(device, N) : 0;
   if (mixed) {
     auto f32 = [&](const std::vector<double> &v) {
       hostf.emplace_back(v.size());
@@ -676,6 +682,7 @@ int nrt_options_default(nrt_options *o) {
   o->max_iter = 0;
   o->device = -1;
   o->use_graphs = 1;
+  o->tiled = 1;
   return NRT_OK;
 }
 

@@ -25,8 +25,11 @@
 // Instances: elements of many trees are packed back to back (global indices); the
 // instance id in the flags selects dT, the stimulus window and the loop index, so one
 // launch advances every tree.  An instance whose loop range is exhausted copies V.
+#include <algorithm>
+
 #include "hh.cuh"
 #include "nrt_internal.h"
+#include "tma.cuh"
 
 namespace nrt {
 
@@ -193,6 +196,226 @@ __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, in
   Fout[j] = (float)vn;
 }
 
+// ---- the mixed step with TMA-staged tiles
+//
+// Same arithmetic as explicit_step_mixed<false> (bit for bit), reorganised for memory-level
+// parallelism: persistent CTAs walk tiles of kTileE consecutive elements; one thread issues
+// bulk copies (cp.async.bulk) of the tile's contiguous element arrays -- flags, FP32 shadow
+// of V with its one-element halo, conductances with theirs, FP64 V, dT/(c_m dX), the class
+// index, and the gates (or W dX, K dX when few elements are HH) -- into shared memory on an
+// mbarrier, while the CTA computes the previous tile from the other buffer.  About 20 KB
+// per tile are in flight per CTA instead of one load per thread.  Far neighbours (branch
+// points, DL children), the per-instance record and the parameter tables come from global
+// memory as before.
+constexpr int kTileE = 512;                      // elements per tile
+constexpr int kTileThreads = 256;                // two elements per thread
+constexpr int kR4 = (kTileE + 8) * 4;            // a 4-byte array's window, 16-byte rounded
+constexpr int kR8 = (kTileE + 4) * 8;            // the FP64 window
+enum { TO_FL = 0, TO_F = kR4, TO_GAX = 2 * kR4, TO_V = 3 * kR4, TO_CDT = 3 * kR4 + kR8,
+       TO_CLS = 4 * kR4 + kR8, TO_G0 = 5 * kR4 + kR8, TO_G1 = 6 * kR4 + kR8,
+       TO_G2 = 7 * kR4 + kR8, kTileBufBytes = 8 * kR4 + kR8 };
+
+// Bytes of the bulk copy of elements [o, o + n) of an array (16-byte aligned base): the
+// window rounded out to 16-byte boundaries.
+template <typename X>
+__device__ __forceinline__ uint32_t stage_bytes(int64_t o, int64_t n) {
+  const uint64_t lo = ((uint64_t)o * sizeof(X)) & ~(uint64_t)15;
+  const uint64_t hi = ((uint64_t)(o + n) * sizeof(X) + 15) & ~(uint64_t)15;
+  return (uint32_t)(hi - lo);
+}
+template <typename X>
+__device__ __forceinline__ void stage(unsigned char *dst, const X *a, int64_t o, int64_t n,
+                                      uint64_t *bar) {
+  const uint64_t lo = ((uint64_t)o * sizeof(X)) & ~(uint64_t)15;
+  bulk_load(dst, (const char *)a + lo, stage_bytes<X>(o, n), bar);
+}
+// The shared-memory copy of element o of a staged array.
+template <typename X>
+__device__ __forceinline__ const X *staged(const unsigned char *dst, int64_t o) {
+  return (const X *)(dst + (((uint64_t)o * sizeof(X)) & 15));
+}
+
+struct TileWin {
+  int64_t s, cnt, of, ngax, nf;  // first element, count, F window start, window lengths
+};
+__device__ __forceinline__ TileWin tile_win(int64_t t, int64_t N) {
+  TileWin w;
+  w.s = t * kTileE;
+  w.cnt = N - w.s < kTileE ? N - w.s : kTileE;
+  w.of = w.s > 0 ? w.s - 1 : 0;
+  const int64_t end = w.s + w.cnt + 1 < N ? w.s + w.cnt + 1 : N;  // one past the halo
+  w.nf = end - w.of;
+  w.ngax = end - w.s;
+  return w;
+}
+
+// Thread 0: expect and issue the copies of tile t into buffer `buf`.
+__device__ __forceinline__ void issue_tile(const PackView &p, const float *Fin, const double *Vin,
+                                           int64_t t, unsigned char *buf, uint64_t *bar) {
+  const int64_t N = p.ntot;
+  const TileWin w = tile_win(t, N);
+  uint32_t bytes = stage_bytes<uint32_t>(w.s, w.cnt) + stage_bytes<float>(w.of, w.nf) +
+                   stage_bytes<float>(w.s, w.ngax) + stage_bytes<double>(w.s, w.cnt) +
+                   stage_bytes<float>(w.s, w.cnt);
+  if (p.hp_cls) bytes += stage_bytes<uint32_t>(w.s, w.cnt);
+  if (p.hh_dense)
+    bytes += stage_bytes<float>(w.s, w.cnt) + stage_bytes<float>(N + w.s, w.cnt) +
+             stage_bytes<float>(2 * N + w.s, w.cnt);
+  else
+    bytes += 2 * stage_bytes<float>(w.s, w.cnt);
+  mbar_expect_tx(bar, bytes);
+  stage(buf + TO_FL, p.eflags, w.s, w.cnt, bar);
+  stage(buf + TO_F, Fin, w.of, w.nf, bar);
+  stage(buf + TO_GAX, p.gaxf, w.s, w.ngax, bar);
+  stage(buf + TO_V, Vin, w.s, w.cnt, bar);
+  stage(buf + TO_CDT, p.cdtf, w.s, w.cnt, bar);
+  if (p.hp_cls) stage(buf + TO_CLS, p.hp_cls, w.s, w.cnt, bar);
+  if (p.hh_dense) {
+    stage(buf + TO_G0, p.gatef, w.s, w.cnt, bar);
+    stage(buf + TO_G1, p.gatef, N + w.s, w.cnt, bar);
+    stage(buf + TO_G2, p.gatef, 2 * N + w.s, w.cnt, bar);
+  } else {
+    stage(buf + TO_G0, p.wdxf, w.s, w.cnt, bar);
+    stage(buf + TO_G1, p.kdxf, w.s, w.cnt, bar);
+  }
+}
+
+// One element of a staged tile (the body of explicit_step_mixed<false>).
+__device__ __forceinline__ void tile_element(const PackView &p, int k, int force,
+                                             const unsigned char *buf, const TileWin &w,
+                                             int64_t j, const float *__restrict__ Fin,
+                                             double *__restrict__ Vout,
+                                             float *__restrict__ Fout) {
+  const int64_t N = p.ntot;
+  const int64_t jm = j > 0 ? j - 1 : j, jp = j + 1 < N ? j + 1 : j;
+  const uint32_t fl = staged<uint32_t>(buf + TO_FL, w.s)[j - w.s];
+  const float *sF = staged<float>(buf + TO_F, w.of) - w.of;     // sF[q] = Fin[q]
+  const float *sG = staged<float>(buf + TO_GAX, w.s) - w.s;     // sG[q] = gaxf[q]
+  const float f0 = sF[j], fm = sF[jm], fp = sF[jp];
+  const float g0 = sG[j], gp = sG[jp];
+  const double v64 = staged<double>(buf + TO_V, w.s)[j - w.s];
+  const float cdt = staged<float>(buf + TO_CDT, w.s)[j - w.s];
+  const uint32_t cls = p.hp_cls ? staged<uint32_t>(buf + TO_CLS, w.s)[j - w.s] : 0u;
+  Topo tj;
+  if (fl & F_XTOPO) {
+    tj = p.topo[j];
+  } else {
+    tj.mother = (int32_t)jm;
+    tj.dr = (int32_t)jp;
+    tj.dl = (int32_t)j;
+    tj.flags = fl;
+  }
+  const uint32_t inst = tj.flags >> INST_SHIFT;
+  const InstDev in = p.inst[inst];
+  const int64_t i = in.base + k;
+  if (i >= in.iend) {
+    Vout[j] = v64;
+    Fout[j] = f0;
+    return;
+  }
+  const bool term = (tj.flags & F_TERM) != 0;
+  if (term && !(tj.flags & F_HH)) return;
+  const int64_t self = term ? ghost_source(tj, j) : j;
+  const float vf = self == j ? f0 : (self == jm ? fm : (self == jp ? fp : Fin[self]));
+  float wdx, kdx;
+  if (tj.flags & F_HH) {
+    float m0, h0, n0;
+    if (p.hh_dense) {
+      m0 = staged<float>(buf + TO_G0, w.s)[j - w.s];
+      h0 = staged<float>(buf + TO_G1, N + w.s)[j - w.s];
+      n0 = staged<float>(buf + TO_G2, 2 * N + w.s)[j - w.s];
+    } else {
+      m0 = p.gatef[j];
+      h0 = p.gatef[N + j];
+      n0 = p.gatef[2 * N + j];
+    }
+    const int64_t L = p.hp_ld;
+    const float *hp = p.hpf + (p.hp_cls ? (int64_t)cls : (p.hp_inst ? (int64_t)inst : j));
+    const float dv = vf - hp[HP_REST * L];
+    GateStep32 g = hh_step32(dv + hp[HP_LSNA * L], dv + hp[HP_LSK * L], m0, h0, n0,
+                             hp[HP_DTMS * L], hp[HP_GNA * L], hp[HP_GK * L], hp[HP_GL * L],
+                             hp[HP_ENA * L], hp[HP_EK * L], hp[HP_EL * L]);
+    p.gatef[j] = g.m;
+    p.gatef[N + j] = g.h;
+    p.gatef[2 * N + j] = g.n;
+    if (term) return;
+    const float dx = hp[HP_DX * L];
+    wdx = g.W * dx;
+    kdx = g.K * dx;
+  } else if (p.hh_dense) {
+    wdx = p.wdxf[j];
+    kdx = p.kdxf[j];
+  } else {
+    wdx = staged<float>(buf + TO_G0, w.s)[j - w.s];
+    kdx = staged<float>(buf + TO_G1, w.s)[j - w.s];
+  }
+  const bool active = input_on(in, i, force);
+  float acc = 0.0f;
+  if ((tj.flags & F_BRANCH) && !(tj.flags & F_DL_TERM))
+    acc = (Fin[tj.dl] - vf) * p.gaxf[tj.dl];
+  if (!(tj.flags & F_DR_TERM)) {
+    const bool adj = tj.dr == jp && jp != j;
+    const float fd = adj ? fp : Fin[tj.dr], gd = adj ? gp : p.gaxf[tj.dr];
+    acc = fmaf(fd - vf, gd, acc);
+  }
+  if (!(tj.flags & F_MO_TERM)) {
+    const float fo = (tj.mother == jm && jm != j) ? fm : Fin[tj.mother];
+    acc = fmaf(fo - vf, g0, acc);
+  }
+  acc = fmaf(wdx, vf, acc) + kdx;
+  if (active && (tj.flags & F_INP)) acc += p.inpf[j];
+  const double vn = v64 + (double)(cdt * acc);
+  Vout[j] = vn;
+  Fout[j] = (float)vn;
+}
+
+__global__ void __launch_bounds__(kTileThreads) explicit_step_mixed_tiled(
+    PackView p, int k, int force, const double *__restrict__ Vin, double *__restrict__ Vout,
+    const float *__restrict__ Fin, float *__restrict__ Fout) {
+  extern __shared__ __align__(16) unsigned char tsm[];
+  uint64_t *bar = (uint64_t *)(tsm + 2 * kTileBufBytes);
+  const int64_t N = p.ntot;
+  const int64_t ntiles = (N + kTileE - 1) / kTileE;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_proxy_async();
+  }
+  __syncthreads();
+  int64_t t = blockIdx.x;
+  if (t < ntiles && threadIdx.x == 0) issue_tile(p, Fin, Vin, t, tsm, &bar[0]);
+  uint32_t phase0 = 0, phase1 = 0;
+  int b = 0;
+  for (; t < ntiles; t += gridDim.x) {
+    const int64_t tn = t + gridDim.x;
+    unsigned char *buf = tsm + b * kTileBufBytes;
+    if (tn < ntiles && threadIdx.x == 0) {
+      fence_proxy_async();  // the other buffer's reads (last iteration) before its refill
+      issue_tile(p, Fin, Vin, tn, tsm + (b ^ 1) * kTileBufBytes, &bar[b ^ 1]);
+    }
+    const uint32_t ph = b ? phase1 : phase0;
+    const bool ok = mbar_wait_ok(&bar[b], ph, p.err);
+    if (__syncthreads_or(!ok)) {
+      // a copy never landed (a device fault): wait, bounded, for what is still in flight
+      if (threadIdx.x == 0) {
+        mbar_wait_ok(&bar[b], ph, p.err);
+        if (tn < ntiles) mbar_wait_ok(&bar[b ^ 1], b ? phase0 : phase1, p.err);
+      }
+      __syncthreads();
+      return;
+    }
+    if (b) phase1 ^= 1; else phase0 ^= 1;
+    const TileWin w = tile_win(t, N);
+#pragma unroll
+    for (int u = 0; u < kTileE / kTileThreads; u++) {
+      const int64_t l = threadIdx.x + u * kTileThreads;
+      if (l < w.cnt) tile_element(p, k, force, buf, w, w.s + l, Fin, Vout, Fout);
+    }
+    __syncthreads();  // this buffer's reads done before it is refilled
+    b ^= 1;
+  }
+}
+
 // V_t = V_source(t) for every terminal (src/solverEx-cpu.cpp:155-161).
 __global__ void terminal_fixup(const Topo *__restrict__ topo, const int64_t *__restrict__ terms,
                                int64_t nterm, double *__restrict__ V, float *__restrict__ Vf) {
@@ -222,7 +445,10 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
   while (threads > 32 && pv.ntot < (int64_t)threads * 2 * 152) threads >>= 1;
   const unsigned blocks = (unsigned)((pv.ntot + threads - 1) / threads);
   if (precision == NRT_MIXED) {
-    if (general)
+    if (!general && pv.tile_blocks > 0 && pv.eflags && pv.err) {
+      explicit_step_mixed_tiled<<<pv.tile_blocks, kTileThreads, 2 * kTileBufBytes + 16, st>>>(
+          pv, k, force, Vin, Vout, Fin, Fout);
+    } else if (general)
       explicit_step_mixed<true><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout, Fin, Fout);
     else
       explicit_step_mixed<false><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout, Fin, Fout);
@@ -234,6 +460,20 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
   }
   NRT_CUDA(cudaGetLastError());
   return NRT_OK;
+}
+
+// Persistent CTAs for the tiled mixed step on this device (0 if it cannot run).
+int explicit_tile_blocks(int device, int64_t ntot) {
+  int sms = 0, per_sm = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, explicit_step_mixed_tiled,
+                                                    kTileThreads, 2 * kTileBufBytes + 16) !=
+          cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  const int64_t ntiles = (ntot + kTileE - 1) / kTileE;
+  return (int)std::min<int64_t>((int64_t)sms * per_sm, ntiles);
 }
 
 int launch_terminal_fixup(const Topo *topo, const int64_t *terms, int64_t nterm, double *V,

@@ -52,6 +52,7 @@
 #include "hh.cuh"
 #include "nrt_solver.h"
 #include "record.cuh"
+#include "tma.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -339,54 +340,7 @@ __device__ __forceinline__ void level_sync(cg::grid_group &grid) {
 
 enum : uint8_t { SL_FIRST = 1, SL_LAST = 2, SL_PAD = 4 };  // slot flags (ImView::sflag)
 
-// ---- bulk (TMA) copies global -> shared, completed on an mbarrier
-__device__ __forceinline__ uint32_t smem_addr(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(phase)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
-}
-// Orders this thread's earlier generic-proxy accesses before later bulk (async-proxy) ones.
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async;" ::: "memory");
-}
-
-// Waits for phase `phase` of the tile barrier; gives up after about two seconds of
-// clock (the copies it waits for are in bounds and always land, so giving up means a
-// device fault), raising the error word the host checks.
-__device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t phase, int *err) {
-  if (mbar_try_wait(bar, phase)) return;
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, phase)) {
-    if (clock64() - t0 > 4000000000ll) {
-      atomicOr(err, 1);
-      return;
-    }
-  }
-}
+// bulk (TMA) copies, mbarriers and the bounded wait: tma.cuh
 
 // Shared-memory tile of the tree preconditioner: three T rows, the slot flags and the
 // slot rows, `cap` slots each.
@@ -2179,14 +2133,17 @@ int pass_counts(Engine &e, int64_t *residuals, int64_t *applies, int64_t *xupdat
   return NRT_OK;
 }
 
-// NRT_EDEVICE when a kernel's bounded wait gave up (the error word is set); synchronises.
+// NRT_EDEVICE when a kernel's bounded wait gave up (an error word is set); synchronises.
 int implicit_check(Engine &e) {
-  if (!e.im) return NRT_OK;
-  int err = 0;
-  NRT_CUDA(cudaMemcpyAsync(&err, e.im->iv.err, sizeof(int), cudaMemcpyDeviceToHost, e.stream));
+  int err[2] = {0, 0};
+  if (e.im)
+    NRT_CUDA(cudaMemcpyAsync(&err[0], e.im->iv.err, sizeof(int), cudaMemcpyDeviceToHost, e.stream));
+  if (e.pv.err)
+    NRT_CUDA(cudaMemcpyAsync(&err[1], e.pv.err, sizeof(int), cudaMemcpyDeviceToHost, e.stream));
   NRT_CUDA(cudaStreamSynchronize(e.stream));
-  if (err) {
-    set_error("implicit kernel: a bounded wait for its tile copies expired");
+  if (err[0] || err[1]) {
+    set_error(err[0] ? "implicit kernel: a bounded wait for its tile copies expired"
+                     : "explicit step: a bounded wait for its tile copies expired");
     return NRT_EDEVICE;
   }
   return NRT_OK;

@@ -111,7 +111,10 @@ typedef struct nrt_options {
   int32_t use_graphs;            /* capture nrt_run time loops in CUDA graphs (default 1) */
   int32_t schedule;              /* implicit: 0 = auto (one tree -> cooperative whole-GPU
                                     launch), 1 = always block per instance */
-  int32_t reserved[6];
+  int32_t tiled;                 /* mixed explicit: 1 (default) = element arrays staged into
+                                    shared memory by bulk copies, tile by tile; 0 = one
+                                    thread per element loading its own (same results) */
+  int32_t reserved[5];
 } nrt_options;
 
 typedef struct nrt_stats {

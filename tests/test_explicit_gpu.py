@@ -148,3 +148,32 @@ def test_large_tree_against_oracle(gpu, pkg, orc, model):
     s = pkg.SolverEx(pkg.ProblemArrays.from_spec(spec, dp, dT))
     s.run(1, 1 + steps, spec.init_time, spec.end_input)
     assert np.abs(s.snapshot() - Vo).max() < TOL_FP64
+
+
+@pytest.mark.parametrize("count,hh", [(7, True), (3, False)])
+def test_tiled_mixed_step_equals_untiled(gpu, pkg, model, count, hh):
+    """The TMA-tiled mixed step (bulk-copied element arrays, persistent CTAs) gives bit for
+    bit what the one-thread-per-element step gives: uneven trees whose total is no multiple
+    of the tile or of 16 bytes, runs that end at different steps, a stimulus window, and
+    mostly-passive trees (W dX, K dX staged instead of the gates)."""
+    specs = [model.random_tree(seed=70 + q, n_target=700 + 1371 * q, tspan=1e-3)
+             for q in range(count)]
+    if not hh:
+        specs = [model.myelinated_axon(n_nodes=12 + 5 * q, internode_len=120e-6, dx=2e-6,
+                                       node_len=2e-6, tspan=1e-3, dtf=0.8) for q in range(count)]
+    probs = []
+    for sp in specs:
+        d = pkg.derive(sp)
+        probs.append(pkg.ProblemArrays.from_spec(sp, d, 0.8 * d.dT_crit))
+    runs = [(1, 1 + 150 + 37 * q, sp.init_time, sp.end_input) for q, sp in enumerate(specs)]
+    out = []
+    for tiled in (True, False):
+        b = pkg.Batch(probs, mode=0, precision="mixed", tiled=tiled)
+        b.set_runs(runs)
+        b.advance(300)
+        out.append([b.get_state(q) for q in range(count)])
+        b.close()
+    for a, c in zip(*out):
+        np.testing.assert_array_equal(a.V, c.V)
+        np.testing.assert_array_equal(a.m, c.m)
+        np.testing.assert_array_equal(a.n, c.n)
