@@ -375,7 +375,7 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   if (!host.hp_cls.empty()) bytes += al(4 * N);
   if (mixed && opt.mode == NRT_EXPLICIT) bytes += al(4 * N);  // flags of the compact step
   if (mixed)
-    bytes += 7 * al(4 * N) + al(4 * 3 * N) + al(4 * hpn);
+    bytes += 7 * al(4 * N) + al(4 * 3 * N) + al(4 * 12 * (size_t)host.hp_ld);
   else
     bytes += 5 * al(8 * N) + al(8 * 3 * N) + al(8 * hpn);
   if (opt.mode == NRT_IMPLICIT_BE) {
@@ -447,7 +447,16 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
     TRY(upload(arena, p, f32(host.kdx), N, st)); pv.kdxf = p;
     TRY(upload(arena, p, f32(host.inp), N, st)); pv.inpf = p;
     TRY(upload(arena, p, f32(host.gate), 3 * N, st)); pv.gatef = p;
-    TRY(upload(arena, p, f32(host.hp), hpn, st)); pv.hpf = p;
+    {  // the parameter table by column: 12 floats (HP_* rows and a pad) per column
+      const int64_t L = host.hp_ld;
+      hostf.emplace_back((size_t)12 * L, 0.0f);
+      float *q = hostf.back().data();
+      for (int64_t c = 0; c < L; c++)
+        for (int r = 0; r < HP_ROWS; r++) q[12 * c + r] = (float)host.hp[(size_t)r * L + c];
+      float4 *dq = nullptr;
+      TRY(upload(arena, dq, (const float4 *)q, 3 * (size_t)L, st));
+      pv.hpq = dq;
+    }
   } else {
     double *p;
     TRY(upload(arena, p, host.cdt.data(), N, st)); pv.cdt = p;

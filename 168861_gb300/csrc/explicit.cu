@@ -159,17 +159,17 @@ __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, in
       h0 = p.gatef[N + j];
       n0 = p.gatef[2 * N + j];
     }
-    const int64_t L = p.hp_ld;
-    const float *hp = p.hpf + (p.hp_cls ? (int64_t)cls : (p.hp_inst ? (int64_t)inst : j));
-    const float dv = vf - hp[HP_REST * L];
-    GateStep32 g = hh_step32(dv + hp[HP_LSNA * L], dv + hp[HP_LSK * L], m0, h0, n0,
-                             hp[HP_DTMS * L], hp[HP_GNA * L], hp[HP_GK * L], hp[HP_GL * L],
-                             hp[HP_ENA * L], hp[HP_EK * L], hp[HP_EL * L]);
+    const HHParams32 q =
+        hh_params32(p.hpq, p.hp_cls ? (int64_t)cls : (p.hp_inst ? (int64_t)inst : j));
+    const float dv = vf - q.v[HP_REST];
+    GateStep32 g = hh_step32(dv + q.v[HP_LSNA], dv + q.v[HP_LSK], m0, h0, n0, q.v[HP_DTMS],
+                             q.v[HP_GNA], q.v[HP_GK], q.v[HP_GL], q.v[HP_ENA], q.v[HP_EK],
+                             q.v[HP_EL]);
     p.gatef[j] = g.m;
     p.gatef[N + j] = g.h;
     p.gatef[2 * N + j] = g.n;
     if (term) return;
-    const float dx = hp[HP_DX * L];
+    const float dx = q.v[HP_DX];
     wdx = g.W * dx;
     kdx = g.K * dx;
   } else {
@@ -329,17 +329,17 @@ __device__ __forceinline__ void tile_element(const PackView &p, int k, int force
       h0 = p.gatef[N + j];
       n0 = p.gatef[2 * N + j];
     }
-    const int64_t L = p.hp_ld;
-    const float *hp = p.hpf + (p.hp_cls ? (int64_t)cls : (p.hp_inst ? (int64_t)inst : j));
-    const float dv = vf - hp[HP_REST * L];
-    GateStep32 g = hh_step32(dv + hp[HP_LSNA * L], dv + hp[HP_LSK * L], m0, h0, n0,
-                             hp[HP_DTMS * L], hp[HP_GNA * L], hp[HP_GK * L], hp[HP_GL * L],
-                             hp[HP_ENA * L], hp[HP_EK * L], hp[HP_EL * L]);
+    const HHParams32 q =
+        hh_params32(p.hpq, p.hp_cls ? (int64_t)cls : (p.hp_inst ? (int64_t)inst : j));
+    const float dv = vf - q.v[HP_REST];
+    GateStep32 g = hh_step32(dv + q.v[HP_LSNA], dv + q.v[HP_LSK], m0, h0, n0, q.v[HP_DTMS],
+                             q.v[HP_GNA], q.v[HP_GK], q.v[HP_GL], q.v[HP_ENA], q.v[HP_EK],
+                             q.v[HP_EL]);
     p.gatef[j] = g.m;
     p.gatef[N + j] = g.h;
     p.gatef[2 * N + j] = g.n;
     if (term) return;
-    const float dx = hp[HP_DX * L];
+    const float dx = q.v[HP_DX];
     wdx = g.W * dx;
     kdx = g.K * dx;
   } else if (p.hh_dense) {

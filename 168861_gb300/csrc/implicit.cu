@@ -107,7 +107,6 @@ struct ImView {
   const float *gf;
   const double *wdx64, *kdx64, *inp64;
   double *diag;
-  float *diagf;
   double *rhs;
   void *Wb, *Z, *yv, *pcd, *pcc;  // T-typed workspace
   const int2 *pieces;             // (first row, length) of every segment piece
@@ -124,7 +123,7 @@ struct ImView {
   // exact tree preconditioner (NRT_PRECOND_TREE).  Segments in tile order; per-slot
   // arrays in slot order (slots: the rows of a worker's segments, level by level, deepest
   // level first; every tile starts on a multiple of 16 slots, padding slots have row -1).
-  void *cdiag;                    // T[ntot]: c_j, written by the assembly
+  void *cdiag;                    // T[ntot]: c_j = c_m dX / dT - W dX, written by the assembly
   const int *seg_len, *seg_c1, *seg_c2, *seg_prow, *seg_soff;
   const int *tile_seg;            // segments of tree tile q: [tile_seg[q], tile_seg[q+1])
   const int *tile_slot;           // slots of tree tile q: [tile_slot[q], tile_slot[q+1])
@@ -288,6 +287,57 @@ __device__ __forceinline__ void apply_rows(const PackView &pv, const ImView &iv,
       if (f & R_UP) s -= gm[u] * mo;
       if (f & R_DOWNR) s -= gp[u] * xp[u];
       if (f & R_DOWNL) s -= gl * xl;
+    }
+    out[u] = s;
+  }
+}
+
+// (A x)_r in the difference form c_r x_r + sum over the row's neighbours q of
+// g_q (x_r - x_q): the same product as apply_rows (the diagonal is c_r plus the row's
+// conductances), without its cancellation.  For the smooth vectors of a stiff cable,
+// d_r x_r and g x_q are each ~g/c times larger than their difference, so the diagonal
+// form loses that factor of precision in FP32; here each difference of neighbouring
+// values is formed first (exactly, when they are within a factor of two).
+template <int kN, typename C, typename X>
+__device__ __forceinline__ void apply_rows_c(const PackView &pv, const ImView &iv,
+                                             const C *__restrict__ Cc, const C *__restrict__ G,
+                                             const X *x, int64_t rb, int64_t stride, int64_t r1,
+                                             X (&out)[kN], uint8_t (&fl)[kN]) {
+  const int64_t N = pv.ntot;
+  C cc[kN], gm[kN], gp[kN];
+  X xs[kN], xm[kN], xp[kN];
+#pragma unroll
+  for (int u = 0; u < kN; u++) {
+    const int64_t r = rb + u * stride;
+    const bool ok = r < r1;
+    const int64_t rm = r > 0 ? r - 1 : r, rp = r + 1 < N ? r + 1 : r;
+    fl[u] = ok ? iv.rowf[r] : (uint8_t)R_IDENT;
+    cc[u] = ok ? Cc[r] : (C)0;
+    gm[u] = ok ? G[r] : (C)0;
+    gp[u] = ok ? G[rp] : (C)0;
+    xs[u] = ok ? x[r] : (X)0;
+    xm[u] = ok ? x[rm] : (X)0;
+    xp[u] = ok ? x[rp] : (X)0;
+  }
+#pragma unroll
+  for (int u = 0; u < kN; u++) {
+    const uint8_t f = fl[u];
+    X s = 0;
+    if (!(f & R_IDENT)) {
+      X mo = xm[u], xl = 0;
+      C gl = 0;
+      if (f & (R_FAR | R_DOWNL)) {
+        const Topo t = pv.topo[rb + u * stride];
+        if (f & R_FAR) mo = x[t.mother];
+        if (f & R_DOWNL) {
+          gl = G[t.dl];
+          xl = x[t.dl];
+        }
+      }
+      s = cc[u] * xs[u];
+      if (f & R_UP) s += gm[u] * (xs[u] - mo);
+      if (f & R_DOWNR) s += gp[u] * (xs[u] - xp[u]);
+      if (f & R_DOWNL) s += gl * (xs[u] - xl);
     }
     out[u] = s;
   }
@@ -901,16 +951,15 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
           g2[u] = gate[2 * N + r];
         }
         if (sizeof(T) == 4) {
-          const float *hp = pv.hpf + hc[u];
-          const float dv = (float)(v[u] - (double)hp[HP_REST * L]);
-          GateStep32 g = hh_step32(dv + hp[HP_LSNA * L], dv + hp[HP_LSK * L], (float)g0[u],
-                                   (float)g1[u], (float)g2[u], hp[HP_DTMS * L],
-                                   hp[HP_GNA * L], hp[HP_GK * L], hp[HP_GL * L],
-                                   hp[HP_ENA * L], hp[HP_EK * L], hp[HP_EL * L]);
+          const HHParams32 q = hh_params32(pv.hpq, hc[u]);
+          const float dv = (float)(v[u] - (double)q.v[HP_REST]);
+          GateStep32 g = hh_step32(dv + q.v[HP_LSNA], dv + q.v[HP_LSK], (float)g0[u],
+                                   (float)g1[u], (float)g2[u], q.v[HP_DTMS], q.v[HP_GNA],
+                                   q.v[HP_GK], q.v[HP_GL], q.v[HP_ENA], q.v[HP_EK], q.v[HP_EL]);
           gate[r] = (T)g.m;
           gate[N + r] = (T)g.h;
           gate[2 * N + r] = (T)g.n;
-          const float dx = hp[HP_DX * L];
+          const float dx = q.v[HP_DX];
           wdx = (double)(g.W * dx);  // FP32 inputs: the product in FP32 loses nothing
           kdx = (double)(g.K * dx);
         } else {
@@ -950,8 +999,7 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
       if (f[u] & R_DOWNR) d += gn[u];
       if (f[u] & R_UP) d += gj[u];
       iv.diag[r] = d;
-      if (iv.diagf) iv.diagf[r] = (float)d;
-      if (cdiag) cdiag[r] = (T)cj;
+      cdiag[r] = (T)cj;
       if (active && (f[u] & R_INP)) inp[u] = iv.inp64[r];  // one row or a few per tree
       double b = cm[u] * v[u] + kdx;
       if (active) b += inp[u];
@@ -1017,7 +1065,7 @@ __device__ __noinline__ DotAcc<T> ph_spmv(Ctx<T, kGrid> c, int j, T sj, int g1) 
   const PackView &pv = *c.pv;
   const ImView &iv = *c.iv;
   const int64_t N = pv.ntot, stride = blockDim.x;
-  const T *DT = sizeof(T) == 4 ? (const T *)(const void *)iv.diagf : (const T *)(const void *)iv.diag;
+  const T *CT = (const T *)iv.cdiag;
   const T *GT = sizeof(T) == 4 ? (const T *)(const void *)iv.gf : (const T *)(const void *)iv.g64;
   const T *Zj = c.w.Z + (size_t)j * N;
   DotAcc<T> acc;
@@ -1026,7 +1074,7 @@ __device__ __noinline__ DotAcc<T> ph_spmv(Ctx<T, kGrid> c, int j, T sj, int g1) 
   for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kU * stride) {
     T y[kU];
     uint8_t fl[kU];
-    apply_rows<kU>(pv, iv, DT, GT, Zj, rb, stride, c.r1, y, fl);
+    apply_rows_c<kU>(pv, iv, CT, GT, Zj, rb, stride, c.r1, y, fl);
 #pragma unroll
     for (int u = 0; u < kU; u++) {
       const int64_t r = rb + u * stride;
@@ -1187,7 +1235,7 @@ __device__ __noinline__ DotAcc<T> ph_matvec(Ctx<T, kGrid> c, const T *x, T *out,
   const PackView &pv = *c.pv;
   const ImView &iv = *c.iv;
   const int64_t stride = blockDim.x;
-  const T *DT = sizeof(T) == 4 ? (const T *)(const void *)iv.diagf : (const T *)(const void *)iv.diag;
+  const T *CT = (const T *)iv.cdiag;
   const T *GT = sizeof(T) == 4 ? (const T *)(const void *)iv.gf : (const T *)(const void *)iv.g64;
   DotAcc<T> acc;
 #pragma unroll
@@ -1201,7 +1249,7 @@ __device__ __noinline__ DotAcc<T> ph_matvec(Ctx<T, kGrid> c, const T *x, T *out,
       e0[u] = q < c.r1 ? d0[q] : (T)0;
       e1[u] = q < c.r1 && d1 ? d1[q] : (T)0;
     }
-    apply_rows<kU>(pv, iv, DT, GT, x, rb, stride, c.r1, y, fl);
+    apply_rows_c<kU>(pv, iv, CT, GT, x, rb, stride, c.r1, y, fl);
 #pragma unroll
     for (int u = 0; u < kU; u++) {
       const int64_t q = rb + u * stride;
@@ -1899,7 +1947,7 @@ int Engine::implicit_plan(size_t &bytes) {
   b += al256(N);                                            // rowf
   b += 5 * al256(8 * N);                                    // cmdt, g64, wdx64, kdx64, inp64
   b += 2 * al256(8 * N);                                    // diag, rhs
-  b += al256(4 * N) + (mixed ? al256(4 * N) : 0);           // gf, diagf
+  b += al256(4 * N) + al256(tb * N);                        // gf, cdiag
   b += 2 * al256(tb * N * (m + 1)) + 3 * al256(tb * N);     // Wb, Z, y, pd, pc
   b += al256(sizeof(int2) * std::max<size_t>(1, S.pieces.size()));
   b += al256(4 * S.tiles.size());
@@ -1912,7 +1960,6 @@ int Engine::implicit_plan(size_t &bytes) {
   if (tree) {
     const TreeSchedule &T = S.tree;
     const size_t ns = T.slot_row.size(), nseg = std::max<size_t>(1, T.seg_len.size());
-    b += al256(tb * N);                                     // cdiag
     b += 5 * al256(4 * nseg);                               // seg_len, c1, c2, prow, soff
     b += al256(4 * T.tile_seg.size()) + al256(4 * T.tile_slot.size()) + al256(4 * ns) + al256(ns);
     b += al256(4 * T.lev_tile.size()) + al256(4 * T.work_lev.size());
@@ -1966,8 +2013,11 @@ int Engine::implicit_init() {
   TRYI(up(arena, iv.rhs, (const double *)nullptr, N, st));
   float *pf;
   TRYI(up(arena, pf, gf.data(), N, st)); iv.gf = pf;
-  iv.diagf = nullptr;
-  if (mixed) TRYI(up(arena, iv.diagf, (const float *)nullptr, N, st));
+  iv.cdiag = arena.take(tb * N);
+  if (!iv.cdiag) {
+    set_error("arena exhausted");
+    return NRT_ENOMEM;
+  }
   const int m = opt.restart;
   iv.Wb = arena.take(tb * N * (m + 1));
   iv.Z = arena.take(tb * N * (m + 1));
@@ -2001,12 +2051,10 @@ int Engine::implicit_init() {
   std::vector<InstStat> zero(ni, InstStat{0, 0, 0, 0.0, 0, 0, 0, 0});
   TRYI(up(arena, iv.stats, zero.data(), ni, st));
   iv.work_lev = nullptr;
-  iv.cdiag = nullptr;
   std::vector<char> sgbuf;
   if (opt.precond == NRT_PRECOND_TREE) {
     const TreeSchedule &T = S.tree;
     const size_t ns = T.slot_row.size(), nseg = std::max<size_t>(1, T.seg_len.size());
-    iv.cdiag = arena.take(tb * N);
     TRYI(up(arena, pi, T.seg_len.data(), T.seg_len.size(), st)); iv.seg_len = pi;
     TRYI(up(arena, pi, T.seg_c1.data(), T.seg_c1.size(), st)); iv.seg_c1 = pi;
     TRYI(up(arena, pi, T.seg_c2.data(), T.seg_c2.size(), st)); iv.seg_c2 = pi;

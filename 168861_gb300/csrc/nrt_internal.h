@@ -40,7 +40,8 @@ struct __align__(16) Topo {
   uint32_t flags;   // F_* | instance << INST_SHIFT
 };
 
-// HH parameters, SoA rows of Pack::hp (FP64) / Pack::hpf (FP32).  Columns: one per
+// HH parameters, SoA rows of Pack::hp (FP64); the mixed path keeps each column's rows
+// together as 12 floats (three 16-byte loads, PackView::hpq).  Columns: one per
 // instance when every HH element of an instance has the same parameters; else one per
 // distinct parameter set ("class", indexed through hp_cls) when there are few of them;
 // else one per element.
@@ -119,7 +120,7 @@ struct PackView {
   double *gate;        // [3][ntot] m, h, n (FP64 path)
   float *gatef;        // [3][ntot] (mixed path)
   const double *hp;    // [HP_ROWS][hp_ld]
-  const float *hpf;    // [HP_ROWS][hp_ld]
+  const float4 *hpq;   // mixed: [hp_ld][3], one column's HP_* rows as 12 floats (11 + pad)
   int64_t hp_ld;       // number of columns
   int hp_inst;         // 1: column = instance
   const uint32_t *hp_cls;  // column per element (class tables), or null
@@ -189,6 +190,20 @@ struct HostPack {
 };
 
 int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp);
+
+// One column of the FP32 parameter table (three vector loads).
+struct HHParams32 {
+  float v[12];  // indexed by HP_*
+};
+__device__ __forceinline__ HHParams32 hh_params32(const float4 *hpq, int64_t col) {
+  const float4 *q = hpq + 3 * col;
+  const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+  HHParams32 r;
+  r.v[0] = a.x; r.v[1] = a.y; r.v[2] = a.z; r.v[3] = a.w;
+  r.v[4] = b.x; r.v[5] = b.y; r.v[6] = b.z; r.v[7] = b.w;
+  r.v[8] = c.x; r.v[9] = c.y; r.v[10] = c.z; r.v[11] = c.w;
+  return r;
+}
 
 // Column of the HH parameter tables for element j of instance `inst`.
 __host__ __device__ inline int64_t hp_col(const PackView &p, int64_t j, uint32_t inst) {
