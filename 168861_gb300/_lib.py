@@ -91,7 +91,7 @@ EXPORTS = (
     "nrt_server_get_stats", "nrt_server_destroy", "nrt_solve_csr_static",
     "nrt_measurement_point", "nrt_record", "nrt_batch_record", "nrt_record_read",
     "nrt_batch_record_read", "nrt_batch_pass_counts", "nrt_get_state", "nrt_set_state",
-    "nrt_batch_get_state", "nrt_batch_set_state",
+    "nrt_batch_get_state", "nrt_batch_set_state", "nrt_batch_snapshot_all",
 )
 
 _lib = None
@@ -130,6 +130,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "nrt_batch_advance": [vp, ctypes.c_int64],
         "nrt_batch_synchronize": [vp],
         "nrt_batch_snapshot": [vp, ctypes.c_int32, _f64p],
+        "nrt_batch_snapshot_all": [vp, _f64p],
         "nrt_batch_remaining": [vp, _i64p],
         "nrt_batch_get_stats": [vp, ctypes.POINTER(Stats)],
         "nrt_batch_destroy": [vp],

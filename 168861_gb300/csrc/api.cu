@@ -934,6 +934,18 @@ int nrt_batch_snapshot(nrt_batch *b, int32_t instance, double *potential) {
   return nrt::implicit_check(e);
 }
 
+int nrt_batch_snapshot_all(nrt_batch *b, double *potential) {
+  if (!b || !potential) return nrt::fail(NRT_EINVAL, "null argument");
+  nrt::Engine &e = b->eng;
+  NRT_CUDA(cudaSetDevice(e.device));
+  int rc = e.fixup();
+  if (rc) return rc;
+  NRT_CUDA(cudaMemcpyAsync(potential, e.V[e.cur], sizeof(double) * e.host.ntot,
+                           cudaMemcpyDeviceToHost, e.stream));
+  NRT_CUDA(cudaStreamSynchronize(e.stream));
+  return nrt::implicit_check(e);
+}
+
 int nrt_batch_remaining(nrt_batch *b, int64_t *remaining) {
   if (!b || !remaining) return nrt::fail(NRT_EINVAL, "null argument");
   nrt::Engine &e = b->eng;

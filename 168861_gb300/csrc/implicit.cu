@@ -47,6 +47,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <memory>
 #include <vector>
 
 #include "hh.cuh"
@@ -1793,6 +1794,138 @@ static void build_tree_schedule(const HostPack &host, int cap, bool grid_mode, i
   }
 }
 
+// The same schedule for a batch (one worker per instance), built per instance on all host
+// cores and concatenated: every instance's slots are padded to a multiple of 16, which is
+// where the sequential builder's next tile would start, so the result is the same.
+struct InstSchedule {
+  std::vector<int> seg_len, seg_c1, seg_c2, seg_prow, seg_soff, tile_seg, tile_slot, slot_row,
+      lev_tile;
+  std::vector<uint8_t> slot_flag;
+};
+
+static void instance_schedule(const HostPack &host, int cap, int32_t i, InstSchedule &L) {
+  struct Seg {
+    int start, len, prow, parent, level, c1, c2;
+  };
+  const int64_t o = host.off[i], n = host.num_elem[i];
+  std::vector<Seg> segs;
+  std::vector<int> seg_of(n, -1);
+  int cur = -1;
+  for (int64_t jl = 0; jl < n; jl++) {
+    const int64_t j = o + jl;
+    const Topo &t = host.topo[j];
+    if (t.flags & F_IDENT) {
+      cur = -1;
+      continue;
+    }
+    const bool linked = cur >= 0 && (t.flags & F_UP) && t.mother == j - 1 &&
+                        !(host.topo[j - 1].flags & F_BRANCH) && segs[cur].len < cap;
+    if (linked) {
+      segs[cur].len++;
+    } else {
+      Seg s;
+      s.start = (int)j;
+      s.len = 1;
+      s.prow = (t.flags & F_UP) ? t.mother : -1;
+      s.parent = s.prow >= 0 ? seg_of[s.prow - o] : -1;
+      s.level = s.parent >= 0 ? segs[s.parent].level + 1 : 0;
+      s.c1 = s.c2 = -1;
+      segs.push_back(s);
+      cur = (int)segs.size() - 1;
+      if (s.parent >= 0) {
+        Seg &p = segs[s.parent];
+        (p.c1 < 0 ? p.c1 : p.c2) = cur;
+      }
+    }
+    seg_of[jl] = cur;
+  }
+  int ml = 0;
+  for (const Seg &s : segs) ml = std::max(ml, s.level);
+  std::vector<std::vector<int>> lists(segs.empty() ? 0 : ml + 1);
+  for (int s = 0; s < (int)segs.size(); s++) lists[segs[s].level].push_back(s);
+  std::vector<int> newid(segs.size(), -1), order;
+  auto pad = [&]() {
+    L.slot_row.push_back(-1);
+    L.slot_flag.push_back(SL_PAD | SL_FIRST | SL_LAST);
+  };
+  for (int lv = (int)lists.size() - 1; lv >= 0; lv--) {
+    L.lev_tile.push_back((int)L.tile_seg.size());
+    int used = cap;
+    for (int s : lists[lv]) {
+      if (used + segs[s].len > cap) {
+        while (L.slot_row.size() & 15) pad();
+        L.tile_seg.push_back((int)order.size());
+        L.tile_slot.push_back((int)L.slot_row.size());
+        used = 0;
+      }
+      newid[s] = (int)order.size();
+      order.push_back(s);
+      L.seg_soff.push_back(used);
+      for (int q = 0; q < segs[s].len; q++) {
+        L.slot_row.push_back(segs[s].start + q);
+        L.slot_flag.push_back((q == 0 ? SL_FIRST : 0) | (q == segs[s].len - 1 ? SL_LAST : 0));
+      }
+      used += segs[s].len;
+    }
+  }
+  while (L.slot_row.size() & 15) pad();
+  for (int s : order) {
+    const Seg &g = segs[s];
+    L.seg_len.push_back(g.len);
+    L.seg_prow.push_back(g.prow);
+    L.seg_c1.push_back(g.c1 >= 0 ? newid[g.c1] : -1);
+    L.seg_c2.push_back(g.c2 >= 0 ? newid[g.c2] : -1);
+  }
+}
+
+static void build_tree_schedule_batch(const HostPack &host, int cap, TreeSchedule &T) {
+  const int32_t ni = host.ninst;
+  std::vector<InstSchedule> loc(ni);
+  parallel_for(ni, [&](int64_t i) { instance_schedule(host, cap, (int32_t)i, loc[i]); });
+  // bases: segments, slots, tiles, level entries
+  std::vector<size_t> sb(ni + 1, 0), lb(ni + 1, 0), tb(ni + 1, 0), eb(ni + 1, 0);
+  for (int32_t i = 0; i < ni; i++) {
+    sb[i + 1] = sb[i] + loc[i].seg_len.size();
+    lb[i + 1] = lb[i] + loc[i].slot_row.size();
+    tb[i + 1] = tb[i] + loc[i].tile_seg.size();
+    eb[i + 1] = eb[i] + loc[i].lev_tile.size();
+  }
+  T.seg_len.resize(sb[ni]); T.seg_c1.resize(sb[ni]); T.seg_c2.resize(sb[ni]);
+  T.seg_prow.resize(sb[ni]); T.seg_soff.resize(sb[ni]);
+  T.slot_row.resize(lb[ni]); T.slot_flag.resize(lb[ni]);
+  T.tile_seg.resize(tb[ni]); T.tile_slot.resize(tb[ni]);
+  T.lev_tile.resize(eb[ni]);
+  T.work_lev.assign(ni + 1, 0);
+  parallel_for(ni, [&](int64_t i) {
+    const InstSchedule &L = loc[i];
+    const int s0 = (int)sb[i], l0 = (int)lb[i], t0 = (int)tb[i];
+    for (size_t q = 0; q < L.seg_len.size(); q++) {
+      T.seg_len[s0 + q] = L.seg_len[q];
+      T.seg_prow[s0 + q] = L.seg_prow[q];
+      T.seg_soff[s0 + q] = L.seg_soff[q];
+      T.seg_c1[s0 + q] = L.seg_c1[q] >= 0 ? L.seg_c1[q] + s0 : -1;
+      T.seg_c2[s0 + q] = L.seg_c2[q] >= 0 ? L.seg_c2[q] + s0 : -1;
+    }
+    std::copy(L.slot_row.begin(), L.slot_row.end(), T.slot_row.begin() + l0);
+    std::copy(L.slot_flag.begin(), L.slot_flag.end(), T.slot_flag.begin() + l0);
+    for (size_t q = 0; q < L.tile_seg.size(); q++) {
+      T.tile_seg[t0 + q] = L.tile_seg[q] + s0;
+      T.tile_slot[t0 + q] = L.tile_slot[q] + l0;
+    }
+    for (size_t q = 0; q < L.lev_tile.size(); q++) T.lev_tile[eb[i] + q] = L.lev_tile[q] + t0;
+    T.work_lev[i] = (int)eb[i];
+  });
+  T.work_lev[ni] = (int)T.lev_tile.size();
+  T.lev_tile.push_back((int)T.tile_seg.size());
+  // sentinel tile (the slot count is already a multiple of 16), then the copy overrun pad
+  T.tile_seg.push_back((int)T.seg_len.size());
+  T.tile_slot.push_back((int)T.slot_row.size());
+  for (int q = 0; q < 16; q++) {
+    T.slot_row.push_back(-1);
+    T.slot_flag.push_back(SL_PAD | SL_FIRST | SL_LAST);
+  }
+}
+
 // Groups pieces [pa, pb) into tiles whose row span fits the shared-memory staging area.
 static void make_tiles(const std::vector<int2> &pieces, int pa, int pb, int tile_rows,
                        std::vector<int> &tiles) {
@@ -1854,23 +1987,30 @@ int Engine::implicit_plan(size_t &bytes) {
   // predecessor (mother == j - 1 with a mother column), cut at kMaxPiece rows.
   S.inst_row.assign(host.off.begin(), host.off.end());
   std::vector<int> inst_piece(ni + 1, 0);
-  for (int32_t i = 0; i < ni; i++) {
-    const int64_t o = host.off[i], n = host.num_elem[i];
-    int64_t start = -1;
-    for (int64_t jl = 0; jl < n; jl++) {
-      const int64_t j = o + jl;
-      const Topo &t = host.topo[j];
-      const bool ident = t.flags & F_IDENT;
-      const bool linked = !ident && (t.flags & F_UP) && t.mother == j - 1 && start >= 0 &&
-                          (j - start) < kMaxPiece;
-      if (!linked && start >= 0) {
-        S.pieces.push_back(make_int2((int)start, (int)(j - start)));
-        start = -1;
+  {
+    std::vector<std::vector<int2>> ip(ni);  // per instance, then concatenated in order
+    parallel_for(ni, [&](int64_t i) {
+      const int64_t o = host.off[i], n = host.num_elem[i];
+      int64_t start = -1;
+      for (int64_t jl = 0; jl < n; jl++) {
+        const int64_t j = o + jl;
+        const Topo &t = host.topo[j];
+        const bool ident = t.flags & F_IDENT;
+        const bool linked = !ident && (t.flags & F_UP) && t.mother == j - 1 && start >= 0 &&
+                            (j - start) < kMaxPiece;
+        if (!linked && start >= 0) {
+          ip[i].push_back(make_int2((int)start, (int)(j - start)));
+          start = -1;
+        }
+        if (!ident && start < 0) start = j;
       }
-      if (!ident && start < 0) start = j;
-    }
-    if (start >= 0) S.pieces.push_back(make_int2((int)start, (int)(o + n - start)));
-    inst_piece[i + 1] = (int)S.pieces.size();
+      if (start >= 0) ip[i].push_back(make_int2((int)start, (int)(o + n - start)));
+    });
+    for (int32_t i = 0; i < ni; i++) inst_piece[i + 1] = inst_piece[i] + (int)ip[i].size();
+    S.pieces.resize(inst_piece[ni]);
+    parallel_for(ni, [&](int64_t i) {
+      std::copy(ip[i].begin(), ip[i].end(), S.pieces.begin() + inst_piece[i]);
+    });
   }
   const int np = (int)S.pieces.size();
   const size_t tb = opt.precision == NRT_MIXED ? 4 : 8;
@@ -1939,7 +2079,10 @@ int Engine::implicit_plan(size_t &bytes) {
   if (tree) {
     // staging slots: three T rows, the slot row and the slot flag per slot
     S.iv.tree_cap = (int)(kTileBytes / (3 * tb + 5)) & ~15;
-    build_tree_schedule(host, S.iv.tree_cap, S.grid_mode, S.grid_blocks, S.tree);
+    if (S.grid_mode)
+      build_tree_schedule(host, S.iv.tree_cap, true, S.grid_blocks, S.tree);
+    else
+      build_tree_schedule_batch(host, S.iv.tree_cap, S.tree);
   }
   // device bytes, in the order implicit_init takes them
   const int m = opt.restart;
@@ -1991,8 +2134,13 @@ int Engine::implicit_init() {
   iv.tile_rows = S.tile_rows;
   uint8_t *pr;
   TRYI(up(arena, pr, S.rowf.data(), N, st)); iv.rowf = pr;
-  std::vector<double> cmdt(N), g64(N), w64(N), k64(N), inp(N);
-  std::vector<float> gf(N);
+  // staging buffers filled in parallel (no zero fill first)
+  std::unique_ptr<double[]> cmdt_b(new double[N]), g64_b(new double[N]), w64_b(new double[N]),
+      k64_b(new double[N]), inp_b(new double[N]);
+  std::unique_ptr<float[]> gf_b(new float[N]);
+  double *cmdt = cmdt_b.get(), *g64 = g64_b.get(), *w64 = w64_b.get(), *k64 = k64_b.get(),
+         *inp = inp_b.get();
+  float *gf = gf_b.get();
   parallel_ranges(N, [&](int64_t a, int64_t b) {
     for (int64_t j = a; j < b; j++) {
       cmdt[j] = host.c_m_dx[j] / host.inst[host.topo[j].flags >> INST_SHIFT].dT;
@@ -2004,15 +2152,15 @@ int Engine::implicit_init() {
     }
   });
   double *p;
-  TRYI(up(arena, p, cmdt.data(), N, st)); iv.cmdt = p;
-  TRYI(up(arena, p, g64.data(), N, st)); iv.g64 = p;
-  TRYI(up(arena, p, w64.data(), N, st)); iv.wdx64 = p;
-  TRYI(up(arena, p, k64.data(), N, st)); iv.kdx64 = p;
-  TRYI(up(arena, p, inp.data(), N, st)); iv.inp64 = p;
+  TRYI(up(arena, p, cmdt, N, st)); iv.cmdt = p;
+  TRYI(up(arena, p, g64, N, st)); iv.g64 = p;
+  TRYI(up(arena, p, w64, N, st)); iv.wdx64 = p;
+  TRYI(up(arena, p, k64, N, st)); iv.kdx64 = p;
+  TRYI(up(arena, p, inp, N, st)); iv.inp64 = p;
   TRYI(up(arena, iv.diag, (const double *)nullptr, N, st));
   TRYI(up(arena, iv.rhs, (const double *)nullptr, N, st));
   float *pf;
-  TRYI(up(arena, pf, gf.data(), N, st)); iv.gf = pf;
+  TRYI(up(arena, pf, gf, N, st)); iv.gf = pf;
   iv.cdiag = arena.take(tb * N);
   if (!iv.cdiag) {
     set_error("arena exhausted");
@@ -2068,15 +2216,17 @@ int Engine::implicit_init() {
     TRYI(up(arena, pi, T.lev_tile.data(), T.lev_tile.size(), st)); iv.lev_tile = pi;
     TRYI(up(arena, pi, T.work_lev.data(), T.work_lev.size(), st)); iv.work_lev = pi;
     // static per-slot conductance to the mother (0 on a row without that column)
-    sgbuf.assign(tb * ns, 0);
-    for (size_t k = 0; k < ns; k++) {
-      const int r = T.slot_row[k];
-      const double g = (r >= 0 && (host.topo[r].flags & F_UP)) ? host.gax[r] : 0.0;
-      if (mixed)
-        ((float *)sgbuf.data())[k] = (float)g;
-      else
-        ((double *)sgbuf.data())[k] = g;
-    }
+    sgbuf.resize(tb * ns);
+    parallel_ranges((int64_t)ns, [&](int64_t a, int64_t b) {
+      for (int64_t k = a; k < b; k++) {
+        const int r = T.slot_row[k];
+        const double g = (r >= 0 && (host.topo[r].flags & F_UP)) ? host.gax[r] : 0.0;
+        if (mixed)
+          ((float *)sgbuf.data())[k] = (float)g;
+        else
+          ((double *)sgbuf.data())[k] = g;
+      }
+    });
     void *sgd = arena.take(tb * ns);
     iv.sinv = arena.take(tb * ns);
     iv.se = arena.take(tb * ns);

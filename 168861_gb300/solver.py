@@ -398,6 +398,14 @@ class Batch(_Recorder):
         check(self.lib.nrt_batch_snapshot(self.h, i, _p(out, ctypes.c_double)), "nrt_batch_snapshot")
         return out
 
+    def snapshot_all(self) -> list:
+        """Latest potential of every instance, from one device-to-host copy."""
+        sizes = [p.num_elem for p in self.problems]
+        out = np.empty(sum(sizes))
+        check(self.lib.nrt_batch_snapshot_all(self.h, _p(out, ctypes.c_double)),
+              "nrt_batch_snapshot_all")
+        return np.split(out, np.cumsum(sizes)[:-1])
+
     def remaining(self) -> np.ndarray:
         out = np.zeros(self.count, np.int64)
         check(self.lib.nrt_batch_remaining(self.h, _p(out, ctypes.c_int64)), "nrt_batch_remaining")

@@ -221,6 +221,9 @@ int nrt_batch_synchronize(nrt_batch *b);
 int nrt_batch_get_stream(nrt_batch *b, void **stream);
 /* Latest potential of one instance (its num_elem doubles) to host memory. */
 int nrt_batch_snapshot(nrt_batch *b, int32_t instance, double *potential);
+/* Latest potential of every instance in one copy: the instances' num_elem doubles back
+ * to back, in instance order. */
+int nrt_batch_snapshot_all(nrt_batch *b, double *potential);
 /* Number of loop iterations still to run per instance (count entries). */
 int nrt_batch_remaining(nrt_batch *b, int64_t *remaining);
 int nrt_batch_get_stats(nrt_batch *b, nrt_stats *st);

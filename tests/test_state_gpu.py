@@ -101,3 +101,16 @@ def test_set_state_general_first_step(gpu, pkg, orc):
     Vo, _ = orc.explicit_run(spec, d, float(g["dT"]), 1, 200, V=V.copy())
     assert np.abs(s.snapshot() - Vo).max() < 1e-9
     s.close()
+
+
+def test_snapshot_all_equals_per_instance(gpu, pkg, model):
+    specs = [model.random_tree(seed=60 + q, n_target=900 + 700 * q, dt=2.5e-5, tspan=1e-3)
+             for q in range(4)]
+    probs = [pkg.ProblemArrays.from_spec(sp, pkg.derive(sp)) for sp in specs]
+    b = pkg.Batch(probs, mode=1, precision="mixed", restart=20, tol=1e-10, tol_mode="rel")
+    b.set_runs([(1, 1 + 5 + q, sp.init_time, sp.end_input) for q, sp in enumerate(specs)])
+    b.advance(8)
+    allv = b.snapshot_all()
+    for q in range(len(specs)):
+        np.testing.assert_array_equal(allv[q], b.snapshot(q))
+    b.close()
