@@ -39,6 +39,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "compartment-steps/s"
+
+# DRAM bytes (read + write) per compartment-step of the dominant kernel, from ncu captures
+# of a 1024-tree case (21.9M elements, above L2; profiles/ gives the commands): the
+# explicit step moved 1391.1 MB per launch, the implicit launch 28.63 GB over 3 steps.
+# The traffic of a full-size step is scaled from these by the compartments it processes.
+TRAFFIC_PER_ELEMENT_STEP = {"batch-explicit-mixed": 1391.1e6 / 21910344,
+                            "batch-implicit-mixed": 28.63e9 / (3 * 21910344)}
 WORKLOADS = ("batch-implicit-mixed", "batch-explicit-mixed", "batch-explicit-fp64",
              "axon-explicit-fp64", "serve")
 DEFAULT_WORKLOAD = "batch-implicit-mixed"
@@ -384,9 +391,13 @@ def run_ours(args, rank: int, world: int):
     peak, peak_kind = measured_peaks()
     # per GPU: the job's algorithmic bytes over the slowest rank's time, divided by N
     achieved = alg_all * K / (ms / 1e3) / 1e9 / world
+    per_el = TRAFFIC_PER_ELEMENT_STEP.get(wl)
+    traffic = per_el * n_all / world if per_el else None  # per GPU and step, like achieved
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-            "algorithmic_bytes_per_step": alg_all}
+            "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+            "algorithmic_bytes_per_step": alg_all,
+            "traffic_note": "DRAM bytes per step, ncu on 1024 trees scaled by compartments"
+                            if per_el else None}
     roof_passes = None
     if passes is not None:
         # the same kernel time against the bytes its own passes must move (preconditioner
