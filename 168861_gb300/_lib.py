@@ -92,6 +92,7 @@ EXPORTS = (
     "nrt_measurement_point", "nrt_record", "nrt_batch_record", "nrt_record_read",
     "nrt_batch_record_read", "nrt_batch_pass_counts", "nrt_get_state", "nrt_set_state",
     "nrt_batch_get_state", "nrt_batch_set_state", "nrt_batch_snapshot_all",
+    "nrt_server_submit_recorded", "nrt_server_recording",
 )
 
 _lib = None
@@ -141,6 +142,11 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "nrt_server_submit": [vp, ctypes.POINTER(Problem), ctypes.c_int,
                               ctypes.POINTER(InstanceRun), _i64p],
         "nrt_server_result": [vp, ctypes.c_int64, _f64p],
+        "nrt_server_submit_recorded": [vp, ctypes.POINTER(Problem), ctypes.c_int,
+                                       ctypes.POINTER(InstanceRun), ctypes.POINTER(RecordConfig),
+                                       _i64p],
+        "nrt_server_recording": [vp, ctypes.c_int64, _i64p, _f64p, _f64p,
+                                 ctypes.POINTER(ctypes.c_int32), _f64p],
         "nrt_server_drain": [vp],
         "nrt_server_get_stats": [vp, ctypes.POINTER(ServerStats)],
         "nrt_server_destroy": [vp],

@@ -68,9 +68,31 @@ struct OwnedProblem {
   }
 };
 
+// Recording settings of a request (nrt_server_submit_recorded); requests are batched only
+// with requests of equal settings, since a batch records under one configuration.
+struct RecSpec {
+  bool on = false;
+  int64_t origin = 1, interval = 0, capacity = 0;
+  double threshold = 0;
+  int32_t max_spikes = 0;
+  bool operator<(const RecSpec &o) const {
+    if (on != o.on) return on < o.on;
+    if (origin != o.origin) return origin < o.origin;
+    if (interval != o.interval) return interval < o.interval;
+    if (capacity != o.capacity) return capacity < o.capacity;
+    if (threshold != o.threshold) return threshold < o.threshold;
+    return max_spikes < o.max_spikes;
+  }
+};
+
 struct Request {
   int64_t id = 0;
   bool implicit = false;
+  RecSpec rec;
+  std::vector<int32_t> probes;          // elements of this tree
+  std::vector<int64_t> rec_ns;          // per probe: samples taken
+  std::vector<int32_t> rec_nk;          // per probe: crossings found
+  std::vector<double> rec_t, rec_v, rec_sp;  // [probe][capacity], [probe][max_spikes]
   OwnedProblem prob;
   nrt_instance_run run{};
   size_t bytes = 0;
@@ -83,6 +105,8 @@ struct Request {
 struct MicroBatch {
   nrt_batch *b = nullptr;
   std::vector<Request *> reqs;
+  RecSpec rec;                     // the batch's recording settings (rec.on: recording)
+  std::vector<int32_t> probe0;     // per request: first probe in the batch's configuration
   std::vector<char> finished;
   size_t bytes = 0;
   size_t open = 0;
@@ -141,6 +165,29 @@ MicroBatch *nrt_server::admit(bool implicit, std::vector<Request *> &batch, bool
   if (wide) o.schedule = 0;
   int rc = nrt_batch_create(probs.data(), (int32_t)probs.size(), &o, &mb->b);
   if (rc == NRT_OK) rc = nrt_batch_set_runs(mb->b, runs.data());
+  mb->rec = batch.empty() ? RecSpec() : batch[0]->rec;
+  if (rc == NRT_OK && mb->rec.on) {  // every request's probes, instance = its batch position
+    std::vector<int32_t> inst, elem;
+    mb->probe0.assign(batch.size() + 1, 0);
+    for (size_t q = 0; q < batch.size(); q++) {
+      for (int32_t e : batch[q]->probes) {
+        inst.push_back((int32_t)q);
+        elem.push_back(e);
+      }
+      mb->probe0[q + 1] = (int32_t)elem.size();
+    }
+    nrt_record_config rc_cfg;
+    memset(&rc_cfg, 0, sizeof(rc_cfg));
+    rc_cfg.num_probes = (int32_t)elem.size();
+    rc_cfg.instance = inst.data();
+    rc_cfg.element = elem.data();
+    rc_cfg.origin = mb->rec.origin;
+    rc_cfg.interval = mb->rec.interval;
+    rc_cfg.capacity = mb->rec.capacity;
+    rc_cfg.threshold = mb->rec.threshold;
+    rc_cfg.max_spikes = mb->rec.max_spikes;
+    rc = nrt_batch_record(mb->b, &rc_cfg);
+  }
   std::lock_guard<std::mutex> lk(mu);
   if (rc != NRT_OK) {
     for (Request *r : batch) {
@@ -220,11 +267,14 @@ void nrt_server::loop() {
       }
       take[1].swap(narrow);
     }
-    for (int k = 0; k < 2; k++)
-      if (!take[k].empty()) {
-        MicroBatch *mb = admit(k == 1, take[k]);
+    for (int k = 0; k < 2; k++) {
+      std::map<RecSpec, std::vector<Request *>> groups;  // one batch per recording setting
+      for (Request *r : take[k]) groups[r->rec].push_back(r);
+      for (auto &g : groups) {
+        MicroBatch *mb = admit(k == 1, g.second);
         if (mb) active.push_back(mb);
       }
+    }
     if (active.empty()) continue;
     const auto t0 = Clock::now();
     // one tick: every resident batch advances on its own stream (all enqueued first)
@@ -247,11 +297,39 @@ void nrt_server::loop() {
       }
       nrt_stats bs;
       const bool bad = rc != NRT_OK;
+      // the batch's recording, read once per tick in which one of its requests finished
+      std::vector<int64_t> rns;
+      std::vector<int32_t> rnk;
+      std::vector<double> rt, rv, rsp;
+      bool rec_read = false;
+      int rec_rc = NRT_OK;
       for (size_t q = 0; q < mb->reqs.size(); q++) {
         if (mb->finished[q] || (!bad && rem[q] > 0)) continue;
         Request *r = mb->reqs[q];
+        if (mb->rec.on && !bad && !rec_read) {
+          const size_t P = (size_t)mb->probe0.back(), cap = (size_t)mb->rec.capacity,
+                       ms = (size_t)mb->rec.max_spikes;
+          rns.resize(P);
+          rnk.resize(P);
+          rt.resize(P * std::max<size_t>(cap, 1));
+          rv.resize(P * std::max<size_t>(cap, 1));
+          rsp.resize(P * std::max<size_t>(ms, 1));
+          rec_rc = nrt_batch_record_read(mb->b, rns.data(), rt.data(), rv.data(), rnk.data(),
+                                         rsp.data());
+          rec_read = true;
+        }
+        if (mb->rec.on && rec_read && rec_rc == NRT_OK) {
+          const size_t p0 = (size_t)mb->probe0[q], p1 = (size_t)mb->probe0[q + 1];
+          const size_t cap = (size_t)mb->rec.capacity, ms = (size_t)mb->rec.max_spikes;
+          r->rec_ns.assign(rns.begin() + p0, rns.begin() + p1);
+          r->rec_nk.assign(rnk.begin() + p0, rnk.begin() + p1);
+          r->rec_t.assign(rt.begin() + p0 * cap, rt.begin() + p1 * cap);
+          r->rec_v.assign(rv.begin() + p0 * cap, rv.begin() + p1 * cap);
+          r->rec_sp.assign(rsp.begin() + p0 * ms, rsp.begin() + p1 * ms);
+        }
         r->result.resize(r->prob.p.num_elem);
         int src = bad ? rc : nrt_batch_snapshot(mb->b, (int32_t)q, r->result.data());
+        if (src == NRT_OK && rec_rc != NRT_OK) src = rec_rc;
         std::lock_guard<std::mutex> lk(mu);
         r->status = src;
         r->done = true;
@@ -288,6 +366,50 @@ void nrt_server::loop() {
   }
 }
 
+static int submit_request(nrt_server *s, const nrt_problem *p, int implicit,
+                          const nrt_instance_run *run, const nrt_record_config *rec,
+                          int64_t *request_id) {
+  if (!s || !p || !run || !request_id) return NRT_EINVAL;
+  if (p->num_elem < 4 || run->i_end < run->i_begin) return NRT_EINVAL;
+  if (rec) {
+    if (rec->num_probes < 0 || (rec->num_probes > 0 && !rec->element) || rec->interval < 0 ||
+        rec->capacity < 0 || rec->max_spikes < 0)
+      return NRT_EINVAL;
+    for (int32_t q = 0; q < rec->num_probes; q++)
+      if (rec->element[q] < 0 || rec->element[q] >= p->num_elem) return NRT_EINVAL;
+  }
+  Request *r = new (std::nothrow) Request();
+  if (!r) return NRT_ENOMEM;
+  r->implicit = implicit != 0;
+  r->prob.copy(*p);
+  r->run = *run;
+  if (rec && rec->num_probes > 0) {  // complete before the worker can see the request
+    r->rec.on = true;
+    r->rec.origin = rec->origin;
+    r->rec.interval = rec->interval;
+    r->rec.capacity = rec->capacity;
+    r->rec.threshold = rec->threshold;
+    r->rec.max_spikes = rec->max_spikes;
+    r->probes.assign(rec->element, rec->element + rec->num_probes);
+  }
+  r->bytes = estimate_bytes(*p, s->opt[r->implicit ? 1 : 0]);
+  r->t_submit = Clock::now();
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->st.submitted++;
+  if (r->bytes > (size_t)s->cfg.budget_bytes) {
+    s->st.rejected++;
+    delete r;
+    return NRT_EBUDGET;
+  }
+  r->id = s->next_id++;
+  *request_id = r->id;
+  s->reqs[r->id] = r;
+  s->pending.push_back(r);
+  s->outstanding++;
+  s->cv_work.notify_one();
+  return NRT_OK;
+}
+
 extern "C" {
 
 int nrt_server_create(const nrt_server_config *cfg, const nrt_options *explicit_opt,
@@ -313,28 +435,31 @@ int nrt_server_create(const nrt_server_config *cfg, const nrt_options *explicit_
 
 int nrt_server_submit(nrt_server *s, const nrt_problem *p, int implicit,
                       const nrt_instance_run *run, int64_t *request_id) {
-  if (!s || !p || !run || !request_id) return NRT_EINVAL;
-  if (p->num_elem < 4 || run->i_end < run->i_begin) return NRT_EINVAL;
-  Request *r = new (std::nothrow) Request();
-  if (!r) return NRT_ENOMEM;
-  r->implicit = implicit != 0;
-  r->prob.copy(*p);
-  r->run = *run;
-  r->bytes = estimate_bytes(*p, s->opt[r->implicit ? 1 : 0]);
-  r->t_submit = Clock::now();
+  return submit_request(s, p, implicit, run, nullptr, request_id);
+}
+
+int nrt_server_submit_recorded(nrt_server *s, const nrt_problem *p, int implicit,
+                               const nrt_instance_run *run, const nrt_record_config *rec,
+                               int64_t *request_id) {
+  if (!rec) return NRT_EINVAL;
+  return submit_request(s, p, implicit, run, rec, request_id);
+}
+
+int nrt_server_recording(nrt_server *s, int64_t id, int64_t *num_samples, double *times,
+                         double *values, int32_t *num_spikes, double *spike_times) {
+  if (!s) return NRT_EINVAL;
   std::lock_guard<std::mutex> lk(s->mu);
-  s->st.submitted++;
-  if (r->bytes > (size_t)s->cfg.budget_bytes) {
-    s->st.rejected++;
-    delete r;
-    return NRT_EBUDGET;
-  }
-  r->id = s->next_id++;
-  *request_id = r->id;
-  s->reqs[r->id] = r;
-  s->pending.push_back(r);
-  s->outstanding++;
-  s->cv_work.notify_one();
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return NRT_ESTATE;
+  Request *r = it->second;
+  if (!r->done) return NRT_ENOTREADY;
+  if (!r->rec.on) return NRT_ESTATE;
+  if (r->rec_ns.size() != r->probes.size()) return r->status != NRT_OK ? r->status : NRT_EDEVICE;
+  if (num_samples) std::copy(r->rec_ns.begin(), r->rec_ns.end(), num_samples);
+  if (num_spikes) std::copy(r->rec_nk.begin(), r->rec_nk.end(), num_spikes);
+  if (times) std::copy(r->rec_t.begin(), r->rec_t.end(), times);
+  if (values) std::copy(r->rec_v.begin(), r->rec_v.end(), values);
+  if (spike_times) std::copy(r->rec_sp.begin(), r->rec_sp.end(), spike_times);
   return NRT_OK;
 }
 

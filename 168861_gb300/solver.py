@@ -468,15 +468,53 @@ class Server:
               "nrt_server_create")
         self.h = h
         self.sizes = {}
+        self.rec_shape = {}
 
     def submit(self, problem: ProblemArrays, implicit: bool, i_begin: int, i_end: int,
-               init_time: float, end_input: float) -> int:
+               init_time: float, end_input: float, probes=None, interval: int = 0,
+               origin: int = 1, capacity: int = 4096, threshold: float = 0.0,
+               max_spikes: int = 64) -> int:
+        """Queues a request; with `probes` (elements of this tree) its samples and spike
+        times are recorded on the device (nrt_server_submit_recorded)."""
         run = _lib.InstanceRun(int(i_begin), int(i_end), float(init_time), float(end_input))
         rid = ctypes.c_int64(0)
-        check(self.lib.nrt_server_submit(self.h, ctypes.byref(problem.struct), int(bool(implicit)),
-                                         ctypes.byref(run), ctypes.byref(rid)), "nrt_server_submit")
+        if probes is None:
+            check(self.lib.nrt_server_submit(self.h, ctypes.byref(problem.struct),
+                                             int(bool(implicit)), ctypes.byref(run),
+                                             ctypes.byref(rid)), "nrt_server_submit")
+        else:
+            el = np.ascontiguousarray(probes, dtype=np.int32)
+            cfg = _lib.RecordConfig()
+            cfg.num_probes = len(el)
+            cfg.element = _p(el, ctypes.c_int32)
+            cfg.origin, cfg.interval, cfg.capacity = int(origin), int(interval), int(capacity)
+            cfg.threshold, cfg.max_spikes = float(threshold), int(max_spikes)
+            check(self.lib.nrt_server_submit_recorded(self.h, ctypes.byref(problem.struct),
+                                                      int(bool(implicit)), ctypes.byref(run),
+                                                      ctypes.byref(cfg), ctypes.byref(rid)),
+                  "nrt_server_submit_recorded")
+            self.rec_shape[rid.value] = (len(el), int(capacity), int(max_spikes))
         self.sizes[rid.value] = problem.num_elem
         return rid.value
+
+    def recording(self, rid: int):
+        """The recording of a finished request (before result()), or None while it runs."""
+        P, cap, ms = self.rec_shape[rid]
+        ns = np.zeros(P, np.int64)
+        nk = np.zeros(P, np.int32)
+        t = np.zeros((P, max(cap, 1)))
+        v = np.zeros((P, max(cap, 1)))
+        sp = np.zeros((P, max(ms, 1)))
+        rc = self.lib.nrt_server_recording(self.h, int(rid), _p(ns, ctypes.c_int64),
+                                           _p(t, ctypes.c_double), _p(v, ctypes.c_double),
+                                           _p(nk, ctypes.c_int32), _p(sp, ctypes.c_double))
+        if rc == _lib.NRT_ENOTREADY:
+            return None
+        check(rc, "nrt_server_recording")
+        kept, ks = np.minimum(ns, cap), np.minimum(nk, ms)
+        return Recording([t[p, :kept[p]].copy() for p in range(P)],
+                         [v[p, :kept[p]].copy() for p in range(P)], ns,
+                         [sp[p, :ks[p]].copy() for p in range(P)], nk)
 
     def result(self, rid: int):
         """Final potential of a finished request, or None while it runs."""

@@ -355,6 +355,19 @@ int nrt_server_create(const nrt_server_config *cfg, const nrt_options *explicit_
 /* Copies the request; returns its id.  NRT_EBUDGET if it can never fit the budget. */
 int nrt_server_submit(nrt_server *s, const nrt_problem *p, int implicit,
                       const nrt_instance_run *run, int64_t *request_id);
+/* As nrt_server_submit, with probes recorded on the device while the request runs
+ * (nrt_record_config: elements of this tree; `instance` is ignored).  Requests are batched
+ * only with requests of the same recording settings (origin, interval, capacity, threshold,
+ * max_spikes). */
+int nrt_server_submit_recorded(nrt_server *s, const nrt_problem *p, int implicit,
+                               const nrt_instance_run *run, const nrt_record_config *rec,
+                               int64_t *request_id);
+/* The recording of a finished request, laid out as nrt_record_read's.  Call it before
+ * nrt_server_result, which releases the request.  NRT_ENOTREADY while it runs;
+ * NRT_ESTATE for a request submitted without probes. */
+int nrt_server_recording(nrt_server *s, int64_t request_id, int64_t *num_samples,
+                         double *times, double *values, int32_t *num_spikes,
+                         double *spike_times);
 /* NRT_ENOTREADY until the request finished; then copies its final potential
  * (num_elem doubles) and releases it.  Returns the request's solver status. */
 int nrt_server_result(nrt_server *s, int64_t request_id, double *potential);

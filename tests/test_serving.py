@@ -64,3 +64,37 @@ def test_server_results_equal_alone_runs(gpu, pkg, model):
         assert np.abs(got - ref).max() < 1e-4, (rid, im)
         alone.close()
     srv.close()
+
+
+@pytest.mark.gpu
+def test_server_recording_equals_alone(gpu, pkg, model):
+    """Per-request probes in the server record what each request records alone: requests
+    with equal settings share batches, a request with other settings gets its own."""
+    reqs = _requests(pkg, model)[:6]
+    srv = pkg.Server(budget_bytes=2 << 30, chunk_steps=16, max_wait_us=0,
+                     explicit_opts=EX_OPTS, implicit_opts=IM_OPTS)
+    ids, probes, settings = [], [], []
+    for q, (p, im, run) in enumerate(reqs):
+        pr = [1, p.num_elem // 2, p.num_elem - 2]
+        st = dict(interval=1 + (q == 4), capacity=400, threshold=-0.06, max_spikes=8)
+        ids.append(srv.submit(p, im, *run, probes=pr, **st))
+        probes.append(pr)
+        settings.append(st)
+    plain = srv.submit(reqs[0][0], False, *reqs[0][2])   # no probes
+    srv.drain()
+    # a request submitted without probes has no recording
+    assert srv.lib.nrt_server_recording(srv.h, plain, None, None, None, None, None) == 7
+    for rid, (p, im, run), pr, st in zip(ids, reqs, probes, settings):
+        got = srv.recording(rid)
+        alone = (pkg.SolverIm if im else pkg.SolverEx)(p, **(IM_OPTS if im else EX_OPTS))
+        alone.record(pr, **st)
+        alone.run(*run)
+        want = alone.recording()
+        alone.close()
+        np.testing.assert_array_equal(got.num_samples, want.num_samples)
+        np.testing.assert_array_equal(got.num_spikes, want.num_spikes)
+        for c in range(len(pr)):
+            np.testing.assert_array_equal(got.times[c], want.times[c])
+            assert np.abs(got.values[c] - want.values[c]).max() < 1e-4
+        assert srv.result(rid) is not None
+    srv.close()
