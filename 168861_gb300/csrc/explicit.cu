@@ -369,49 +369,75 @@ __device__ __forceinline__ void tile_element(const PackView &p, int k, int force
   Fout[j] = (float)vn;
 }
 
-__global__ void __launch_bounds__(kTileThreads) explicit_step_mixed_tiled(
+// Buffers pass between the issuing thread and the warps on mbarriers: `full[b]` completes
+// when tile data has landed in buffer b, `empty[b]` when every warp is done with it.  A warp
+// that finishes its part of a tile moves on to the other buffer without waiting for the
+// rest of the CTA; only the issuing thread waits, for `empty`, before refilling a buffer.
+constexpr int kTileWarps = kTileThreads / 32;
+
+__global__ void __launch_bounds__(kTileThreads, 5) explicit_step_mixed_tiled(
     PackView p, int k, int force, const double *__restrict__ Vin, double *__restrict__ Vout,
     const float *__restrict__ Fin, float *__restrict__ Fout) {
   extern __shared__ __align__(16) unsigned char tsm[];
-  uint64_t *bar = (uint64_t *)(tsm + 2 * kTileBufBytes);
+  uint64_t *full = (uint64_t *)(tsm + 2 * kTileBufBytes);
+  uint64_t *empty = full + 2;
   const int64_t N = p.ntot;
   const int64_t ntiles = (N + kTileE - 1) / kTileE;
   if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    mbar_init(&empty[0], kTileWarps);
+    mbar_init(&empty[1], kTileWarps);
     fence_proxy_async();
   }
   __syncthreads();
+  const bool issuer = threadIdx.x == 0;
   int64_t t = blockIdx.x;
-  if (t < ntiles && threadIdx.x == 0) issue_tile(p, Fin, Vin, t, tsm, &bar[0]);
-  uint32_t phase0 = 0, phase1 = 0;
+  // per buffer: phase bits of `full` and `empty`, and (issuer) copies in flight; bit q of
+  // each word is buffer q (no per-thread arrays: they would live in local memory)
+  uint32_t pf = 0, pe = 0, pending = 0;
+  if (t < ntiles && issuer) {
+    issue_tile(p, Fin, Vin, t, tsm, &full[0]);
+    pending = 1;
+  }
   int b = 0;
+  bool first = true;
   for (; t < ntiles; t += gridDim.x) {
     const int64_t tn = t + gridDim.x;
-    unsigned char *buf = tsm + b * kTileBufBytes;
-    if (tn < ntiles && threadIdx.x == 0) {
-      fence_proxy_async();  // the other buffer's reads (last iteration) before its refill
-      issue_tile(p, Fin, Vin, tn, tsm + (b ^ 1) * kTileBufBytes, &bar[b ^ 1]);
-    }
-    const uint32_t ph = b ? phase1 : phase0;
-    const bool ok = mbar_wait_ok(&bar[b], ph, p.err);
-    if (__syncthreads_or(!ok)) {
-      // a copy never landed (a device fault): wait, bounded, for what is still in flight
-      if (threadIdx.x == 0) {
-        mbar_wait_ok(&bar[b], ph, p.err);
-        if (tn < ntiles) mbar_wait_ok(&bar[b ^ 1], b ? phase0 : phase1, p.err);
+    bool ok = true;
+    if (issuer && tn < ntiles) {
+      const int nb = b ^ 1;
+      if (!first) {  // every warp released buffer nb (the previous tile) before its refill
+        ok = mbar_wait_ok(&empty[nb], (pe >> nb) & 1u, p.err);
+        pe ^= 1u << nb;
       }
-      __syncthreads();
+      if (ok) {
+        fence_proxy_async();
+        issue_tile(p, Fin, Vin, tn, tsm + nb * kTileBufBytes, &full[nb]);
+        pending |= 1u << nb;
+      }
+    }
+    first = false;
+    if (ok) ok = mbar_wait_ok(&full[b], (pf >> b) & 1u, p.err);
+    if (!ok) {
+      // a copy never landed or a warp never released its buffer (a device fault): the
+      // issuer waits, bounded, for the copies it still has in flight; every thread returns
+      if (issuer)
+        for (int q = 0; q < 2; q++)
+          if ((pending >> q) & 1u) mbar_wait_ok(&full[q], (pf >> q) & 1u, p.err);
       return;
     }
-    if (b) phase1 ^= 1; else phase0 ^= 1;
+    pending &= ~(1u << b);
+    pf ^= 1u << b;
     const TileWin w = tile_win(t, N);
+    const unsigned char *buf = tsm + b * kTileBufBytes;
 #pragma unroll
     for (int u = 0; u < kTileE / kTileThreads; u++) {
       const int64_t l = threadIdx.x + u * kTileThreads;
       if (l < w.cnt) tile_element(p, k, force, buf, w, w.s + l, Fin, Vout, Fout);
     }
-    __syncthreads();  // this buffer's reads done before it is refilled
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[b]);
     b ^= 1;
   }
 }
@@ -446,7 +472,7 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
   const unsigned blocks = (unsigned)((pv.ntot + threads - 1) / threads);
   if (precision == NRT_MIXED) {
     if (!general && pv.tile_blocks > 0 && pv.eflags && pv.err) {
-      explicit_step_mixed_tiled<<<pv.tile_blocks, kTileThreads, 2 * kTileBufBytes + 16, st>>>(
+      explicit_step_mixed_tiled<<<pv.tile_blocks, kTileThreads, 2 * kTileBufBytes + 32, st>>>(
           pv, k, force, Vin, Vout, Fin, Fout);
     } else if (general)
       explicit_step_mixed<true><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout, Fin, Fout);
@@ -467,7 +493,7 @@ int explicit_tile_blocks(int device, int64_t ntot) {
   int sms = 0, per_sm = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, explicit_step_mixed_tiled,
-                                                    kTileThreads, 2 * kTileBufBytes + 16) !=
+                                                    kTileThreads, 2 * kTileBufBytes + 32) !=
           cudaSuccess) {
     cudaGetLastError();
     return 0;

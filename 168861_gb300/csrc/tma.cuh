@@ -35,6 +35,10 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
+// One arrival on an mbarrier (a consumer releasing a buffer).
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 // Orders this thread's earlier generic-proxy accesses before later bulk (async-proxy) ones.
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async;" ::: "memory");
