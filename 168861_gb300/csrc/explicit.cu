@@ -375,7 +375,7 @@ __device__ __forceinline__ void tile_element(const PackView &p, int k, int force
 // rest of the CTA; only the issuing thread waits, for `empty`, before refilling a buffer.
 constexpr int kTileWarps = kTileThreads / 32;
 
-__global__ void __launch_bounds__(kTileThreads, 5) explicit_step_mixed_tiled(
+__global__ void __launch_bounds__(kTileThreads) explicit_step_mixed_tiled(
     PackView p, int k, int force, const double *__restrict__ Vin, double *__restrict__ Vout,
     const float *__restrict__ Fin, float *__restrict__ Fout) {
   extern __shared__ __align__(16) unsigned char tsm[];
