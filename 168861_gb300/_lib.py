@@ -92,7 +92,7 @@ EXPORTS = (
     "nrt_measurement_point", "nrt_record", "nrt_batch_record", "nrt_record_read",
     "nrt_batch_record_read", "nrt_batch_pass_counts", "nrt_get_state", "nrt_set_state",
     "nrt_batch_get_state", "nrt_batch_set_state", "nrt_batch_snapshot_all",
-    "nrt_server_submit_recorded", "nrt_server_recording",
+    "nrt_server_submit_recorded", "nrt_server_recording", "nrt_derive_batch",
 )
 
 _lib = None
@@ -126,6 +126,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "nrt_destroy": [vp],
         "nrt_derive": [ctypes.c_int32, _i32p, _f64p, ctypes.c_int32, ctypes.c_double, _f64p, _i32p,
                        _f64p, _i32p, _f64p],
+        "nrt_derive_batch": [ctypes.c_int32, _i64p, _i32p, _f64p, _i32p, _f64p, _f64p, _i32p,
+                             _f64p, _i64p, _f64p],
         "nrt_batch_create": [ctypes.POINTER(Problem), ctypes.c_int32, ctypes.POINTER(Options), vpp],
         "nrt_batch_set_runs": [vp, ctypes.POINTER(InstanceRun)],
         "nrt_batch_advance": [vp, ctypes.c_int64],

@@ -6,37 +6,8 @@
 #include <math.h>
 #include <string.h>
 
+#include "derive_elem.h"
 #include "neurite_gb300.h"
-
-namespace {
-
-// Model constants as the reference defines them: its truncated pi (src/neurite.cpp:72),
-// the HH voltage scale (src/coupling.cpp:162), the strain-damage exponent
-// (src/discretization.cpp:94) and the 45-layer myelin constants (src/discretization.cpp:54-58).
-const double kPi = 3.14159265;
-const double kScale = 0.001;
-const double kNDamage = 2.0;
-const double kThMy = 18E-9, kPerMy = 1.08E-10, kRoMy = 4.44E6;
-const int kLayersMy = 45;
-
-struct Rates {
-  double am, bm, ah, bh, an, bn;
-};
-
-Rates rates(double rest, double v, double ls_na, double ls_k) {
-  double vna = ((v + ls_na) - rest) / kScale;
-  double vk = ((v + ls_k) - rest) / kScale;
-  Rates r;
-  r.am = (2.5 - 0.1 * vna) / (exp(2.5 - 0.1 * vna) - 1);
-  r.bm = 4 * exp(-vna / 18);
-  r.ah = 0.07 * exp(-vna / 20);
-  r.bh = 1 / (exp(3 - 0.1 * vna) + 1);
-  r.an = (0.1 - 0.01 * vk) / (exp(1 - 0.1 * vk) - 1);
-  r.bn = 0.125 * exp(-vk / 80);
-  return r;
-}
-
-}  // namespace
 
 extern "C" int nrt_derive(int32_t n, const int32_t *ispec, const double *dspec, int32_t myelin,
                           double e_max, double *eparam, int32_t *hh_elem, double *hparam,
@@ -53,63 +24,19 @@ extern "C" int nrt_derive(int32_t n, const int32_t *ispec, const double *dspec, 
   const double *sna_a = dspec + 9 * N, *sk_a = dspec + 10 * N, *sl_a = dspec + 11 * N;
   const size_t H = (size_t)num_hh;
   for (size_t i = 0, k = 0; i < N; i++) {
-    const double eps = eps_a[i];
-    const double eps_s = sqrt(1 + eps) - 1;
-    const double dX = dX0[i] * (1 + eps);
-    const double d = diam0[i] / (sqrt(1 + eps));
-    const double th = th_a[i], rest = rest_a[i];
-    const double r_a = 4 * ro_a_a[i] / (kPi * d * d);
-    double r_m = (ro_m_a[i] * th) / (kPi * d);
-    double c_m = (per_m_a[i] * kPi * d) / (th);
-    double W = 0, K = 0, crit;
+    nrt_param::ElemIn in;
+    in.kind = kind[i];
+    in.dX0 = dX0[i]; in.diam0 = diam0[i]; in.eps = eps_a[i]; in.ro_a = ro_a_a[i];
+    in.ro_m = ro_m_a[i]; in.per_m = per_m_a[i]; in.th = th_a[i]; in.rest = rest_a[i];
+    in.sna = sna_a[i]; in.sk = sk_a[i]; in.sl = sl_a[i];
+    double ep[6], hp[12];
+    nrt_param::derive_element(in, myelin, e_max, ep, hp);
+    for (int q = 0; q < 6; q++) eparam[q * N + i] = ep[q];
     if (kind[i] == 1) {
-      const double ENa0 = 0.115 + rest, EK0 = -0.012 + rest;
-      double ENa, EK, lsna, lsk;
-      if (eps_s <= e_max) {
-        const double f = pow((eps_s / e_max), kNDamage);
-        ENa = ENa0 - f * (ENa0);
-        EK = EK0 - f * (EK0);
-        lsna = f * (ENa0);
-        lsk = f * (EK0);
-      } else {
-        ENa = 0;
-        EK = 0;
-        lsna = ENa0;
-        lsk = EK0;
-      }
-      const double gL = sl_a[i] * kPi * d / th;
-      double gNa = sna_a[i] * kPi * d / th;
-      double gK = sk_a[i] * kPi * d / th;
-      gNa = gNa / (sqrt(1 + eps));
-      gK = gK / (sqrt(1 + eps));
-      Rates r = rates(rest, rest, lsna, lsk);
-      const double m = r.am / (r.am + r.bm), h = r.ah / (r.ah + r.bh), nn = r.an / (r.an + r.bn);
-      const double EL = (gNa * m * m * m * h * (rest - ENa) + gK * nn * nn * nn * nn * (rest - EK) +
-                         gL * rest) / gL;
       hh_elem[k] = (int32_t)i;
-      const double vals[12] = {m, h, nn, gNa, gK, gL, ENa, EK, EL, lsna, lsk, rest};
-      for (int q = 0; q < 12; q++) hparam[q * H + k] = vals[q];
+      for (int q = 0; q < 12; q++) hparam[q * H + k] = hp[q];
       k++;
-      crit = (2 * r_a * c_m * dX * dX) / 4;
-    } else {
-      if (myelin) {
-        double temp = 0;
-        for (int l = 1; l <= kLayersMy; l++) temp = temp + 1 / (d + th * 2 + 2 * (l - 1) * kThMy);
-        const double c_my = 1 / (kThMy * temp / (kPerMy * kPi));
-        const double r_my = (kRoMy * kThMy * temp) / kPi;
-        r_m = r_m + r_my;
-        c_m = (c_m * c_my) / (c_my + c_m);
-      }
-      W = -1 / r_m;
-      K = rest / r_m;
-      crit = (2 * r_a * c_m * dX * dX) / (4 + (r_a * dX * dX) / r_m);
     }
-    eparam[0 * N + i] = c_m;
-    eparam[1 * N + i] = r_a;
-    eparam[2 * N + i] = dX;
-    eparam[3 * N + i] = W;
-    eparam[4 * N + i] = K;
-    eparam[5 * N + i] = crit;
   }
   double t = eparam[5 * N + 1];
   for (size_t i = 2; i < N - 1; i++)

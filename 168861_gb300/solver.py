@@ -64,6 +64,43 @@ def derive(spec) -> Derived:
     return Derived(ep, he[:nh].copy(), hparam, crit.value)
 
 
+def derive_batch(specs) -> list:
+    """The parameter pipeline for many trees in one GPU call (nrt_derive_batch); the same
+    results as derive() per tree up to the last bits of the device's math."""
+    lib = _lib.load()
+    count = len(specs)
+    sizes = np.array([sp.n for sp in specs], np.int64)
+    off = np.zeros(count + 1, np.int64)
+    off[1:] = np.cumsum(sizes)
+    T = int(off[-1])
+    isp = np.empty((5, T), np.int32)
+    dsp = np.empty((12, T))
+    for k, sp in enumerate(specs):
+        isp[:, off[k]:off[k + 1]] = sp.ispec().reshape(5, -1)
+        dsp[:, off[k]:off[k + 1]] = sp.dspec().reshape(12, -1)
+    my = np.array([int(sp.myelin) for sp in specs], np.int32)
+    em = np.array([float(sp.e_max) for sp in specs])
+    ep = np.empty((6, T))
+    hoff = np.zeros(count + 1, np.int64)
+    nh = int(sum(int(np.count_nonzero(sp.kind == 1)) for sp in specs))
+    he = np.empty(max(nh, 1), np.int32)
+    hp = np.empty((12, max(nh, 1)))
+    crit = np.empty(count)
+    check(lib.nrt_derive_batch(count, _p(off, ctypes.c_int64), _p(isp, ctypes.c_int32),
+                               _p(dsp, ctypes.c_double), _p(my, ctypes.c_int32),
+                               _p(em, ctypes.c_double), _p(ep, ctypes.c_double),
+                               _p(he, ctypes.c_int32), _p(hp, ctypes.c_double),
+                               _p(hoff, ctypes.c_int64), _p(crit, ctypes.c_double)),
+          "nrt_derive_batch")
+    out = []
+    for k in range(count):
+        a, b = int(off[k]), int(off[k + 1])
+        h0, h1 = int(hoff[k]), int(hoff[k + 1])
+        out.append(Derived(np.ascontiguousarray(ep[:, a:b]), he[h0:h1].copy(),
+                           np.ascontiguousarray(hp[:, h0:h1]), float(crit[k])))
+    return out
+
+
 def step_size(spec, d: Derived) -> float:
     """dT = dtf * critical dT, or the spec's absolute step (src/neurite.cpp:171-173)."""
     return spec.dt_abs if spec.dt_abs > 0 else d.dT_crit * spec.dtf

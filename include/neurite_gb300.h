@@ -198,6 +198,20 @@ int nrt_derive(int32_t n, const int32_t *ispec, const double *dspec, int32_t mye
                double e_max, double *eparam, int32_t *hh_elem, double *hparam,
                int32_t *num_hh_out, double *dT_crit_out);
 
+/* The same pipeline on the GPU for many trees in one call (one CTA per tree), for front
+ * ends that admit thousands of trees at once.  Trees are packed back to back: tree t owns
+ * elements [offsets[t], offsets[t+1]) of ispec [5][total] and dspec [12][total] (nrt_derive's
+ * rows, each spanning all trees; total = offsets[count]).  myelin and e_max are per tree.
+ * Outputs: eparam [6][total], hh_offsets [count + 1] (tree t's HH elements are
+ * [hh_offsets[t], hh_offsets[t+1]) of hh_elem and of hparam's rows), hh_elem (indices local
+ * to the tree), hparam [12][hh_offsets[count]], dT_crit [count].  All arrays are host
+ * memory; the call allocates and frees its device buffers.  Results are nrt_derive's up
+ * to the last bits of the device's exp, pow, sqrt and fused multiply-adds. */
+int nrt_derive_batch(int32_t count, const int64_t *offsets, const int32_t *ispec,
+                     const double *dspec, const int32_t *myelin, const double *e_max,
+                     double *eparam, int32_t *hh_elem, double *hparam, int64_t *hh_offsets,
+                     double *dT_crit);
+
 /* ----------------------------------------------------------------------------------
  * Batches: many independent trees of uneven size advanced together, one persistent
  * block-per-instance launch per chunk of steps.  Each instance keeps its own dT,
