@@ -16,7 +16,7 @@ import dataclasses
 
 import numpy as np
 
-from . import _lib
+from . import _lib, model
 from ._lib import check
 
 _PREC = {"fp64": _lib.NRT_FP64, "mixed": _lib.NRT_MIXED}
@@ -75,9 +75,13 @@ def derive_batch(specs) -> list:
     T = int(off[-1])
     isp = np.empty((5, T), np.int32)
     dsp = np.empty((12, T))
-    for k, sp in enumerate(specs):
-        isp[:, off[k]:off[k + 1]] = sp.ispec().reshape(5, -1)
-        dsp[:, off[k]:off[k + 1]] = sp.dspec().reshape(12, -1)
+    rows_i, rows_d = model.ISPEC_ROWS, model.DSPEC_ROWS
+    for k, sp in enumerate(specs):  # one copy per row, straight into the packed arrays
+        a, b = off[k], off[k + 1]
+        for r, name in enumerate(rows_i):
+            isp[r, a:b] = getattr(sp, name)
+        for r, name in enumerate(rows_d):
+            dsp[r, a:b] = getattr(sp, name)
     my = np.array([int(sp.myelin) for sp in specs], np.int32)
     em = np.array([float(sp.e_max) for sp in specs])
     ep = np.empty((6, T))
@@ -93,11 +97,10 @@ def derive_batch(specs) -> list:
                                _p(hoff, ctypes.c_int64), _p(crit, ctypes.c_double)),
           "nrt_derive_batch")
     out = []
-    for k in range(count):
+    for k in range(count):  # views into the packed results
         a, b = int(off[k]), int(off[k + 1])
         h0, h1 = int(hoff[k]), int(hoff[k + 1])
-        out.append(Derived(np.ascontiguousarray(ep[:, a:b]), he[h0:h1].copy(),
-                           np.ascontiguousarray(hp[:, h0:h1]), float(crit[k])))
+        out.append(Derived(ep[:, a:b], he[h0:h1], hp[:, h0:h1], float(crit[k])))
     return out
 
 
