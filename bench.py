@@ -246,13 +246,13 @@ def algorithmic_bytes_implicit(probs, steps: int, iters, counts):
       It counts no preconditioner and no refinement residual.
 
     passes: what this kernel's passes must move per row, counted per pass:
-      assembly (HH 89 / passive 81 B: rowf 1, V^n 8, V^n-1 8, c_m dX/dT 8, 1/(r_a dX) 8,
-        class index 4, gates r/w 24 or W dX, K dX 16; writes diagonal 8 + 4, c 4, b 8, W_0 4),
+      assembly (HH 85 / passive 77 B: rowf 1, V^n 8, V^n-1 8, c_m dX/dT 8, 1/(r_a dX) 8,
+        class index 4, gates r/w 24 or W dX, K dX 16; writes diagonal 8, c 4, b 8, W_0 4),
       tree factorisation 21 (slot row 4, flag 1, conductance 4, c 4; 1/pivot 4, e 4),
       each later FP64 residual 37 (b 8, rowf 1, diagonal 8, conductance 8, x 8; W_0 4),
       each preconditioner application 38 (two passes: slot rows and flags twice 10, e twice
         8, 1/pivot 4, input 4, eliminated side 4 + 4, output 4),
-      each Arnoldi step j: SpMV 17 (rowf, diagonal, conductance, Z_j, y) + products and
+      each Arnoldi step j: SpMV 17 (rowf, c, conductance, Z_j, y) + products and
         update 8 (j + 1) + 8, and its share of the solution update 4,
       each solution update 17 (rowf 1, V r/w 16), plus V^n 8 once per step for x0.
     Neighbour values come from cache; topology records of branch rows and the
@@ -264,7 +264,7 @@ def algorithmic_bytes_implicit(probs, steps: int, iters, counts):
         asm_rule = n_hh * (24 + 24 + ph) + (n - n_hh) * (24 + pp)
         I, B = float(iters[k]), float(counts["basis"][k])
         rule += asm_rule + n * (36 * I + 4 * (2 * B + I)) / steps
-        asm = n_hh * 89 + (n - n_hh) * 81
+        asm = n_hh * 85 + (n - n_hh) * 77
         per_run = (37 * counts["residuals"][k] + 38 * counts["applies"][k]
                    + (17 + 8 + 4) * I + 8 * B + 17 * counts["xupdates"][k])
         passes += asm + n * (21 + 8) + n * per_run / steps
