@@ -417,11 +417,13 @@ __device__ __forceinline__ TreeTile<T> tree_tile(const Shared &S, int cap) {
 // arrays (null sources are skipped) into the tile, then waits for them.  s0 is a multiple
 // of 16 slots and the slot arrays are padded, so every copy starts 16-byte aligned and
 // its size rounded up to 16 bytes stays inside the arrays and the tile.
+// Tile q_next (-1: none) is the one this CTA stages after this one: its arrays are
+// prefetched into L2 while this tile is worked on.
 template <typename T>
 __device__ __forceinline__ void tile_bulk_load(const ImView &iv, const Shared &S,
                                                const TreeTile<T> &t, int s0, int cnt,
                                                const T *x0, T *d0, const T *x1, T *d1,
-                                               const T *x2, T *d2) {
+                                               const T *x2, T *d2, int q_next = -1) {
   const uint32_t nt = ((uint32_t)cnt * sizeof(T) + 15u) & ~15u;
   const uint32_t nr = ((uint32_t)cnt * 4u + 15u) & ~15u;
   const uint32_t nf = ((uint32_t)cnt + 15u) & ~15u;
@@ -434,6 +436,15 @@ __device__ __forceinline__ void tile_bulk_load(const ImView &iv, const Shared &S
     if (x0) bulk_load(d0, x0 + s0, nt, S.bar);
     if (x1) bulk_load(d1, x1 + s0, nt, S.bar);
     if (x2) bulk_load(d2, x2 + s0, nt, S.bar);
+    if (q_next >= 0) {
+      const int s1 = iv.tile_slot[q_next], c1 = iv.tile_slot[q_next + 1] - s1;
+      const uint32_t mt = ((uint32_t)c1 * sizeof(T) + 15u) & ~15u;
+      prefetch_l2(iv.srow + s1, ((uint32_t)c1 * 4u + 15u) & ~15u);
+      prefetch_l2(iv.sflag + s1, ((uint32_t)c1 + 15u) & ~15u);
+      if (x0) prefetch_l2(x0 + s1, mt);
+      if (x1) prefetch_l2(x1 + s1, mt);
+      if (x2) prefetch_l2(x2 + s1, mt);
+    }
   }
   const uint32_t ph = (uint32_t)S.flag[2];
   mbar_wait(S.bar, ph, iv.err);
@@ -690,8 +701,9 @@ __device__ __noinline__ void tree_factor(Ctx<T, kGrid> c) {
   for (int e = c.l0; e < c.l1; e++) {
     for (int q = iv.lev_tile[e]; q < iv.lev_tile[e + 1]; q++) {
       const int s0 = iv.tile_slot[q], cnt = iv.tile_slot[q + 1] - s0;
+      const int qn = q + 1 < iv.lev_tile[c.l1] ? q + 1 : -1;
       tile_bulk_load<T>(iv, S, t, s0, cnt, (const T *)iv.sg, t.b, nullptr, nullptr, nullptr,
-                        nullptr);
+                        nullptr, qn);
       tile_gather(t.a, t.r, (const T *)iv.cdiag, cnt);  // c of every slot's row
       __syncthreads();
       for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {
@@ -728,8 +740,9 @@ __device__ __noinline__ void tree_apply(Ctx<T, kGrid> c, const T *v, T *z) {
   for (int e = c.l0; e < c.l1; e++) {
     for (int q = iv.lev_tile[e]; q < iv.lev_tile[e + 1]; q++) {
       const int s0 = iv.tile_slot[q], cnt = iv.tile_slot[q + 1] - s0;
+      const int qn = q + 1 < iv.lev_tile[c.l1] ? q + 1 : -1;
       tile_bulk_load<T>(iv, S, t, s0, cnt, (const T *)iv.se, t.b, nullptr, nullptr, nullptr,
-                        nullptr);
+                        nullptr, qn);
       tile_gather(t.a, t.r, v, cnt);
       __syncthreads();
       for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {
@@ -756,8 +769,11 @@ __device__ __noinline__ void tree_apply(Ctx<T, kGrid> c, const T *v, T *z) {
   for (int e = c.l1 - 1; e >= c.l0; e--) {
     for (int q = iv.lev_tile[e]; q < iv.lev_tile[e + 1]; q++) {
       const int s0 = iv.tile_slot[q], cnt = iv.tile_slot[q + 1] - s0;
+      // next: the following tile of this level, else the first tile of the level above
+      const int qn = q + 1 < iv.lev_tile[e + 1] ? q + 1
+                                                : (e > c.l0 ? iv.lev_tile[e - 1] : -1);
       tile_bulk_load<T>(iv, S, t, s0, cnt, (const T *)iv.sy, t.a, (const T *)iv.se, t.b,
-                        (const T *)iv.sinv, t.d);
+                        (const T *)iv.sinv, t.d, qn);
       for (int k = threadIdx.x; k < cnt; k += blockDim.x) t.a[k] *= t.d[k];
       __syncthreads();
       for (int s = iv.tile_seg[q] + threadIdx.x; s < iv.tile_seg[q + 1]; s += blockDim.x) {

@@ -35,6 +35,11 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
+// Asks for bytes [p, p + bytes) to be brought into L2 (no completion, no data returned);
+// 16-byte aligned address and size, like the bulk copies.
+__device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
 // One arrival on an mbarrier (a consumer releasing a buffer).
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
