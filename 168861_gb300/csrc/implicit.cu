@@ -929,12 +929,7 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
   double racc = 0;
   // gates of this precision (the mixed path keeps them in FP32)
   T *gate = sizeof(T) == 4 ? (T *)(void *)pv.gatef : (T *)(void *)pv.gate;
-  // x0 of the neighbours j-1 and j+1 comes from the neighbouring lanes (consecutive rows);
-  // the loop runs warp-uniformly so that every lane takes part in the shuffles
-  static_assert(kA == 1, "the neighbour shuffles assume one row per thread");
-  const int lane = threadIdx.x & 31;
-  for (int64_t wb = c.r0 + (threadIdx.x - lane); wb < c.r1; wb += stride) {
-    const int64_t rb = wb + lane;
+  for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kA * stride) {
     uint8_t f[kA];
     double v[kA], vo[kA], cm[kA], gj[kA], gn[kA], inp[kA], xm[kA], xp[kA];
     int64_t hc[kA];
@@ -957,13 +952,8 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
       gj[u] = ok ? iv.g64[r] : 0.0;
       gn[u] = ok ? iv.g64[rp] : 0.0;
       inp[u] = 0.0;
-      // this row's x0 for the lanes beside it, also past this group's last row (a row's DR
-      // may belong to the next CTA of a cooperative launch)
-      const double x0s = r < N ? x0_of(Vin, Vout, r) : 0.0;
-      xm[u] = __shfl_up_sync(0xffffffffu, x0s, 1);
-      xp[u] = __shfl_down_sync(0xffffffffu, x0s, 1);
-      if (lane == 0) xm[u] = ok ? x0_of(Vin, Vout, rm) : 0.0;
-      if (lane == 31) xp[u] = ok ? x0_of(Vin, Vout, rp) : 0.0;
+      xm[u] = ok ? x0_of(Vin, Vout, rm) : 0.0;
+      xp[u] = ok ? x0_of(Vin, Vout, rp) : 0.0;
     }
 #pragma unroll
     for (int u = 0; u < kA; u++) {
