@@ -17,6 +17,7 @@ NRT_FP64, NRT_MIXED = 0, 1
 NRT_GMRES, NRT_BICGSTAB = 0, 1
 NRT_PRECOND_NONE, NRT_PRECOND_JACOBI, NRT_PRECOND_SEGMENT, NRT_PRECOND_TREE = 0, 1, 2, 3
 NRT_TOL_ABS, NRT_TOL_REL = 0, 1
+NRT_BACKWARD_EULER, NRT_CRANK_NICOLSON = 0, 1
 
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _f64p = ctypes.POINTER(ctypes.c_double)
@@ -41,7 +42,8 @@ class Options(ctypes.Structure):
         ("precond", ctypes.c_int32), ("restart", ctypes.c_int32), ("tol_mode", ctypes.c_int32),
         ("tol", ctypes.c_double), ("max_iter", ctypes.c_int32), ("device", ctypes.c_int32),
         ("use_graphs", ctypes.c_int32), ("schedule", ctypes.c_int32),
-        ("tiled", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5),
+        ("tiled", ctypes.c_int32), ("scheme", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 4),
     ]
 
 

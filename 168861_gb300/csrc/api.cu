@@ -705,6 +705,8 @@ static int check_options(const nrt_options *o, std::string &why) {
   if (o->restart < 1 || o->restart > nrt::kMaxRestart) return (why = "restart must be in [1, 32]", NRT_EINVAL);
   if (!(o->tol > 0)) return (why = "tol must be > 0", NRT_EINVAL);
   if (o->max_iter < 0) return (why = "max_iter must be >= 0", NRT_EINVAL);
+  if (o->scheme != NRT_BACKWARD_EULER && o->scheme != NRT_CRANK_NICOLSON)
+    return (why = "bad scheme", NRT_EINVAL);
   return NRT_OK;
 }
 

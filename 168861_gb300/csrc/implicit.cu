@@ -96,6 +96,7 @@ struct ImView {
   int64_t ntot;
   int m;             // GMRES restart (BiCGSTAB: sizes the shared work vectors only)
   int krylov;        // NRT_GMRES or NRT_BICGSTAB
+  int scheme;        // NRT_BACKWARD_EULER or NRT_CRANK_NICOLSON
   int precond;
   int tol_mode;
   double tol;
@@ -929,9 +930,10 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
   double racc = 0;
   // gates of this precision (the mixed path keeps them in FP32)
   T *gate = sizeof(T) == 4 ? (T *)(void *)pv.gatef : (T *)(void *)pv.gate;
+  const bool cn = iv.scheme == NRT_CRANK_NICOLSON;
   for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kA * stride) {
     uint8_t f[kA];
-    double v[kA], vo[kA], cm[kA], gj[kA], gn[kA], inp[kA], xm[kA], xp[kA];
+    double v[kA], vo[kA], cm[kA], gj[kA], gn[kA], inp[kA], xm[kA], xp[kA], vm[kA], vp[kA];
     int64_t hc[kA];
     T g0[kA], g1[kA], g2[kA];
     // every load that does not depend on the row's flags goes out in this first round
@@ -954,6 +956,8 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
       inp[u] = 0.0;
       xm[u] = ok ? x0_of(Vin, Vout, rm) : 0.0;
       xp[u] = ok ? x0_of(Vin, Vout, rp) : 0.0;
+      vm[u] = ok && cn ? Vin[rm] : 0.0;  // Crank-Nicolson: V^n of the neighbours
+      vp[u] = ok && cn ? Vin[rp] : 0.0;
     }
 #pragma unroll
     for (int u = 0; u < kA; u++) {
@@ -1002,24 +1006,39 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
         c.w.Wb[r] = 0;
         continue;
       }
-      const double cj = cm[u] - wdx;
-      double d = cj, gl = 0.0, xl = 0.0, xmo = xm[u];
+      // backward Euler: c = c_m dX/dT - W dX; Crank-Nicolson (doubled): 2 c_m dX/dT - W dX
+      const double cj = (cn ? 2.0 * cm[u] : cm[u]) - wdx;
+      double d = cj, gl = 0.0, xl = 0.0, xmo = xm[u], vmo = vm[u], vl = 0.0;
       if (f[u] & (R_DOWNL | R_FAR)) {
         const Topo t = pv.topo[r];
         if (f[u] & R_DOWNL) {
           gl = iv.g64[t.dl];
           xl = x0_of(Vin, Vout, t.dl);
+          if (cn) vl = Vin[t.dl];
           d += gl;
         }
-        if (f[u] & R_FAR) xmo = x0_of(Vin, Vout, t.mother);
+        if (f[u] & R_FAR) {
+          xmo = x0_of(Vin, Vout, t.mother);
+          if (cn) vmo = Vin[t.mother];
+        }
       }
       if (f[u] & R_DOWNR) d += gn[u];
       if (f[u] & R_UP) d += gj[u];
       iv.diag[r] = d;
       cdiag[r] = (T)cj;
       if (active && (f[u] & R_INP)) inp[u] = iv.inp64[r];  // one row or a few per tree
-      double b = cm[u] * v[u] + kdx;
-      if (active) b += inp[u];
+      double b;
+      if (!cn) {
+        b = cm[u] * v[u] + kdx;
+        if (active) b += inp[u];
+      } else {  // (2 c_m dX/dT + W dX) V^n - sum g (V^n - V^n_q) + 2 (K dX + I)
+        b = (2.0 * cm[u] + wdx) * v[u];
+        if (f[u] & R_UP) b -= gj[u] * (v[u] - vmo);
+        if (f[u] & R_DOWNR) b -= gn[u] * (v[u] - vp[u]);
+        if (f[u] & R_DOWNL) b -= gl * (v[u] - vl);
+        b += 2.0 * kdx;
+        if (active) b += 2.0 * inp[u];
+      }
       iv.rhs[r] = b;
       bacc += (T)b * (T)b;
       // r = b - A x0, in the order of row_apply: diagonal, mother, DR, DL
@@ -2143,6 +2162,7 @@ int Engine::implicit_init() {
   iv.m = opt.restart;
   iv.precond = opt.precond;
   iv.krylov = opt.krylov;
+  iv.scheme = opt.scheme;
   iv.tol_mode = opt.tol_mode;
   iv.tol = opt.tol;
   iv.max_iter = opt.max_iter;

@@ -250,7 +250,8 @@ class ProblemArrays:
 def make_options(mode: int, precision: str = "fp64", krylov: str = "gmres",
                  precond: str = "tree", restart: int = 30, tol: float = 1e-14,
                  tol_mode: str = "abs", max_iter: int = 0, use_graphs: bool = True,
-                 device: int = -1, schedule: int = 0, tiled: bool = True) -> _lib.Options:
+                 device: int = -1, schedule: int = 0, tiled: bool = True,
+                 scheme: str = "be") -> _lib.Options:
     lib = _lib.load()
     o = _lib.Options()
     check(lib.nrt_options_default(ctypes.byref(o)), "nrt_options_default")
@@ -266,6 +267,7 @@ def make_options(mode: int, precision: str = "fp64", krylov: str = "gmres",
     o.device = device
     o.schedule = int(schedule)
     o.tiled = int(bool(tiled))
+    o.scheme = {"be": _lib.NRT_BACKWARD_EULER, "cn": _lib.NRT_CRANK_NICOLSON}[scheme]
     return o
 
 

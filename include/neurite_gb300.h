@@ -65,6 +65,15 @@ typedef enum nrt_precond {
                                 about one iteration per refinement cycle */
 } nrt_precond;
 
+/* Implicit time discretisation.  The reference is backward Euler only
+ * (src/solverIm-cpu.cpp:83,115).  Crank-Nicolson applies the trapezoidal rule to the same
+ * operator: with A = C/dT + L the backward-Euler matrix and b = C/dT V^n + K dX + I, it
+ * solves (A + C/dT) x = 2 b + C/dT V^n - A V^n (gates, W and K as in backward Euler). */
+typedef enum nrt_scheme {
+  NRT_BACKWARD_EULER = 0,
+  NRT_CRANK_NICOLSON = 1
+} nrt_scheme;
+
 typedef enum nrt_tol_mode {
   NRT_TOL_ABS = 0,        /* ||b - A x||_2 <= tol (the reference's test, RANGE_ERROR 1e-14) */
   NRT_TOL_REL = 1         /* ||b - A x||_2 <= tol * ||b||_2 over the physical rows */
@@ -114,7 +123,9 @@ typedef struct nrt_options {
   int32_t tiled;                 /* mixed explicit: 1 (default) = element arrays staged into
                                     shared memory by bulk copies, tile by tile; 0 = one
                                     thread per element loading its own (same results) */
-  int32_t reserved[5];
+  int32_t scheme;                /* implicit: NRT_BACKWARD_EULER (default, the reference's)
+                                    or NRT_CRANK_NICOLSON */
+  int32_t reserved[4];
 } nrt_options;
 
 typedef struct nrt_stats {

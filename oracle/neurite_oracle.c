@@ -403,11 +403,33 @@ out:
   return rc;
 }
 
+/* Crank-Nicolson from the backward-Euler system (not in the reference, which is backward
+ * Euler only).  With A = C/dT + L the reference's matrix (C/dT = c_m dX / dT on the
+ * diagonal, L the membrane and coupling terms) and b = C/dT V^n + K dX + I its right-hand
+ * side, the trapezoidal rule (C/dT + L/2) x = (C/dT - L/2) V^n + K dX + I, doubled, is
+ *   (A + C/dT) x = 2 b + C/dT V^n - A V^n
+ * on every row except the identity rows (a single unit entry), which stay as they are. */
+static void cn_from_be(int n, const int32_t *row_ptr, const int32_t *col, double *val, double *rhs,
+                       const double *Vn, const double *c_m, const double *dX, double dT) {
+  for (int j = 0; j < n; j++) {
+    if (row_ptr[j + 1] - row_ptr[j] == 1) continue;
+    const double cdt = c_m[j] * dX[j] / dT;
+    double av = 0;
+    int kd = -1;
+    for (int k = row_ptr[j]; k < row_ptr[j + 1]; k++) {
+      av += val[k] * Vn[col[k]];
+      if (col[k] == j) kd = k;
+    }
+    rhs[j] = 2 * rhs[j] + cdt * Vn[j] - av;
+    val[kd] += cdt;
+  }
+}
+
 int nro_implicit_run(int n, const int32_t *ispec, const double *eparam, const double *input_on,
                      int num_hh, const int32_t *hh_elem, double *hparam, double dT, int i_begin,
                      int i_end, double init_time, double end_input, double *V, double *Vother,
                      int linsolve, int record_every, int nprobe, const int32_t *probes,
-                     double *trace, int *nrec_out, long long *krylov_iters_out) {
+                     double *trace, int *nrec_out, long long *krylov_iters_out, int scheme) {
   if (n < 4) return NRO_EINVAL;
   size_t cap = (size_t)4 * n + 2;
   double *W = malloc(sizeof(double) * n), *K = malloc(sizeof(double) * n);
@@ -433,6 +455,9 @@ int nro_implicit_run(int n, const int32_t *ispec, const double *eparam, const do
     int nnz;
     rc = nro_implicit_matrix(n, ispec, eparam, W, K, input, dT, prevT, row_ptr, col, val, currT, &nnz);
     if (rc) goto out;
+    if (scheme == 1)
+      cn_from_be(n, row_ptr, col, val, currT, prevT, eparam + (size_t)EP_CM * n,
+                 eparam + (size_t)EP_DX * n, dT);
     if (linsolve == 0) {
       rc = nro_tree_solve(n, row_ptr, col, val, currT, currT);
     } else {

@@ -77,7 +77,7 @@ int nro_implicit_run(int n, const int32_t *ispec, const double *eparam, const do
                      int num_hh, const int32_t *hh_elem, double *hparam, double dT, int i_begin,
                      int i_end, double init_time, double end_input, double *V, double *Vother,
                      int linsolve, int record_every, int nprobe, const int32_t *probes,
-                     double *trace, int *nrec_out, long long *krylov_iters_out);
+                     double *trace, int *nrec_out, long long *krylov_iters_out, int scheme);
 
 #ifdef __cplusplus
 }

@@ -68,7 +68,7 @@ class Oracle:
         lib.nro_implicit_run.argtypes = [c_int, _i32p, _f64p, _f64p, c_int, _i32p, _f64p, c_double,
                                          c_int, c_int, c_double, c_double, _f64p, _f64p, c_int,
                                          c_int, c_int, _i32p, _f64p, ctypes.POINTER(c_int),
-                                         ctypes.POINTER(ctypes.c_longlong)]
+                                         ctypes.POINTER(ctypes.c_longlong), c_int]
         lib.nro_implicit_matrix.argtypes = [c_int, _i32p, _f64p, _f64p, _f64p, _f64p, c_double,
                                             _f64p, _i32p, _i32p, _f64p, _f64p, ctypes.POINTER(c_int)]
         lib.nro_tree_solve.argtypes = [c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
@@ -112,8 +112,10 @@ class Oracle:
         return V, trace[: nrec.value]
 
     def implicit_run(self, spec, d: Derived, dT: float, i_begin: int, i_end: int, V=None,
-                     Vother=None, linsolve: int = 0, record_every: int = 0, probes=()):
-        """Backward-Euler steps [i_begin, i_end); returns (V, Vother, trace, krylov_iters)."""
+                     Vother=None, linsolve: int = 0, record_every: int = 0, probes=(),
+                     scheme: int = 0):
+        """Implicit steps [i_begin, i_end): backward Euler (scheme 0, the reference's) or
+        Crank-Nicolson (scheme 1); returns (V, Vother, trace, krylov_iters)."""
         n = spec.n
         V = np.ascontiguousarray(spec.rest_pot.copy() if V is None else V, dtype=np.float64)
         Vo = np.ascontiguousarray(spec.rest_pot.copy() if Vother is None else Vother, dtype=np.float64)
@@ -128,7 +130,7 @@ class Oracle:
             d.num_hh, d.hh_elem if d.num_hh else np.zeros(1, np.int32),
             d.hparam if d.num_hh else np.zeros((12, 1)), dT, i_begin, i_end, spec.init_time,
             spec.end_input, V, Vo, linsolve, record_every, nprobe, probes, trace,
-            ctypes.byref(nrec), ctypes.byref(kit))
+            ctypes.byref(nrec), ctypes.byref(kit), int(scheme))
         if rc:
             raise RuntimeError(f"nro_implicit_run failed: {rc}")
         return V, Vo, trace[: nrec.value], kit.value

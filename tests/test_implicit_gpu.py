@@ -268,3 +268,74 @@ def test_pass_counts_follow_the_gmres_structure(gpu, pkg, model):
     np.testing.assert_array_equal(pc["residuals"], pc["xupdates"])
     assert (pc["xupdates"] >= 20).all()            # at least one update per step
     assert (pc["basis"] >= it).all() and (pc["basis"] <= it * (it + 1) // 2).all()
+
+
+@pytest.mark.parametrize("name", golden_names("i"))
+@pytest.mark.parametrize("precond", ["tree", "segment"])
+def test_crank_nicolson_fp64_matches_exact_solution(gpu, pkg, orc, name, precond):
+    """Crank-Nicolson (not in the reference) against the oracle's restatement, solved
+    exactly, at the FP64 bar."""
+    g = load_golden(name)
+    spec = g["spec"]
+    steps = int(g["numStepsT"]) - 2
+    s = pkg.SolverIm(problem(pkg, g), scheme="cn", **tight(precond=precond, max_iter=20000))
+    s.run(1, 1 + steps, spec.init_time, spec.end_input)
+    d = orc.derive(spec)
+    Vo, _, _, _ = orc.implicit_run(spec, d, float(g["dT"]), 1, 1 + steps, linsolve=0, scheme=1)
+    assert np.abs(s.snapshot() - Vo).max() < TOL_FP64
+    Vbe, _, _, _ = orc.implicit_run(spec, d, float(g["dT"]), 1, 1 + steps, linsolve=0)
+    assert np.abs(Vo - Vbe).max() > 1e-6   # a different scheme indeed
+    s.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_crank_nicolson_batch_and_cooperative(gpu, pkg, orc, model, precision):
+    specs = [model.random_tree(seed=s, n_target=n, dt=2.5e-5, tspan=1e-3)
+             for s, n in [(81, 2000), (82, 30000)]]
+    opts = tight(precond="tree") if precision == "fp64" else dict(
+        precision="mixed", restart=20, tol=1e-10, tol_mode="rel")
+    tol = TOL_FP64 if precision == "fp64" else TOL_MIXED
+    probs = [pkg.ProblemArrays.from_spec(sp, pkg.derive(sp)) for sp in specs]
+    steps = [20, 12]
+    b = pkg.Batch(probs, mode=1, scheme="cn", **opts)                 # block per instance
+    b.set_runs([(1, 1 + k, sp.init_time, sp.end_input) for k, sp in zip(steps, specs)])
+    b.advance(max(steps))
+    for q, sp in enumerate(specs):
+        Vo, _, _, _ = orc.implicit_run(sp, orc.derive(sp), sp.dt_abs, 1, 1 + steps[q],
+                                       linsolve=0, scheme=1)
+        assert np.abs(b.snapshot(q) - Vo).max() < tol
+        if q == 1:  # the large tree alone: the cooperative whole-GPU launch
+            s = pkg.SolverIm(probs[q], scheme="cn", **opts)
+            s.run(1, 1 + steps[q], sp.init_time, sp.end_input)
+            assert np.abs(s.snapshot() - Vo).max() < tol
+            s.close()
+    b.close()
+
+
+def test_crank_nicolson_system_matches_oracle(gpu, pkg, orc):
+    """nrt_export_system in Crank-Nicolson mode: the oracle's transform of the reference's
+    backward-Euler matrix (A + C/dT, 2 b + C/dT V^n - A V^n)."""
+    g = load_golden("im_ytree_d3")
+    spec = g["spec"]
+    be = pkg.SolverIm(problem(pkg, g), **tight())
+    cn = pkg.SolverIm(problem(pkg, g), scheme="cn", **tight())
+    rp, col, val, rhs = be.export_system(True)
+    rp2, col2, val2, rhs2 = cn.export_system(True)
+    np.testing.assert_array_equal(rp, rp2)
+    np.testing.assert_array_equal(col, col2)
+    d = orc.derive(spec)
+    n = spec.n
+    cdt = d.eparam[0] * d.eparam[2] / float(g["dT"])
+    V = spec.rest_pot.copy()
+    av = np.array([val[rp[j]:rp[j + 1]] @ V[col[rp[j]:rp[j + 1]]] for j in range(n)])
+    ident = (rp[1:] - rp[:-1]) == 1
+    want_val = val.copy()
+    want_rhs = rhs.copy()
+    for j in np.nonzero(~ident)[0]:
+        k = rp[j] + int(np.nonzero(col[rp[j]:rp[j + 1]] == j)[0][0])
+        want_val[k] += cdt[j]
+        want_rhs[j] = 2 * rhs[j] + cdt[j] * V[j] - av[j]
+    np.testing.assert_allclose(val2, want_val, rtol=1e-13, atol=0)
+    np.testing.assert_allclose(rhs2[~ident], want_rhs[~ident], rtol=1e-12, atol=1e-20)
+    be.close()
+    cn.close()
