@@ -272,12 +272,13 @@ def algorithmic_bytes_implicit(probs, steps: int, iters, counts):
 
 
 def plain_fp64_single(pkg, torch):
-    """The plain FP64 single-tree GPU path on the 2047-branch, ~2.6e5-element tree: the
-    drop-in solver in FP64 (GMRES(30), tolerance 1e-10 relative), 10 timed steps."""
+    """The plain FP64 single-tree GPU path of the depth-10 random binary tree workload
+    (2047 branches, ~2.6e5 elements, Crank-Nicolson as that workload specifies): the drop-in
+    solver in FP64 (GMRES(30), tolerance 1e-10 relative), 10 timed steps."""
     spec = pkg.model.random_binary_tree(depth=10, seed=2)
     p = pkg.ProblemArrays.from_spec(spec, pkg.derive(spec))
     s = pkg.SolverIm(p, precision="fp64", restart=30, tol=1e-10, tol_mode="rel", precond="tree",
-                     max_iter=2000)
+                     max_iter=2000, scheme="cn")
     s.run(1, 4, spec.init_time, spec.end_input)
     stream = torch.cuda.ExternalStream(s.stream())
     e0 = torch.cuda.Event(enable_timing=True)
@@ -292,7 +293,7 @@ def plain_fp64_single(pkg, torch):
     s.close()
     return {"value": spec.n * 10 / (ms / 1e3), "unit": METRIC, "elements": spec.n, "steps": 10,
             "ms_per_step": ms / 10, "config": "random binary tree depth 10 (2047 branches), dx 1 um, "
-            "HH everywhere, backward Euler, FP64 GMRES(30) tree-preconditioned, tol 1e-10 rel, "
+            "HH everywhere, Crank-Nicolson, FP64 GMRES(30) tree-preconditioned, tol 1e-10 rel, "
             "dt 0.01 ms", "krylov_iters": int(st.krylov_iters)}
 
 
