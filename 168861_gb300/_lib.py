@@ -81,6 +81,13 @@ class RecordConfig(ctypes.Structure):
                 ("max_spikes", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
 
+class StrainConfig(ctypes.Structure):
+    _fields_ = [("num_elem", ctypes.c_int32), ("instance", _i32p), ("element", _i32p),
+                ("kind", _i32p), ("dspec", _f64p), ("myelin", ctypes.c_int32),
+                ("e_max", ctypes.c_double), ("eps0", ctypes.c_double), ("eps1", ctypes.c_double),
+                ("t0", ctypes.c_double), ("t1", ctypes.c_double), ("reserved", ctypes.c_int32 * 4)]
+
+
 # Every symbol include/neurite_gb300.h declares.
 EXPORTS = (
     "nrt_options_default", "nrt_create", "nrt_update", "nrt_calculate", "nrt_snapshot", "nrt_run",
@@ -95,6 +102,7 @@ EXPORTS = (
     "nrt_batch_record_read", "nrt_batch_pass_counts", "nrt_get_state", "nrt_set_state",
     "nrt_batch_get_state", "nrt_batch_set_state", "nrt_batch_snapshot_all",
     "nrt_server_submit_recorded", "nrt_server_recording", "nrt_derive_batch",
+    "nrt_set_strain", "nrt_batch_set_strain",
 )
 
 _lib = None
@@ -162,6 +170,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "nrt_batch_get_state": [vp, ctypes.c_int32, _f64p, _f64p, _f64p, _f64p, _f64p],
         "nrt_batch_set_state": [vp, ctypes.c_int32, _f64p, _f64p, _f64p, _f64p, _f64p],
         "nrt_record": [vp, ctypes.POINTER(RecordConfig)],
+        "nrt_set_strain": [vp, ctypes.POINTER(StrainConfig)],
+        "nrt_batch_set_strain": [vp, ctypes.POINTER(StrainConfig)],
         "nrt_batch_record": [vp, ctypes.POINTER(RecordConfig)],
         "nrt_record_read": [vp, _i64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int32), _f64p],
         "nrt_batch_record_read": [vp, _i64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int32), _f64p],

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libneurite_gb300.so")
-SOURCES = ["api.cu", "explicit.cu", "implicit.cu", "derive.cpp", "serve.cpp", "static_solve.cu", "record.cu", "derive_device.cu"]
+SOURCES = ["api.cu", "explicit.cu", "implicit.cu", "derive.cpp", "serve.cpp", "static_solve.cu", "record.cu", "derive_device.cu", "strain.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -481,6 +481,8 @@ Engine::~Engine() {
   if (stream) cudaStreamSynchronize(stream);
   implicit_release();
   record_release();
+  strain_release();
+  for (void *p : extra_mem) cudaFree(p);
   arena.release();
   if (stream) cudaStreamDestroy(stream);
 }
@@ -602,6 +604,7 @@ int Engine::advance(int64_t steps) {
   if (opt.mode == NRT_IMPLICIT_BE) return implicit_advance(*this, steps);
   int64_t left = steps;
   while (left > 0 && needs_general()) {  // exact first step
+    if (strain) TRY(launch_strain_update(*this, 0, stream));
     TRY(step(0, -1));
     if (rec) TRY(launch_record_step(rec_view_host(), pv.inst, 0, V[cur], stream));
     TRY(launch_advance_base(pv.inst, pv.ninst, 1, stream));
@@ -614,6 +617,8 @@ int Engine::advance(int64_t steps) {
       NRT_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
       int rc = NRT_OK;
       for (int k = 0; k < kChunk && rc == NRT_OK; k++) {
+        if (strain) rc = launch_strain_update(*this, k, stream);
+        if (rc != NRT_OK) break;
         rc = launch_explicit_step(pv, opt.precision, false, k, -1, V[(cur + k) & 1],
                                   V[(cur + k + 1) & 1], Vf[(cur + k) & 1], Vf[(cur + k + 1) & 1],
                                   stream);
@@ -636,6 +641,7 @@ int Engine::advance(int64_t steps) {
     }
   }
   while (left > 0) {
+    if (strain) TRY(launch_strain_update(*this, 0, stream));
     TRY(step(0, -1));
     if (rec) TRY(launch_record_step(rec_view_host(), pv.inst, 0, V[cur], stream));
     TRY(launch_advance_base(pv.inst, pv.ninst, 1, stream));
@@ -1013,6 +1019,21 @@ int nrt_batch_set_state(nrt_batch *b, int32_t instance, const double *V, const d
   if (instance < 0 || instance >= b->eng.pv.ninst) return nrt::fail(NRT_EINVAL, "instance out of range");
   NRT_CUDA(cudaSetDevice(b->eng.device));
   return b->eng.set_state(instance, V, V_other, m, h, n);
+}
+
+int nrt_set_strain(nrt_solver *s, const nrt_strain_config *cfg) {
+  if (!s || !cfg) return nrt::fail(NRT_EINVAL, "null argument");
+  if (cfg->instance)
+    for (int32_t q = 0; q < cfg->num_elem; q++)
+      if (cfg->instance[q] != 0) return nrt::fail(NRT_EINVAL, "a solver has only instance 0");
+  NRT_CUDA(cudaSetDevice(s->eng.device));
+  return s->eng.strain_config(cfg);
+}
+
+int nrt_batch_set_strain(nrt_batch *b, const nrt_strain_config *cfg) {
+  if (!b || !cfg) return nrt::fail(NRT_EINVAL, "null argument");
+  NRT_CUDA(cudaSetDevice(b->eng.device));
+  return b->eng.strain_config(cfg);
 }
 
 int nrt_record(nrt_solver *s, const nrt_record_config *cfg) {

@@ -18,6 +18,7 @@ struct Arena {
 
 struct ImplicitState;  // implicit.cu
 struct RecState;       // record.cu
+struct StrainState;    // strain.cu
 
 struct Engine {
   nrt_options opt{};
@@ -37,6 +38,8 @@ struct Engine {
   std::vector<std::vector<float>> hostf;  // staging for FP32 uploads
   ImplicitState *im = nullptr;
   RecState *rec = nullptr;                // recording at probes, or null
+  StrainState *strain = nullptr;          // time-varying strain of some elements, or null
+  std::vector<void *> extra_mem;          // device tables that replaced the arena's (freed last)
 
   int init(const nrt_problem *probs, int32_t count, const nrt_options *o);
   int step(int k, int force);
@@ -62,8 +65,14 @@ struct Engine {
                       const std::vector<int64_t> &raw, const std::vector<int32_t> &sinst,
                       const std::vector<int32_t> &p0);
   void record_release();
+  // strain.cu
+  int strain_config(const nrt_strain_config *c);
+  void strain_release();
   ~Engine();
 };
+
+// strain.cu: the strained elements' coefficients for explicit step k
+int launch_strain_update(const Engine &e, int k, cudaStream_t st);
 
 // implicit.cu
 int implicit_advance(Engine &e, int64_t steps);

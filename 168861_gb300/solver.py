@@ -163,6 +163,31 @@ def _state_set(fn, h, args, st: State, where):
     check(fn(h, *args, *ptr), where)
 
 
+def _strain_config(spec_rows, instances, elements, kinds, myelin, e_max, eps0, eps1, t0, t1,
+                   keep):
+    el = np.ascontiguousarray(elements, dtype=np.int32)
+    kd = np.ascontiguousarray(kinds, dtype=np.int32)
+    ds = np.ascontiguousarray(spec_rows, dtype=np.float64)
+    keep += [el, kd, ds]
+    c = _lib.StrainConfig()
+    c.num_elem = len(el)
+    c.element = _p(el, ctypes.c_int32)
+    c.kind = _p(kd, ctypes.c_int32)
+    c.dspec = _p(ds, ctypes.c_double)
+    if instances is not None:
+        ins = np.ascontiguousarray(instances, dtype=np.int32)
+        keep.append(ins)
+        c.instance = _p(ins, ctypes.c_int32)
+    c.myelin, c.e_max = int(myelin), float(e_max)
+    c.eps0, c.eps1, c.t0, c.t1 = float(eps0), float(eps1), float(t0), float(t1)
+    return c
+
+
+def strain_rows(spec, elements) -> np.ndarray:
+    """The unstrained description of some elements of a tree (nrt_derive's dspec rows)."""
+    return np.ascontiguousarray(spec.dspec()[:, np.asarray(elements)])
+
+
 class _Recorder:
     """nrt_record / nrt_record_read (and the batch forms) for a handle."""
 
@@ -305,6 +330,15 @@ class Solver(_Recorder):
 
     def synchronize(self) -> None:
         check(self.lib.nrt_synchronize(self.h), "nrt_synchronize")
+
+    def set_strain(self, spec, elements, eps0: float, eps1: float, t0: float, t1: float) -> None:
+        """Strain of `elements` of `spec` (this solver's tree) ramping linearly from eps0 at
+        t0 to eps1 at t1 (nrt_set_strain); an empty list stops it."""
+        el = np.asarray(elements, dtype=np.int32)
+        keep = []
+        c = _strain_config(strain_rows(spec, el), None, el, spec.kind[el], spec.myelin,
+                           spec.e_max, eps0, eps1, t0, t1, keep)
+        check(self.lib.nrt_set_strain(self.h, ctypes.byref(c)), "nrt_set_strain")
 
     def get_state(self) -> State:
         return _state_get(self.lib.nrt_get_state, self.h, (), self.n, self.num_hh, "nrt_get_state")

@@ -267,6 +267,34 @@ int nrt_batch_pass_counts(nrt_batch *b, int64_t *residuals, int64_t *precond_app
 int nrt_batch_destroy(nrt_batch *b);
 
 /* ----------------------------------------------------------------------------------
+ * Time-varying strain (explicit stepper).  The reference applies a static strain once,
+ * before the run (src/init.cpp:235-254,320-333).  Here the listed elements follow
+ *   e(t) = e0 + (e1 - e0) (t - t0) / (t1 - t0), clamped to [t0, t1],
+ * and before each step of nrt_run / nrt_batch_advance (t = i dT) the static formulas are
+ * re-evaluated for them at e(t): the element length and diameter, r_a, c_m, r_m (with the
+ * 45-layer myelin when `myelin`), the damage shifts of E_Na, E_K and the left shifts, the
+ * channel conductances and E_L.  The gates are state and keep their values.  A constant
+ * ramp (e0 == e1) gives what a static strain of e0 gives.  Steps taken through
+ * nrt_update / nrt_calculate see the parameters as they were last set.  No reference
+ * counterpart (a time ramp is an extension). */
+typedef struct nrt_strain_config {
+  int32_t num_elem;              /* strained elements; 0 stops the ramp */
+  const int32_t *instance;       /* batch: instance of each element; NULL -> 0 */
+  const int32_t *element;        /* element index, local to its instance */
+  const int32_t *kind;           /* 1 HH / 0 cable, as in the tree */
+  const double *dspec;           /* [12][num_elem]: the elements' unstrained description in
+                                    nrt_derive's dspec rows (the epsilon row is ignored) */
+  int32_t myelin;                /* the tree's myelin flag (cables) */
+  double e_max;                  /* the damage threshold E_MAX */
+  double eps0, eps1;             /* strain at t0 and from t1 on */
+  double t0, t1;                 /* ramp window, s (t1 > t0) */
+  int32_t reserved[4];
+} nrt_strain_config;
+
+int nrt_set_strain(nrt_solver *s, const nrt_strain_config *cfg);
+int nrt_batch_set_strain(nrt_batch *b, const nrt_strain_config *cfg);
+
+/* ----------------------------------------------------------------------------------
  * State export / import, for checkpoints and for moving a tree between handles (serving
  * preemption).  The reference exports V only (Solver::snapshot, inc/solver.h:21) and keeps
  * its gates inside the Hodgkin_Huxley objects; no reference counterpart.

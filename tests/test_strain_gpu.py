@@ -1,0 +1,94 @@
+"""Time-varying strain on the explicit stepper (nrt_set_strain).
+
+- A constant ramp gives what the reference's static strain gives (the static problem is
+  derived on the host with the pipeline pinned to the reference).
+- A ramp matches the oracle re-deriving the strained elements at every step (its C
+  restatement of the reference's static formulas), carrying the gates as state.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def axon(model):
+    """A 3 mm squid axon of 300 compartments (HH everywhere), stimulated at one end."""
+    return model.straight_axon(n_comp=300, length=3e-3, dtf=0.8, tspan=4e-3)
+
+
+def segment(spec):
+    """The first third of the axon, where the action potential starts."""
+    return np.arange(1, spec.n // 3)
+
+
+def step_size(pkg, spec, seg, eps_max):
+    """Half the smaller critical step of the unstrained and the most strained tree."""
+    s2 = copy.deepcopy(spec)
+    s2.epsilon[seg] = eps_max
+    return 0.5 * min(pkg.derive(spec).dT_crit, pkg.derive(s2).dT_crit)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 1e-6)])
+def test_constant_ramp_equals_static_strain(gpu, pkg, model, precision, tol):
+    spec = axon(model)
+    seg = segment(spec)
+    dT = step_size(pkg, spec, seg, 0.15)
+    static = copy.deepcopy(spec)
+    static.epsilon[seg] = 0.15
+    a = pkg.SolverEx(pkg.ProblemArrays.from_spec(static, pkg.derive(static), dT),
+                     precision=precision)
+    b = pkg.SolverEx(pkg.ProblemArrays.from_spec(spec, pkg.derive(spec), dT), precision=precision)
+    b.set_strain(spec, seg, 0.15, 0.15, 0.0, 1.0)
+    b.set_state(a.get_state())  # the static problem's rest gates (hhIconds at the strain)
+    steps = 3000
+    a.run(1, 1 + steps, spec.init_time, spec.end_input)
+    b.run(1, 1 + steps, spec.init_time, spec.end_input)
+    sa, sb = a.get_state(), b.get_state()
+    assert np.abs(sa.V - sb.V).max() < tol
+    assert np.abs(sa.m - sb.m).max() < 1e3 * tol
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 1e-4)])
+def test_strain_ramp_matches_oracle(gpu, pkg, orc, model, precision, tol):
+    spec = axon(model)
+    seg = segment(spec)
+    dT = step_size(pkg, spec, seg, 0.2)
+    steps = 2000
+    t0, t1 = 100 * dT, 1500 * dT  # the ramp runs from step 100 to step 1500
+    s = pkg.SolverEx(pkg.ProblemArrays.from_spec(spec, pkg.derive(spec), dT), precision=precision)
+    s.set_strain(spec, seg, 0.0, 0.2, t0, t1)
+    s.run(1, 1 + steps, spec.init_time, spec.end_input)
+    got = s.snapshot()
+    s.close()
+    # the oracle: re-derive the tree at e(t) before every step; the gates are state
+    st = copy.deepcopy(spec)
+    d = orc.derive(st)
+    gates = d.hparam[:3].copy()
+    V = spec.rest_pot.copy()
+    for i in range(1, 1 + steps):
+        t = i * dT
+        e = 0.0 if t <= t0 else (0.2 if t >= t1 else 0.2 * ((t - t0) / (t1 - t0)))
+        st.epsilon[seg] = e
+        dd = orc.derive(st)
+        dd.hparam[:3] = gates
+        V, _ = orc.explicit_run(st, dd, dT, i, i + 1, V=V)
+        gates = dd.hparam[:3].copy()
+    assert np.abs(got - V).max() < tol
+    # and the strain made a difference
+    plain = pkg.SolverEx(pkg.ProblemArrays.from_spec(spec, pkg.derive(spec), dT),
+                         precision=precision)
+    plain.run(1, 1 + steps, spec.init_time, spec.end_input)
+    assert np.abs(plain.snapshot() - got).max() > 1e-5
+    plain.close()
+
+
+def test_strain_needs_the_explicit_stepper(gpu, pkg, model):
+    spec = model.random_tree(seed=3, n_target=1500, dt=2.5e-5, tspan=1e-3)
+    s = pkg.SolverIm(pkg.ProblemArrays.from_spec(spec, pkg.derive(spec)))
+    with pytest.raises(pkg.NeuriteError):
+        s.set_strain(spec, [5, 6], 0.0, 0.1, 0.0, 1e-3)
+    s.close()
