@@ -446,6 +446,15 @@ class Batch(_Recorder):
     def synchronize(self) -> None:
         check(self.lib.nrt_batch_synchronize(self.h), "nrt_batch_synchronize")
 
+    def set_strain(self, i: int, spec, elements, eps0: float, eps1: float, t0: float,
+                   t1: float) -> None:
+        """As Solver.set_strain, for `elements` of instance i (whose tree is `spec`)."""
+        el = np.asarray(elements, dtype=np.int32)
+        keep = []
+        c = _strain_config(strain_rows(spec, el), np.full(len(el), int(i), np.int32), el,
+                           spec.kind[el], spec.myelin, spec.e_max, eps0, eps1, t0, t1, keep)
+        check(self.lib.nrt_batch_set_strain(self.h, ctypes.byref(c)), "nrt_batch_set_strain")
+
     def get_state(self, i: int) -> State:
         p = self.problems[i]
         return _state_get(self.lib.nrt_batch_get_state, self.h, (int(i),), p.num_elem,

@@ -47,7 +47,7 @@ METRIC = "compartment-steps/s"
 TRAFFIC_PER_ELEMENT_STEP = {"batch-explicit-mixed": 1391.1e6 / 21910344,
                             "batch-implicit-mixed": 28.63e9 / (3 * 21910344)}
 WORKLOADS = ("batch-implicit-mixed", "batch-explicit-mixed", "batch-explicit-fp64",
-             "axon-explicit-fp64", "serve")
+             "axon-explicit-fp64", "myelin-explicit-mixed", "serve")
 DEFAULT_WORKLOAD = "batch-implicit-mixed"
 
 
@@ -118,10 +118,32 @@ def build_batch_problems(workload: str, count: int, seed: int, rank: int, world:
     return probs, runs, n_elem
 
 
+def myelin_workload(pkg):
+    """The myelinated axon: 200 nodes of Ranvier (1 um, HH at 10x density) between 1 mm
+    passive internodes (myelin Cm 0.005 uF/cm^2, Rm x1000), dx 1 um, with a strain ramp
+    0 -> 20% over 5 ms on the 5 mm segment in the middle.  Returns (spec, problem, segment),
+    dT = 0.8 of the smaller critical step of the unstrained and the fully strained axon."""
+    import copy
+    spec = pkg.model.myelinated_axon()
+    mid = spec.n // 2
+    seg = np.arange(mid - 2500, mid + 2500)
+    s2 = copy.deepcopy(spec)
+    s2.epsilon[seg] = 0.2
+    d = pkg.derive(spec)
+    dT = 0.8 * min(d.dT_crit, pkg.derive(s2).dT_crit)
+    return spec, pkg.ProblemArrays.from_spec(spec, d, dT), seg
+
+
 def workload_config(workload: str, count: int, precond: str = "tree"):
     if workload == "axon-explicit-fp64":
         return {"workload": "axon-explicit-fp64", "trees": 1, "elements_per_tree": 1002,
                 "mode": "explicit", "precision": "fp64", "dt": "0.8 dT_crit = 8e-4 ms"}
+    if workload == "myelin-explicit-mixed":
+        return {"workload": "myelin-explicit-mixed", "trees": 1,
+                "geometry": "200 nodes (1 um, HH x10) + 1 mm internodes, dx 1 um",
+                "mode": "explicit", "precision": "FP32 state + FP64 accumulator",
+                "strain": "ramp 0 -> 20% over 5 ms on the middle 5 mm",
+                "dt": "0.8 of the smaller critical step (unstrained, 20% strained)"}
     cfg = {"workload": workload, "trees": count, "elements_per_tree": "log-uniform 1e3-1e5",
            "depth": "4-12", "branching_prob": "0.6-0.9", "stimulus_nA": "U(0.5,3)",
            "strain": "U(0,0.15)"}
@@ -316,6 +338,7 @@ def run_ours(args, rank: int, world: int):
     W = max(3, args.warmup)
 
     t_build = time.time()
+    strained = None
     if wl == "axon-explicit-fp64":
         spec = pkg.model.straight_axon(dtf=0.8)
         d = pkg.derive(spec)
@@ -323,6 +346,12 @@ def run_ours(args, rank: int, world: int):
         probs = [pkg.ProblemArrays.from_spec(spec, d, dT)]
         runs = [(1, spec.num_steps(dT) - 1, spec.init_time, spec.end_input)]
         n_elem = spec.n
+    elif wl == "myelin-explicit-mixed":
+        spec, p, seg = myelin_workload(pkg)
+        probs = [p]
+        runs = [(1, spec.num_steps(p.dT) - 1, spec.init_time, spec.end_input)]
+        n_elem = spec.n
+        strained = (spec, seg)
     else:
         probs, runs, n_elem = build_batch_problems(wl, count, args.seed, rank, world)
     t_build = time.time() - t_build
@@ -341,6 +370,8 @@ def run_ours(args, rank: int, world: int):
     t0 = time.perf_counter()
     b = pkg.Batch(probs, mode=mode, **opts)
     b.set_runs(runs)
+    if strained:
+        b.set_strain(0, strained[0], strained[1], 0.0, 0.2, 0.0, 5e-3)
     b.advance(K)
     outs = b.snapshot_all()
     torch.cuda.synchronize()
@@ -353,6 +384,8 @@ def run_ours(args, rank: int, world: int):
     # ---- device-resident throughput
     b = pkg.Batch(probs, mode=mode, **opts)
     b.set_runs(runs)
+    if strained:
+        b.set_strain(0, strained[0], strained[1], 0.0, 0.2, 0.0, 5e-3)
     stream = torch.cuda.ExternalStream(b.stream())
     b.advance(W)
     b.synchronize()
@@ -409,7 +442,8 @@ def run_ours(args, rank: int, world: int):
                        "frac": a2 / peak, "bytes_per_step": passes_all}
     # our kernels launched in the timed region: one persistent launch + one loop-index
     # update per 64-step chunk (implicit); 64 step launches + 1 update per graph (explicit)
-    launches = 2 * math.ceil(K / 64) if implicit else K + math.ceil(K / 64)
+    launches = (2 * math.ceil(K / 64) if implicit
+                else K * (2 if strained else 1) + math.ceil(K / 64))  # + the strain update
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms / K, "higher_is_better": True,
@@ -547,6 +581,8 @@ def _oracle_job(job):
     model = importlib.import_module("168861_gb300.model")
     if wl == "axon-explicit-fp64":
         spec = model.straight_axon(dtf=0.8)
+    elif wl == "myelin-explicit-mixed":  # a scaled axon (20 nodes), as the oracle can cover
+        spec = model.myelinated_axon(n_nodes=20)
     else:
         spec = model.random_tree(seed=tseed, n_target=size)
     orc = O.Oracle()
@@ -564,6 +600,9 @@ def _sample_jobs(wl: str, seed: int, count: int, cores: int):
     """About 10-20 s of CPU work spread over `cores` processes."""
     if wl == "axon-explicit-fp64":
         return [(wl, 0, 1002, 12000)] * cores, "1002-element axon, 12000 steps per process"
+    if wl == "myelin-explicit-mixed":
+        return ([(wl, 0, 0, 400)] * cores,
+                "20-node myelinated axon (~2e4 elements, no strain ramp), 400 steps per process")
     pop = tree_population(count, seed)
     if wl.startswith("batch-implicit"):
         # unpreconditioned GMRES(150) to 1e-14 (the reference's solve) on the smallest trees,
