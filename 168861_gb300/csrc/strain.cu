@@ -107,7 +107,9 @@ __global__ void strain_update(StrainView s, PackView p, int k, int mixed) {
 int launch_strain_update(const Engine &e, int k, cudaStream_t st) {
   const StrainView &v = e.strain->view;
   if (v.n <= 0) return NRT_OK;
-  strain_update<<<(v.n + 127) / 128, 128, 0, st>>>(v, e.pv, k, e.opt.precision == NRT_MIXED);
+  // one warp per block: the FP64 re-derivation is bound by each SM's FP64 pipe, so the
+  // elements are spread over as many SMs as there are warps of them
+  strain_update<<<(v.n + 31) / 32, 32, 0, st>>>(v, e.pv, k, e.opt.precision == NRT_MIXED);
   NRT_CUDA(cudaGetLastError());
   return NRT_OK;
 }
