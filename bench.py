@@ -601,8 +601,8 @@ def _sample_jobs(wl: str, seed: int, count: int, cores: int):
     if wl == "axon-explicit-fp64":
         return [(wl, 0, 1002, 12000)] * cores, "1002-element axon, 12000 steps per process"
     if wl == "myelin-explicit-mixed":
-        return ([(wl, 0, 0, 20000)] * cores,
-                "20-node myelinated axon (~2e4 elements, no strain ramp), 20000 steps per process")
+        return ([(wl, 0, 0, 200000)] * cores,
+                "20-node myelinated axon (~2e4 elements, no strain ramp), 2e5 steps per process")
     pop = tree_population(count, seed)
     if wl.startswith("batch-implicit"):
         # unpreconditioned GMRES(150) to 1e-14 (the reference's solve) on the smallest trees,
