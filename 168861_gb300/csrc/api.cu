@@ -616,8 +616,11 @@ int Engine::advance(int64_t steps) {
       cudaGraph_t g;
       NRT_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
       int rc = NRT_OK;
+      const bool tabled = strain_tabled(*this);
+      if (tabled) rc = launch_strain_derive(*this, kChunk, stream);
       for (int k = 0; k < kChunk && rc == NRT_OK; k++) {
-        if (strain) rc = launch_strain_update(*this, k, stream);
+        if (strain)
+          rc = tabled ? launch_strain_apply(*this, k, stream) : launch_strain_update(*this, k, stream);
         if (rc != NRT_OK) break;
         rc = launch_explicit_step(pv, opt.precision, false, k, -1, V[(cur + k) & 1],
                                   V[(cur + k + 1) & 1], Vf[(cur + k) & 1], Vf[(cur + k + 1) & 1],

@@ -71,8 +71,13 @@ struct Engine {
   ~Engine();
 };
 
-// strain.cu: the strained elements' coefficients for explicit step k
+// strain.cu: the strained elements' coefficients for explicit step k, derived and written
+// in one launch; or, in a graph chunk, derived ahead for steps 0 .. nk-1 in one launch
+// (when strain_tabled) and written by one launch per step
 int launch_strain_update(const Engine &e, int k, cudaStream_t st);
+bool strain_tabled(const Engine &e);
+int launch_strain_derive(const Engine &e, int nk, cudaStream_t st);
+int launch_strain_apply(const Engine &e, int k, cudaStream_t st);
 
 // implicit.cu
 int implicit_advance(Engine &e, int64_t steps);

@@ -10,6 +10,8 @@
 // column of each HH element (each strained HH element gets a column of its own).  The
 // gates are state: strain changes their rates, not their values.
 #include <algorithm>
+#include <cstring>
+#include <memory>
 #include <vector>
 
 #include "derive_elem.h"
@@ -17,13 +19,21 @@
 
 namespace nrt {
 
+// The strained elements are grouped into classes of identical input columns (instance,
+// kind and the ten description values): the derivation is a pure function of those and
+// of t, so one evaluation per class gives every member bit for bit what its own would.
+// Elements are stored sorted by class, and a class's members are consecutive.
 struct StrainView {
-  int32_t n;
-  const int64_t *elem;   // global element index
-  const int32_t *inst;   // instance (time and dT)
-  const int32_t *kind;   // 1 HH / 0 cable
-  const int64_t *col;    // parameter column of an HH element
-  const double *spec;    // [10][n]: dX, diameter, ro_a, ro_m, per_m, thickness, rest, sigma_Na, sigma_K, sigma_L
+  int32_t n;             // strained elements
+  int32_t ncls;          // classes
+  const int64_t *elem;   // global element index, sorted by class
+  const int64_t *col;    // parameter column of an HH element (same order)
+  const int32_t *cls;    // class of each element (same order; non-decreasing)
+  const int32_t *inst;   // [ncls] instance (time and dT)
+  const int32_t *kind;   // [ncls] 1 HH / 0 cable
+  const double *spec;    // [10][ncls]: dX, diameter, ro_a, ro_m, per_m, thickness, rest, sigma_Na, sigma_K, sigma_L
+  double *tab;           // [kChunk][ncls][kStrainOut] derived ahead for a graph chunk, or null
+  int32_t *tlive;        // [kChunk][ncls]: the class's instance still runs at that step
   int32_t myelin;
   double e_max, eps0, eps1, t0, t1;
 };
@@ -38,43 +48,40 @@ struct StrainState {
 
 namespace {
 
-__global__ void strain_update(StrainView s, PackView p, int k, int mixed) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= s.n) return;
-  const InstDev in = p.inst[s.inst[q]];
+constexpr int kStrainBlock = 32;          // strained elements (or table entries) per block
+constexpr int kStrainOut = 2 + HP_ROWS;   // dT/(c_m dX), 1/(r_a dX), then W dX, K dX or the column
+
+// Class c's coefficients for step k of the current loop range into o[kStrainOut]; false
+// when the class's instance has finished its run (nothing is written then).
+__device__ bool derive_class(const StrainView &s, const PackView &p, int c, int k, double *o) {
+  const InstDev in = p.inst[s.inst[c]];
   const int64_t i = in.base + k;
-  if (i >= in.iend) return;
+  if (i >= in.iend) return false;
   const double t = (double)i * in.dT;
-  const double e = t <= s.t0 ? s.eps0
-                             : (t >= s.t1 ? s.eps1
-                                          : s.eps0 + (s.eps1 - s.eps0) * ((t - s.t0) / (s.t1 - s.t0)));
+  const double e =
+      t <= s.t0 ? s.eps0
+                : (t >= s.t1 ? s.eps1 : s.eps0 + (s.eps1 - s.eps0) * ((t - s.t0) / (s.t1 - s.t0)));
+  const int n = s.ncls;
   nrt_param::ElemIn x;
-  x.kind = s.kind[q];
-  x.dX0 = s.spec[q];
-  x.diam0 = s.spec[s.n + q];
+  x.kind = s.kind[c];
+  x.dX0 = s.spec[c];
+  x.diam0 = s.spec[n + c];
   x.eps = e;
-  x.ro_a = s.spec[2 * s.n + q];
-  x.ro_m = s.spec[3 * s.n + q];
-  x.per_m = s.spec[4 * s.n + q];
-  x.th = s.spec[5 * s.n + q];
-  x.rest = s.spec[6 * s.n + q];
-  x.sna = s.spec[7 * s.n + q];
-  x.sk = s.spec[8 * s.n + q];
-  x.sl = s.spec[9 * s.n + q];
+  x.ro_a = s.spec[2 * n + c];
+  x.ro_m = s.spec[3 * n + c];
+  x.per_m = s.spec[4 * n + c];
+  x.th = s.spec[5 * n + c];
+  x.rest = s.spec[6 * n + c];
+  x.sna = s.spec[7 * n + c];
+  x.sk = s.spec[8 * n + c];
+  x.sl = s.spec[9 * n + c];
   double ep[6], hp[12];
   nrt_param::derive_element(x, s.myelin, s.e_max, ep, hp);
-  const int64_t j = s.elem[q];
   const double c_m = ep[0], r_a = ep[1], dx = ep[2];
-  const double cdt = in.dT / (c_m * dx), gax = 1.0 / (r_a * dx);  // as the pack builds them
-  if (mixed) {
-    ((float *)p.cdtf)[j] = (float)cdt;
-    ((float *)p.gaxf)[j] = (float)gax;
-  } else {
-    ((double *)p.cdt)[j] = cdt;
-    ((double *)p.gax)[j] = gax;
-  }
+  o[0] = in.dT / (c_m * dx);  // as the pack builds them
+  o[1] = 1.0 / (r_a * dx);
   if (x.kind == 1) {
-    double v[HP_ROWS];
+    double *v = o + 2;
     v[HP_GNA] = hp[3];
     v[HP_GK] = hp[4];
     v[HP_GL] = hp[5];
@@ -86,20 +93,76 @@ __global__ void strain_update(StrainView s, PackView p, int k, int mixed) {
     v[HP_REST] = hp[11];
     v[HP_DX] = dx;
     v[HP_DTMS] = in.dT * 1000;  // src/solverEx-cpu.cpp:96
-    const int64_t c = s.col[q];
+  } else {
+    o[2] = ep[3] * dx;
+    o[3] = ep[4] * dx;
+  }
+  return true;
+}
+
+// Element q (class-sorted position) takes its class's coefficients o.
+__device__ void apply_element(const StrainView &s, const PackView &p, int q, const double *o,
+                              int mixed) {
+  const int64_t j = s.elem[q];
+  if (mixed) {
+    ((float *)p.cdtf)[j] = (float)o[0];
+    ((float *)p.gaxf)[j] = (float)o[1];
+  } else {
+    ((double *)p.cdt)[j] = o[0];
+    ((double *)p.gax)[j] = o[1];
+  }
+  if (s.kind[s.cls[q]] == 1) {
+    const int64_t cc = s.col[q];
     if (mixed) {
-      float *col = (float *)(p.hpq + 3 * c);
-      for (int r = 0; r < HP_ROWS; r++) col[r] = (float)v[r];
+      float *col = (float *)(p.hpq + 3 * cc);
+      for (int r = 0; r < HP_ROWS; r++) col[r] = (float)o[2 + r];
     } else {
-      for (int r = 0; r < HP_ROWS; r++) ((double *)p.hp)[r * p.hp_ld + c] = v[r];
+      for (int r = 0; r < HP_ROWS; r++) ((double *)p.hp)[r * p.hp_ld + cc] = o[2 + r];
     }
   } else if (mixed) {
-    ((float *)p.wdxf)[j] = (float)(ep[3] * dx);
-    ((float *)p.kdxf)[j] = (float)(ep[4] * dx);
+    ((float *)p.wdxf)[j] = (float)o[2];
+    ((float *)p.kdxf)[j] = (float)o[3];
   } else {
-    ((double *)p.wdx)[j] = ep[3] * dx;
-    ((double *)p.kdx)[j] = ep[4] * dx;
+    ((double *)p.wdx)[j] = o[2];
+    ((double *)p.kdx)[j] = o[3];
   }
+}
+
+// Step k, derivation and writes in one launch.  Block b owns elements [32 b, 32 b + 32)
+// of the class-sorted list, which span at most 32 consecutive classes.  Thread t derives
+// class (first class of the block) + t, if the block has it, into shared memory; then
+// every thread writes its own element.
+__global__ void __launch_bounds__(kStrainBlock) strain_update(StrainView s, PackView p, int k,
+                                                                int mixed) {
+  __shared__ double out[kStrainBlock][kStrainOut];
+  __shared__ int live[kStrainBlock];
+  const int q0 = blockIdx.x * kStrainBlock;
+  const int qlast = min(q0 + kStrainBlock, s.n) - 1;
+  const int c0 = s.cls[q0], c = c0 + (int)threadIdx.x;
+  if (c <= s.cls[qlast]) live[threadIdx.x] = derive_class(s, p, c, k, out[threadIdx.x]);
+  __syncthreads();
+  const int q = q0 + (int)threadIdx.x;
+  if (q > qlast) return;
+  const int t = s.cls[q] - c0;
+  if (live[t]) apply_element(s, p, q, out[t], mixed);
+}
+
+// Steps 0 .. nk-1 of a graph chunk, derived ahead in one launch: the coefficients depend
+// on time only, so all (step, class) pairs run in parallel instead of one chain of FP64
+// work per step.  Entry g is step g / ncls, class g % ncls.
+__global__ void __launch_bounds__(kStrainBlock) strain_derive(StrainView s, PackView p, int nk) {
+  const int64_t g = (int64_t)blockIdx.x * kStrainBlock + threadIdx.x;
+  if (g >= (int64_t)nk * s.ncls) return;
+  const int k = (int)(g / s.ncls), c = (int)(g % s.ncls);
+  s.tlive[g] = derive_class(s, p, c, k, s.tab + g * kStrainOut);
+}
+
+// Step k of the chunk: every strained element takes its class's row of the table.
+__global__ void __launch_bounds__(256) strain_apply(StrainView s, PackView p, int k, int mixed) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= s.n) return;
+  const int64_t g = (int64_t)k * s.ncls + s.cls[q];
+  if (s.tlive[g]) apply_element(s, p, q, s.tab + g * kStrainOut, mixed);
 }
 
 }  // namespace
@@ -107,9 +170,32 @@ __global__ void strain_update(StrainView s, PackView p, int k, int mixed) {
 int launch_strain_update(const Engine &e, int k, cudaStream_t st) {
   const StrainView &v = e.strain->view;
   if (v.n <= 0) return NRT_OK;
-  // one warp per block: the FP64 re-derivation is bound by each SM's FP64 pipe, so the
-  // elements are spread over as many SMs as there are warps of them
-  strain_update<<<(v.n + 31) / 32, 32, 0, st>>>(v, e.pv, k, e.opt.precision == NRT_MIXED);
+  // one warp per block: distinct classes are bound by each SM's FP64 pipe, so they are
+  // spread over as many SMs as there are warps of elements
+  strain_update<<<(v.n + kStrainBlock - 1) / kStrainBlock, kStrainBlock, 0, st>>>(
+      v, e.pv, k, e.opt.precision == NRT_MIXED);
+  NRT_CUDA(cudaGetLastError());
+  return NRT_OK;
+}
+
+bool strain_tabled(const Engine &e) { return e.strain && e.strain->view.tab; }
+
+int launch_strain_derive(const Engine &e, int nk, cudaStream_t st) {
+  const StrainView &v = e.strain->view;
+  if (v.n <= 0) return NRT_OK;
+  if (!v.tab || nk > kChunk) return NRT_EINVAL;
+  const int64_t entries = (int64_t)nk * v.ncls;
+  strain_derive<<<(unsigned)((entries + kStrainBlock - 1) / kStrainBlock), kStrainBlock, 0, st>>>(
+      v, e.pv, nk);
+  NRT_CUDA(cudaGetLastError());
+  return NRT_OK;
+}
+
+int launch_strain_apply(const Engine &e, int k, cudaStream_t st) {
+  const StrainView &v = e.strain->view;
+  if (v.n <= 0) return NRT_OK;
+  if (!v.tab || k < 0 || k >= kChunk) return NRT_EINVAL;
+  strain_apply<<<(v.n + 255) / 256, 256, 0, st>>>(v, e.pv, k, e.opt.precision == NRT_MIXED);
   NRT_CUDA(cudaGetLastError());
   return NRT_OK;
 }
@@ -158,7 +244,7 @@ int Engine::strain_config(const nrt_strain_config *c) {
     }
   strain_release();
   if (n == 0) return NRT_OK;
-  StrainState *S = new (std::nothrow) StrainState();
+  std::unique_ptr<StrainState> S(new (std::nothrow) StrainState());
   if (!S) {
     set_error("host allocation");
     return NRT_ENOMEM;
@@ -192,7 +278,6 @@ int Engine::strain_config(const nrt_strain_config *c) {
     if (cudaMalloc(&d_tab, tab_bytes) != cudaSuccess || cudaMalloc(&d_cls, 4 * (size_t)N) != cudaSuccess) {
       cudaGetLastError();
       if (d_tab) cudaFree(d_tab);
-      delete S;
       set_error("device allocation for the strained parameter table");
       return NRT_ENOMEM;
     }
@@ -220,15 +305,50 @@ int Engine::strain_config(const nrt_strain_config *c) {
     host.hp_ld = L1;
     host.hp_inst = false;
   }
-  // the strained elements' description, unstrained
-  std::vector<double> spec((size_t)10 * n);
-  const int rows[10] = {0, 1, 4, 5, 6, 7, 8, 9, 10, 11};  // dspec rows used (no epsilon, input)
-  for (int r = 0; r < 10; r++)
-    for (int32_t q = 0; q < n; q++) spec[(size_t)r * n + q] = c->dspec[(size_t)rows[r] * n + q];
-  const size_t bytes = 8 * (size_t)n * 2 + 4 * (size_t)n * 2 + 8 * spec.size() + 256 * 4;
+  // classes of identical input columns (instance, kind, the ten description values used:
+  // no epsilon, no input), the elements sorted by class
+  const int rows[10] = {0, 1, 4, 5, 6, 7, 8, 9, 10, 11};
+  constexpr int kKey = 11;
+  std::vector<uint64_t> key((size_t)kKey * n);
+  for (int32_t q = 0; q < n; q++) {
+    key[(size_t)kKey * q] = ((uint64_t)(uint32_t)inst[q] << 1) | (uint64_t)(kind[q] == 1);
+    for (int r = 0; r < 10; r++)
+      std::memcpy(&key[(size_t)kKey * q + 1 + r], &c->dspec[(size_t)rows[r] * n + q], 8);
+  }
+  std::vector<int32_t> order(n);
+  for (int32_t q = 0; q < n; q++) order[q] = q;
+  auto key_less = [&](int32_t x, int32_t y) {
+    return std::lexicographical_compare(&key[(size_t)kKey * x], &key[(size_t)kKey * x + kKey],
+                                        &key[(size_t)kKey * y], &key[(size_t)kKey * y + kKey]);
+  };
+  std::stable_sort(order.begin(), order.end(), key_less);
+  std::vector<int64_t> s_elem(n), s_col(n);
+  std::vector<int32_t> s_cls(n), first;  // first: one member of each class
+  for (int32_t r = 0; r < n; r++) {
+    const int32_t q = order[r];
+    if (r == 0 || key_less(order[r - 1], q)) first.push_back(q);
+    s_elem[r] = elem[q];
+    s_col[r] = col[q];
+    s_cls[r] = (int32_t)first.size() - 1;
+  }
+  const int32_t ncls = (int32_t)first.size();
+  std::vector<int32_t> c_inst(ncls), c_kind(ncls);
+  std::vector<double> c_spec((size_t)10 * ncls);
+  for (int32_t k = 0; k < ncls; k++) {
+    c_inst[k] = inst[first[k]];
+    c_kind[k] = kind[first[k]];
+    for (int r = 0; r < 10; r++)
+      c_spec[(size_t)r * ncls + k] = c->dspec[(size_t)rows[r] * n + first[k]];
+  }
+  // the table a graph chunk derives ahead, when it stays small (64 MiB); otherwise each
+  // step derives its own coefficients
+  const size_t tab_entries = (size_t)kChunk * ncls;
+  const bool tabled = tab_entries * (8 * kStrainOut + 4) <= ((size_t)64 << 20);
+  const size_t bytes = 8 * (size_t)n * 2 + 4 * (size_t)n + 4 * (size_t)ncls * 2 +
+                       8 * c_spec.size() +
+                       (tabled ? tab_entries * (8 * kStrainOut + 4) : 0) + 256 * 8;
   if (cudaMalloc(&S->mem, bytes) != cudaSuccess) {
     cudaGetLastError();
-    delete S;
     set_error("device allocation for the strain");
     return NRT_ENOMEM;
   }
@@ -240,19 +360,28 @@ int Engine::strain_config(const nrt_strain_config *c) {
   };
   StrainView &v = S->view;
   int64_t *d_elem = (int64_t *)take(8 * (size_t)n), *d_col = (int64_t *)take(8 * (size_t)n);
-  int32_t *d_inst = (int32_t *)take(4 * (size_t)n), *d_kind = (int32_t *)take(4 * (size_t)n);
-  double *d_spec = (double *)take(8 * spec.size());
-  NRT_CUDA(cudaMemcpyAsync(d_elem, elem.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, stream));
-  NRT_CUDA(cudaMemcpyAsync(d_col, col.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, stream));
-  NRT_CUDA(cudaMemcpyAsync(d_inst, inst.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, stream));
-  NRT_CUDA(cudaMemcpyAsync(d_kind, kind.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, stream));
-  NRT_CUDA(cudaMemcpyAsync(d_spec, spec.data(), 8 * spec.size(), cudaMemcpyHostToDevice, stream));
+  int32_t *d_cls = (int32_t *)take(4 * (size_t)n);
+  int32_t *d_inst = (int32_t *)take(4 * (size_t)ncls), *d_kind = (int32_t *)take(4 * (size_t)ncls);
+  double *d_spec = (double *)take(8 * c_spec.size());
+  v.tab = tabled ? (double *)take(8 * kStrainOut * tab_entries) : nullptr;
+  v.tlive = tabled ? (int32_t *)take(4 * tab_entries) : nullptr;
+  NRT_CUDA(cudaMemcpyAsync(d_elem, s_elem.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, stream));
+  NRT_CUDA(cudaMemcpyAsync(d_col, s_col.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, stream));
+  NRT_CUDA(cudaMemcpyAsync(d_cls, s_cls.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, stream));
+  NRT_CUDA(cudaMemcpyAsync(d_inst, c_inst.data(), 4 * (size_t)ncls, cudaMemcpyHostToDevice,
+                           stream));
+  NRT_CUDA(cudaMemcpyAsync(d_kind, c_kind.data(), 4 * (size_t)ncls, cudaMemcpyHostToDevice,
+                           stream));
+  NRT_CUDA(cudaMemcpyAsync(d_spec, c_spec.data(), 8 * c_spec.size(), cudaMemcpyHostToDevice,
+                           stream));
   NRT_CUDA(cudaStreamSynchronize(stream));
   v.n = n;
+  v.ncls = ncls;
   v.elem = d_elem;
+  v.col = d_col;
+  v.cls = d_cls;
   v.inst = d_inst;
   v.kind = d_kind;
-  v.col = d_col;
   v.spec = d_spec;
   v.myelin = c->myelin;
   v.e_max = c->e_max;
@@ -260,7 +389,7 @@ int Engine::strain_config(const nrt_strain_config *c) {
   v.eps1 = c->eps1;
   v.t0 = c->t0;
   v.t1 = c->t1;
-  strain = S;
+  strain = S.release();
   return NRT_OK;
 }
 

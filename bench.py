@@ -441,9 +441,10 @@ def run_ours(args, rank: int, world: int):
         roof_passes = {"bound": "hbm", "achieved": a2, "peak": peak, "unit": "GB/s",
                        "frac": a2 / peak, "bytes_per_step": passes_all}
     # our kernels launched in the timed region: one persistent launch + one loop-index
-    # update per 64-step chunk (implicit); 64 step launches + 1 update per graph (explicit)
+    # update per 64-step chunk (implicit); 64 step launches + 1 update per graph (explicit),
+    # and with strain one coefficient write per step + one derivation per graph
     launches = (2 * math.ceil(K / 64) if implicit
-                else K * (2 if strained else 1) + math.ceil(K / 64))  # + the strain update
+                else (K + math.ceil(K / 64)) * (2 if strained else 1))
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms / K, "higher_is_better": True,

@@ -52,10 +52,38 @@ def test_constant_ramp_equals_static_strain(gpu, pkg, model, precision, tol):
     b.close()
 
 
+def small_myelin(model):
+    """12 HH nodes between 40 um internodes (452 elements): strained blocks mix HH nodes
+    and passive internodes."""
+    return model.myelinated_axon(n_nodes=12, internode_len=40e-6, tspan=2e-3)
+
+
+def small_tree(model):
+    """A random tree whose diameter halves every 1.5 levels: many distinct strained
+    columns, several per block of the strain update."""
+    return model.random_tree(seed=11, n_target=600, depth_lo=5, depth_hi=6, tspan=2e-3)
+
+
+def strained(spec):
+    """Every element but the root and the terminals."""
+    keep = np.ones(spec.n, bool)
+    keep[0] = False
+    keep[np.asarray(spec.terminals, int)] = False
+    return np.nonzero(keep)[0]
+
+
+TREES = {"axon": (axon, segment), "myelin": (small_myelin, strained),
+         "tree": (small_tree, strained)}
+
+
+@pytest.mark.parametrize("tree", sorted(TREES))
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 1e-4)])
-def test_strain_ramp_matches_oracle(gpu, pkg, orc, model, precision, tol):
-    spec = axon(model)
-    seg = segment(spec)
+def test_strain_ramp_matches_oracle(gpu, pkg, orc, model, precision, tol, tree):
+    build, pick = TREES[tree]
+    if precision == "mixed" and tree != "axon":
+        tol = 1e-5  # strain moves V by 6e-5 V (myelin) and 1.2e-4 V (tree) here
+    spec = build(model)
+    seg = pick(spec)
     dT = step_size(pkg, spec, seg, 0.2)
     steps = 2000
     t0, t1 = 100 * dT, 1500 * dT  # the ramp runs from step 100 to step 1500
@@ -84,6 +112,30 @@ def test_strain_ramp_matches_oracle(gpu, pkg, orc, model, precision, tol):
     plain.run(1, 1 + steps, spec.init_time, spec.end_input)
     assert np.abs(plain.snapshot() - got).max() > 1e-5
     plain.close()
+
+
+def test_strained_columns_share_derivations(model):
+    """The strain update derives once per distinct input column; the test trees above
+    give few classes (uniform axon), classes of two kinds (myelinated axon) and many
+    classes with several per block of 32 elements (random tree)."""
+    def classes(spec, seg):
+        cols = np.stack([spec.kind[seg], spec.dX[seg], spec.diameter[seg], spec.ro_a[seg],
+                         spec.ro_m[seg], spec.per_m[seg], spec.thickness[seg],
+                         spec.rest_pot[seg], spec.sigma_Na[seg], spec.sigma_K[seg],
+                         spec.sigma_L[seg]], axis=1)
+        return np.unique(cols, axis=0, return_inverse=True)[1].ravel()
+
+    got = {}
+    for name, (build, pick) in TREES.items():
+        spec = build(model)
+        seg = pick(spec)
+        inv = classes(spec, seg)
+        order = np.argsort(inv, kind="stable")
+        per_block = [len(np.unique(inv[order][b:b + 32])) for b in range(0, len(seg), 32)]
+        got[name] = (len(np.unique(inv)), max(per_block))
+    assert got["axon"][0] <= 2
+    assert len(np.unique(small_myelin(model).kind[strained(small_myelin(model))])) == 2
+    assert got["tree"][0] >= 5 and got["tree"][1] >= 2
 
 
 def test_strain_needs_the_explicit_stepper(gpu, pkg, model):
