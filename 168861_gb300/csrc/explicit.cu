@@ -29,6 +29,7 @@
 
 #include "hh.cuh"
 #include "nrt_internal.h"
+#include "pdl.cuh"
 #include "tma.cuh"
 
 namespace nrt {
@@ -49,6 +50,8 @@ template <bool kGeneral>
 __global__ void __launch_bounds__(256) explicit_step_f64(PackView p, int k, int force,
                                                          const double *__restrict__ Vin,
                                                          double *__restrict__ Vout) {
+  chain_acquire();  // the previous launch of the time loop has finished
+  chain_release();
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= p.ntot) return;
   const Topo tj = p.topo[j];
@@ -109,6 +112,8 @@ __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, in
                                                            double *__restrict__ Vout,
                                                            const float *__restrict__ Fin,
                                                            float *__restrict__ Fout) {
+  chain_acquire();  // the previous launch of the time loop has finished
+  chain_release();
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= p.ntot) return;
   const int64_t N = p.ntot;
@@ -378,6 +383,8 @@ constexpr int kTileWarps = kTileThreads / 32;
 __global__ void __launch_bounds__(kTileThreads) explicit_step_mixed_tiled(
     PackView p, int k, int force, const double *__restrict__ Vin, double *__restrict__ Vout,
     const float *__restrict__ Fin, float *__restrict__ Fout) {
+  chain_acquire();  // the previous launch of the time loop has finished
+  chain_release();
   extern __shared__ __align__(16) unsigned char tsm[];
   uint64_t *full = (uint64_t *)(tsm + 2 * kTileBufBytes);
   uint64_t *empty = full + 2;
@@ -454,6 +461,8 @@ __global__ void terminal_fixup(const Topo *__restrict__ topo, const int64_t *__r
 }
 
 __global__ void advance_base(InstDev *inst, int32_t ninst, int64_t steps) {
+  chain_acquire();  // the previous launch of the time loop has finished
+  chain_release();
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ninst) return;
   int64_t b = inst[i].base + steps;
@@ -471,20 +480,16 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
   while (threads > 32 && pv.ntot < (int64_t)threads * 2 * 152) threads >>= 1;
   const unsigned blocks = (unsigned)((pv.ntot + threads - 1) / threads);
   if (precision == NRT_MIXED) {
-    if (!general && pv.tile_blocks > 0 && pv.eflags && pv.err) {
-      explicit_step_mixed_tiled<<<pv.tile_blocks, kTileThreads, 2 * kTileBufBytes + 32, st>>>(
-          pv, k, force, Vin, Vout, Fin, Fout);
-    } else if (general)
-      explicit_step_mixed<true><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout, Fin, Fout);
+    if (!general && pv.tile_blocks > 0 && pv.eflags && pv.err)
+      NRT_CUDA(launch_chained(explicit_step_mixed_tiled, pv.tile_blocks, kTileThreads,
+                              2 * kTileBufBytes + 32, st, pv, k, force, Vin, Vout, Fin, Fout));
     else
-      explicit_step_mixed<false><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout, Fin, Fout);
+      NRT_CUDA(launch_chained(general ? explicit_step_mixed<true> : explicit_step_mixed<false>,
+                              blocks, threads, 0, st, pv, k, force, Vin, Vout, Fin, Fout));
   } else {
-    if (general)
-      explicit_step_f64<true><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout);
-    else
-      explicit_step_f64<false><<<blocks, threads, 0, st>>>(pv, k, force, Vin, Vout);
+    NRT_CUDA(launch_chained(general ? explicit_step_f64<true> : explicit_step_f64<false>, blocks,
+                            threads, 0, st, pv, k, force, Vin, Vout));
   }
-  NRT_CUDA(cudaGetLastError());
   return NRT_OK;
 }
 
@@ -511,8 +516,7 @@ int launch_terminal_fixup(const Topo *topo, const int64_t *terms, int64_t nterm,
 }
 
 int launch_advance_base(InstDev *inst, int32_t ninst, int64_t steps, cudaStream_t st) {
-  advance_base<<<(ninst + 255) / 256, 256, 0, st>>>(inst, ninst, steps);
-  NRT_CUDA(cudaGetLastError());
+  NRT_CUDA(launch_chained(advance_base, (ninst + 255) / 256, 256, 0, st, inst, ninst, steps));
   return NRT_OK;
 }
 

@@ -9,6 +9,7 @@
 #include <numeric>
 
 #include "nrt_solver.h"
+#include "pdl.cuh"
 #include "record.cuh"
 
 namespace nrt {
@@ -17,6 +18,8 @@ namespace {
 
 __global__ void record_step(RecView r, const InstDev *__restrict__ inst, int k,
                             const double *__restrict__ V) {
+  chain_acquire();  // the previous launch of the time loop has finished
+  chain_release();
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= r.nprobe) return;
   const InstDev in = inst[r.inst[p]];
@@ -55,8 +58,7 @@ struct RecState {
 int launch_record_step(const RecView &r, const InstDev *inst, int k, const double *V,
                        cudaStream_t st) {
   if (r.nprobe <= 0) return NRT_OK;
-  record_step<<<(r.nprobe + 127) / 128, 128, 0, st>>>(r, inst, k, V);
-  NRT_CUDA(cudaGetLastError());
+  NRT_CUDA(launch_chained(record_step, (r.nprobe + 127) / 128, 128, 0, st, r, inst, k, V));
   return NRT_OK;
 }
 

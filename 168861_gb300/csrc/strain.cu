@@ -16,6 +16,7 @@
 
 #include "derive_elem.h"
 #include "nrt_solver.h"
+#include "pdl.cuh"
 
 namespace nrt {
 
@@ -134,6 +135,8 @@ __device__ void apply_element(const StrainView &s, const PackView &p, int q, con
 // every thread writes its own element.
 __global__ void __launch_bounds__(kStrainBlock) strain_update(StrainView s, PackView p, int k,
                                                                 int mixed) {
+  chain_acquire();  // the previous launch of the time loop has finished
+  chain_release();
   __shared__ double out[kStrainBlock][kStrainOut];
   __shared__ int live[kStrainBlock];
   const int q0 = blockIdx.x * kStrainBlock;
@@ -151,6 +154,8 @@ __global__ void __launch_bounds__(kStrainBlock) strain_update(StrainView s, Pack
 // on time only, so all (step, class) pairs run in parallel instead of one chain of FP64
 // work per step.  Entry g is step g / ncls, class g % ncls.
 __global__ void __launch_bounds__(kStrainBlock) strain_derive(StrainView s, PackView p, int nk) {
+  chain_acquire();  // the previous launch of the time loop has finished
+  chain_release();
   const int64_t g = (int64_t)blockIdx.x * kStrainBlock + threadIdx.x;
   if (g >= (int64_t)nk * s.ncls) return;
   const int k = (int)(g / s.ncls), c = (int)(g % s.ncls);
@@ -159,6 +164,8 @@ __global__ void __launch_bounds__(kStrainBlock) strain_derive(StrainView s, Pack
 
 // Step k of the chunk: every strained element takes its class's row of the table.
 __global__ void __launch_bounds__(256) strain_apply(StrainView s, PackView p, int k, int mixed) {
+  chain_acquire();  // the previous launch of the time loop has finished
+  chain_release();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= s.n) return;
   const int64_t g = (int64_t)k * s.ncls + s.cls[q];
@@ -172,9 +179,8 @@ int launch_strain_update(const Engine &e, int k, cudaStream_t st) {
   if (v.n <= 0) return NRT_OK;
   // one warp per block: distinct classes are bound by each SM's FP64 pipe, so they are
   // spread over as many SMs as there are warps of elements
-  strain_update<<<(v.n + kStrainBlock - 1) / kStrainBlock, kStrainBlock, 0, st>>>(
-      v, e.pv, k, e.opt.precision == NRT_MIXED);
-  NRT_CUDA(cudaGetLastError());
+  NRT_CUDA(launch_chained(strain_update, (v.n + kStrainBlock - 1) / kStrainBlock, kStrainBlock, 0,
+                          st, v, e.pv, k, (int)(e.opt.precision == NRT_MIXED)));
   return NRT_OK;
 }
 
@@ -185,9 +191,8 @@ int launch_strain_derive(const Engine &e, int nk, cudaStream_t st) {
   if (v.n <= 0) return NRT_OK;
   if (!v.tab || nk > kChunk) return NRT_EINVAL;
   const int64_t entries = (int64_t)nk * v.ncls;
-  strain_derive<<<(unsigned)((entries + kStrainBlock - 1) / kStrainBlock), kStrainBlock, 0, st>>>(
-      v, e.pv, nk);
-  NRT_CUDA(cudaGetLastError());
+  NRT_CUDA(launch_chained(strain_derive, (unsigned)((entries + kStrainBlock - 1) / kStrainBlock),
+                          kStrainBlock, 0, st, v, e.pv, nk));
   return NRT_OK;
 }
 
@@ -195,8 +200,8 @@ int launch_strain_apply(const Engine &e, int k, cudaStream_t st) {
   const StrainView &v = e.strain->view;
   if (v.n <= 0) return NRT_OK;
   if (!v.tab || k < 0 || k >= kChunk) return NRT_EINVAL;
-  strain_apply<<<(v.n + 255) / 256, 256, 0, st>>>(v, e.pv, k, e.opt.precision == NRT_MIXED);
-  NRT_CUDA(cudaGetLastError());
+  NRT_CUDA(launch_chained(strain_apply, (v.n + 255) / 256, 256, 0, st, v, e.pv, k,
+                          (int)(e.opt.precision == NRT_MIXED)));
   return NRT_OK;
 }
 
