@@ -688,20 +688,22 @@ const char *nrt_status_string(int s) {
 const char *nrt_last_error(void) { return nrt::g_last_error.c_str(); }
 
 int nrt_options_default(nrt_options *o) {
-  if (!o) return NRT_EINVAL;
-  memset(o, 0, sizeof(*o));
-  o->mode = NRT_EXPLICIT;
-  o->precision = NRT_FP64;
-  o->krylov = NRT_GMRES;
-  o->precond = NRT_PRECOND_TREE;
-  o->restart = 30;
-  o->tol_mode = NRT_TOL_ABS;
-  o->tol = 1e-14;  // RANGE_ERROR, inc/configuration.h:16
-  o->max_iter = 0;
-  o->device = -1;
-  o->use_graphs = 1;
-  o->tiled = 1;
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!o) return NRT_EINVAL;
+    memset(o, 0, sizeof(*o));
+    o->mode = NRT_EXPLICIT;
+    o->precision = NRT_FP64;
+    o->krylov = NRT_GMRES;
+    o->precond = NRT_PRECOND_TREE;
+    o->restart = 30;
+    o->tol_mode = NRT_TOL_ABS;
+    o->tol = 1e-14;  // RANGE_ERROR, inc/configuration.h:16
+    o->max_iter = 0;
+    o->device = -1;
+    o->use_graphs = 1;
+    o->tiled = 1;
+    return NRT_OK;
+  });
 }
 
 static int check_options(const nrt_options *o, std::string &why) {
@@ -720,354 +722,416 @@ static int check_options(const nrt_options *o, std::string &why) {
 }
 
 int nrt_create(const nrt_problem *p, const nrt_options *opt, nrt_solver **out) {
-  if (!p || !out) return nrt::fail(NRT_EINVAL, "null argument");
-  *out = nullptr;
-  nrt_options o;
-  if (opt) o = *opt; else nrt_options_default(&o);
-  std::string why;
-  int rc = check_options(&o, why);
-  if (rc) return nrt::fail(rc, why);
-  rc = nrt::validate_problem(p, o.mode == NRT_IMPLICIT_BE, why);
-  if (rc) return nrt::fail(rc, why);
-  nrt_solver *s = new (std::nothrow) nrt_solver();
-  if (!s) return nrt::fail(NRT_ENOMEM, "host allocation");
-  rc = s->eng.init(p, 1, &o);
-  if (rc) {
-    delete s;
-    return rc;
-  }
-  *out = s;
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!p || !out) return nrt::fail(NRT_EINVAL, "null argument");
+    *out = nullptr;
+    nrt_options o;
+    if (opt) o = *opt; else nrt_options_default(&o);
+    std::string why;
+    int rc = check_options(&o, why);
+    if (rc) return nrt::fail(rc, why);
+    rc = nrt::validate_problem(p, o.mode == NRT_IMPLICIT_BE, why);
+    if (rc) return nrt::fail(rc, why);
+    std::unique_ptr<nrt_solver> s(new (std::nothrow) nrt_solver());
+    if (!s) return nrt::fail(NRT_ENOMEM, "host allocation");
+    rc = s->eng.init(p, 1, &o);
+    if (rc) return rc;
+    *out = s.release();
+    return NRT_OK;
+  });
 }
 
 int nrt_update(nrt_solver *s, int input_active) {
-  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
-  s->pending_input = input_active ? 1 : 0;
-  s->have_update = true;
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+    s->pending_input = input_active ? 1 : 0;
+    s->have_update = true;
+    return NRT_OK;
+  });
 }
 
 int nrt_calculate(nrt_solver *s) {
-  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
-  if (!s->have_update) return nrt::fail(NRT_ESTATE, "calculate() without a preceding update()");
-  NRT_CUDA(cudaSetDevice(s->eng.device));
-  const int64_t before = s->eng.opt.mode == NRT_IMPLICIT_BE ? nrt::nonconverged_total(s->eng) : 0;
-  int rc = s->eng.step(0, s->pending_input);
-  s->have_update = false;
-  if (rc == NRT_OK && s->eng.opt.mode == NRT_IMPLICIT_BE) {
-    const int64_t after = nrt::nonconverged_total(s->eng);
-    if (after < 0) return NRT_EDEVICE;
-    if (after > before)
-      return nrt::fail(NRT_ENOCONV, "implicit step hit its Krylov iteration budget");
-  }
-  return rc;
+  return nrt::guarded([&]() -> int {
+    if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+    if (!s->have_update) return nrt::fail(NRT_ESTATE, "calculate() without a preceding update()");
+    NRT_CUDA(cudaSetDevice(s->eng.device));
+    const int64_t before = s->eng.opt.mode == NRT_IMPLICIT_BE ? nrt::nonconverged_total(s->eng) : 0;
+    int rc = s->eng.step(0, s->pending_input);
+    s->have_update = false;
+    if (rc == NRT_OK && s->eng.opt.mode == NRT_IMPLICIT_BE) {
+      const int64_t after = nrt::nonconverged_total(s->eng);
+      if (after < 0) return NRT_EDEVICE;
+      if (after > before)
+        return nrt::fail(NRT_ENOCONV, "implicit step hit its Krylov iteration budget");
+    }
+    return rc;
+  });
 }
 
 int nrt_export_system(nrt_solver *s, int input_active, int32_t *row_ptr, int32_t *col, double *val,
                       double *rhs, int32_t *nnz_out) {
-  if (!s || !row_ptr || !col || !val || !rhs || !nnz_out) return nrt::fail(NRT_EINVAL, "null argument");
-  NRT_CUDA(cudaSetDevice(s->eng.device));
-  return nrt::export_system(s->eng, input_active, row_ptr, col, val, rhs, nnz_out);
+  return nrt::guarded([&]() -> int {
+    if (!s || !row_ptr || !col || !val || !rhs || !nnz_out) return nrt::fail(NRT_EINVAL, "null argument");
+    NRT_CUDA(cudaSetDevice(s->eng.device));
+    return nrt::export_system(s->eng, input_active, row_ptr, col, val, rhs, nnz_out);
+  });
 }
 
 int nrt_snapshot(nrt_solver *s, double *potential) {
-  if (!s || !potential) return nrt::fail(NRT_EINVAL, "null argument");
-  nrt::Engine &e = s->eng;
-  NRT_CUDA(cudaSetDevice(e.device));
-  int rc = e.fixup();
-  if (rc) return rc;
-  NRT_CUDA(cudaMemcpyAsync(potential, e.V[e.cur], sizeof(double) * e.host.ntot,
-                           cudaMemcpyDeviceToHost, e.stream));
-  NRT_CUDA(cudaStreamSynchronize(e.stream));
-  return nrt::implicit_check(e);
+  return nrt::guarded([&]() -> int {
+    if (!s || !potential) return nrt::fail(NRT_EINVAL, "null argument");
+    nrt::Engine &e = s->eng;
+    NRT_CUDA(cudaSetDevice(e.device));
+    int rc = e.fixup();
+    if (rc) return rc;
+    NRT_CUDA(cudaMemcpyAsync(potential, e.V[e.cur], sizeof(double) * e.host.ntot,
+                             cudaMemcpyDeviceToHost, e.stream));
+    NRT_CUDA(cudaStreamSynchronize(e.stream));
+    return nrt::implicit_check(e);
+  });
 }
 
 int nrt_run(nrt_solver *s, int64_t i_begin, int64_t i_end, double init_time, double end_input) {
-  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
-  if (i_end < i_begin) return nrt::fail(NRT_EINVAL, "i_end < i_begin");
-  nrt::Engine &e = s->eng;
-  NRT_CUDA(cudaSetDevice(e.device));
-  nrt::InstDev in = e.host.inst[0];
-  in.base = i_begin;
-  in.iend = i_end;
-  in.t0 = init_time;
-  in.t1 = end_input;
-  nrt::set_window(in);
-  e.host.inst[0] = in;
-  NRT_CUDA(cudaMemcpyAsync(e.pv.inst, &e.host.inst[0], sizeof(in), cudaMemcpyHostToDevice, e.stream));
-  const bool implicit = e.opt.mode == NRT_IMPLICIT_BE;
-  const int64_t before = implicit ? nrt::nonconverged_total(e) : 0;
-  int rc = e.advance(i_end - i_begin);
-  if (rc) return rc;
-  if (implicit && nrt::nonconverged_total(e) > before)
-    rc = nrt::fail(NRT_ENOCONV, "an implicit step hit its Krylov iteration budget");
-  // leave the drop-in path's device loop range open again
-  e.host.inst[0].base = 0;
-  e.host.inst[0].iend = INT64_MAX;
-  NRT_CUDA(cudaMemcpyAsync(e.pv.inst, &e.host.inst[0], sizeof(in), cudaMemcpyHostToDevice, e.stream));
-  NRT_CUDA(cudaStreamSynchronize(e.stream));
-  return rc;
+  return nrt::guarded([&]() -> int {
+    if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+    if (i_end < i_begin) return nrt::fail(NRT_EINVAL, "i_end < i_begin");
+    nrt::Engine &e = s->eng;
+    NRT_CUDA(cudaSetDevice(e.device));
+    nrt::InstDev in = e.host.inst[0];
+    in.base = i_begin;
+    in.iend = i_end;
+    in.t0 = init_time;
+    in.t1 = end_input;
+    nrt::set_window(in);
+    e.host.inst[0] = in;
+    NRT_CUDA(cudaMemcpyAsync(e.pv.inst, &e.host.inst[0], sizeof(in), cudaMemcpyHostToDevice, e.stream));
+    const bool implicit = e.opt.mode == NRT_IMPLICIT_BE;
+    const int64_t before = implicit ? nrt::nonconverged_total(e) : 0;
+    int rc = e.advance(i_end - i_begin);
+    if (rc) return rc;
+    if (implicit && nrt::nonconverged_total(e) > before)
+      rc = nrt::fail(NRT_ENOCONV, "an implicit step hit its Krylov iteration budget");
+    // leave the drop-in path's device loop range open again
+    e.host.inst[0].base = 0;
+    e.host.inst[0].iend = INT64_MAX;
+    NRT_CUDA(cudaMemcpyAsync(e.pv.inst, &e.host.inst[0], sizeof(in), cudaMemcpyHostToDevice, e.stream));
+    NRT_CUDA(cudaStreamSynchronize(e.stream));
+    return rc;
+  });
 }
 
 int nrt_synchronize(nrt_solver *s) {
-  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
-  NRT_CUDA(cudaSetDevice(s->eng.device));
-  NRT_CUDA(cudaStreamSynchronize(s->eng.stream));
-  return nrt::implicit_check(s->eng);
+  return nrt::guarded([&]() -> int {
+    if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+    NRT_CUDA(cudaSetDevice(s->eng.device));
+    NRT_CUDA(cudaStreamSynchronize(s->eng.stream));
+    return nrt::implicit_check(s->eng);
+  });
 }
 
 int nrt_get_stream(nrt_solver *s, void **stream) {
-  if (!s || !stream) return nrt::fail(NRT_EINVAL, "null argument");
-  *stream = (void *)s->eng.stream;
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!s || !stream) return nrt::fail(NRT_EINVAL, "null argument");
+    *stream = (void *)s->eng.stream;
+    return NRT_OK;
+  });
 }
 
 int nrt_batch_get_stream(nrt_batch *b, void **stream) {
-  if (!b || !stream) return nrt::fail(NRT_EINVAL, "null argument");
-  *stream = (void *)b->eng.stream;
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!b || !stream) return nrt::fail(NRT_EINVAL, "null argument");
+    *stream = (void *)b->eng.stream;
+    return NRT_OK;
+  });
 }
 
 int nrt_potential_device(nrt_solver *s, const double **dev_ptr) {
-  if (!s || !dev_ptr) return nrt::fail(NRT_EINVAL, "null argument");
-  NRT_CUDA(cudaSetDevice(s->eng.device));
-  int rc = s->eng.fixup();
-  if (rc) return rc;
-  *dev_ptr = s->eng.V[s->eng.cur];
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!s || !dev_ptr) return nrt::fail(NRT_EINVAL, "null argument");
+    NRT_CUDA(cudaSetDevice(s->eng.device));
+    int rc = s->eng.fixup();
+    if (rc) return rc;
+    *dev_ptr = s->eng.V[s->eng.cur];
+    return NRT_OK;
+  });
 }
 
 int nrt_get_gates(nrt_solver *s, double *m, double *h, double *n) {
-  if (!s || !m || !h || !n) return nrt::fail(NRT_EINVAL, "null argument");
-  nrt::Engine &e = s->eng;
-  NRT_CUDA(cudaSetDevice(e.device));
-  const int64_t N = e.host.ntot;
-  std::vector<double> g(3 * N);
-  if (e.opt.precision == NRT_MIXED) {
-    std::vector<float> gf(3 * N);
-    NRT_CUDA(cudaMemcpyAsync(gf.data(), e.pv.gatef, sizeof(float) * 3 * N, cudaMemcpyDeviceToHost, e.stream));
-    NRT_CUDA(cudaStreamSynchronize(e.stream));
-    for (int64_t q = 0; q < 3 * N; q++) g[q] = gf[q];
-  } else {
-    NRT_CUDA(cudaMemcpyAsync(g.data(), e.pv.gate, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, e.stream));
-    NRT_CUDA(cudaStreamSynchronize(e.stream));
-  }
-  const int64_t nh = e.host.hh_off[1];
-  for (int64_t k = 0; k < nh; k++) {
-    const int64_t el = e.host.hh_local[k];
-    m[k] = g[el];
-    h[k] = g[N + el];
-    n[k] = g[2 * N + el];
-  }
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!s || !m || !h || !n) return nrt::fail(NRT_EINVAL, "null argument");
+    nrt::Engine &e = s->eng;
+    NRT_CUDA(cudaSetDevice(e.device));
+    const int64_t N = e.host.ntot;
+    std::vector<double> g(3 * N);
+    if (e.opt.precision == NRT_MIXED) {
+      std::vector<float> gf(3 * N);
+      NRT_CUDA(cudaMemcpyAsync(gf.data(), e.pv.gatef, sizeof(float) * 3 * N, cudaMemcpyDeviceToHost, e.stream));
+      NRT_CUDA(cudaStreamSynchronize(e.stream));
+      for (int64_t q = 0; q < 3 * N; q++) g[q] = gf[q];
+    } else {
+      NRT_CUDA(cudaMemcpyAsync(g.data(), e.pv.gate, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, e.stream));
+      NRT_CUDA(cudaStreamSynchronize(e.stream));
+    }
+    const int64_t nh = e.host.hh_off[1];
+    for (int64_t k = 0; k < nh; k++) {
+      const int64_t el = e.host.hh_local[k];
+      m[k] = g[el];
+      h[k] = g[N + el];
+      n[k] = g[2 * N + el];
+    }
+    return NRT_OK;
+  });
 }
 
 int nrt_get_stats(nrt_solver *s, nrt_stats *st) {
-  if (!s || !st) return nrt::fail(NRT_EINVAL, "null argument");
-  return s->eng.get_stats(st);
+  return nrt::guarded([&]() -> int {
+    if (!s || !st) return nrt::fail(NRT_EINVAL, "null argument");
+    return s->eng.get_stats(st);
+  });
 }
 
 int nrt_destroy(nrt_solver *s) {
-  delete s;
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    delete s;
+    return NRT_OK;
+  });
 }
 
 // ------------------------------------------------------------------ batches
 
 int nrt_batch_create(const nrt_problem *problems, int32_t count, const nrt_options *opt,
                      nrt_batch **out) {
-  if (!problems || count < 1 || !out) return nrt::fail(NRT_EINVAL, "bad arguments");
-  *out = nullptr;
-  nrt_options o;
-  if (opt) o = *opt; else nrt_options_default(&o);
-  std::string why;
-  int rc = check_options(&o, why);
-  if (rc) return nrt::fail(rc, why);
-  for (int32_t i = 0; i < count; i++) {
-    rc = nrt::validate_problem(&problems[i], o.mode == NRT_IMPLICIT_BE, why);
-    if (rc) return nrt::fail(rc, "instance " + std::to_string(i) + ": " + why);
-  }
-  nrt_batch *b = new (std::nothrow) nrt_batch();
-  if (!b) return nrt::fail(NRT_ENOMEM, "host allocation");
-  rc = b->eng.init(problems, count, &o);
-  if (rc) {
-    delete b;
-    return rc;
-  }
-  b->runs.assign(count, nrt_instance_run{0, 0, 0.0, -1.0});
-  *out = b;
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!problems || count < 1 || !out) return nrt::fail(NRT_EINVAL, "bad arguments");
+    *out = nullptr;
+    nrt_options o;
+    if (opt) o = *opt; else nrt_options_default(&o);
+    std::string why;
+    int rc = check_options(&o, why);
+    if (rc) return nrt::fail(rc, why);
+    for (int32_t i = 0; i < count; i++) {
+      rc = nrt::validate_problem(&problems[i], o.mode == NRT_IMPLICIT_BE, why);
+      if (rc) return nrt::fail(rc, "instance " + std::to_string(i) + ": " + why);
+    }
+    std::unique_ptr<nrt_batch> b(new (std::nothrow) nrt_batch());
+    if (!b) return nrt::fail(NRT_ENOMEM, "host allocation");
+    rc = b->eng.init(problems, count, &o);
+    if (rc) return rc;
+    b->runs.assign(count, nrt_instance_run{0, 0, 0.0, -1.0});
+    *out = b.release();
+    return NRT_OK;
+  });
 }
 
 int nrt_batch_set_runs(nrt_batch *b, const nrt_instance_run *runs) {
-  if (!b || !runs) return nrt::fail(NRT_EINVAL, "null argument");
-  nrt::Engine &e = b->eng;
-  NRT_CUDA(cudaSetDevice(e.device));
-  for (int32_t i = 0; i < e.pv.ninst; i++) {
-    if (runs[i].i_end < runs[i].i_begin) return nrt::fail(NRT_EINVAL, "i_end < i_begin");
-    b->runs[i] = runs[i];
-    e.host.inst[i].base = runs[i].i_begin;
-    e.host.inst[i].iend = runs[i].i_end;
-    e.host.inst[i].t0 = runs[i].init_time;
-    e.host.inst[i].t1 = runs[i].end_input;
-    nrt::set_window(e.host.inst[i]);
-  }
-  NRT_CUDA(cudaMemcpyAsync(e.pv.inst, e.host.inst.data(), sizeof(nrt::InstDev) * e.pv.ninst,
-                           cudaMemcpyHostToDevice, e.stream));
-  NRT_CUDA(cudaStreamSynchronize(e.stream));
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!b || !runs) return nrt::fail(NRT_EINVAL, "null argument");
+    nrt::Engine &e = b->eng;
+    NRT_CUDA(cudaSetDevice(e.device));
+    for (int32_t i = 0; i < e.pv.ninst; i++) {
+      if (runs[i].i_end < runs[i].i_begin) return nrt::fail(NRT_EINVAL, "i_end < i_begin");
+      b->runs[i] = runs[i];
+      e.host.inst[i].base = runs[i].i_begin;
+      e.host.inst[i].iend = runs[i].i_end;
+      e.host.inst[i].t0 = runs[i].init_time;
+      e.host.inst[i].t1 = runs[i].end_input;
+      nrt::set_window(e.host.inst[i]);
+    }
+    NRT_CUDA(cudaMemcpyAsync(e.pv.inst, e.host.inst.data(), sizeof(nrt::InstDev) * e.pv.ninst,
+                             cudaMemcpyHostToDevice, e.stream));
+    NRT_CUDA(cudaStreamSynchronize(e.stream));
+    return NRT_OK;
+  });
 }
 
 int nrt_batch_advance(nrt_batch *b, int64_t steps) {
-  if (!b || steps < 0) return nrt::fail(NRT_EINVAL, "bad arguments");
-  NRT_CUDA(cudaSetDevice(b->eng.device));
-  return b->eng.advance(steps);
+  return nrt::guarded([&]() -> int {
+    if (!b || steps < 0) return nrt::fail(NRT_EINVAL, "bad arguments");
+    NRT_CUDA(cudaSetDevice(b->eng.device));
+    return b->eng.advance(steps);
+  });
 }
 
 int nrt_batch_synchronize(nrt_batch *b) {
-  if (!b) return nrt::fail(NRT_EINVAL, "null batch");
-  NRT_CUDA(cudaSetDevice(b->eng.device));
-  NRT_CUDA(cudaStreamSynchronize(b->eng.stream));
-  return nrt::implicit_check(b->eng);
+  return nrt::guarded([&]() -> int {
+    if (!b) return nrt::fail(NRT_EINVAL, "null batch");
+    NRT_CUDA(cudaSetDevice(b->eng.device));
+    NRT_CUDA(cudaStreamSynchronize(b->eng.stream));
+    return nrt::implicit_check(b->eng);
+  });
 }
 
 int nrt_batch_snapshot(nrt_batch *b, int32_t instance, double *potential) {
-  if (!b || !potential) return nrt::fail(NRT_EINVAL, "null argument");
-  nrt::Engine &e = b->eng;
-  if (instance < 0 || instance >= e.pv.ninst) return nrt::fail(NRT_EINVAL, "instance out of range");
-  NRT_CUDA(cudaSetDevice(e.device));
-  int rc = e.fixup();
-  if (rc) return rc;
-  const int64_t o = e.host.off[instance];
-  NRT_CUDA(cudaMemcpyAsync(potential, e.V[e.cur] + o, sizeof(double) * e.host.num_elem[instance],
-                           cudaMemcpyDeviceToHost, e.stream));
-  NRT_CUDA(cudaStreamSynchronize(e.stream));
-  return nrt::implicit_check(e);
+  return nrt::guarded([&]() -> int {
+    if (!b || !potential) return nrt::fail(NRT_EINVAL, "null argument");
+    nrt::Engine &e = b->eng;
+    if (instance < 0 || instance >= e.pv.ninst) return nrt::fail(NRT_EINVAL, "instance out of range");
+    NRT_CUDA(cudaSetDevice(e.device));
+    int rc = e.fixup();
+    if (rc) return rc;
+    const int64_t o = e.host.off[instance];
+    NRT_CUDA(cudaMemcpyAsync(potential, e.V[e.cur] + o, sizeof(double) * e.host.num_elem[instance],
+                             cudaMemcpyDeviceToHost, e.stream));
+    NRT_CUDA(cudaStreamSynchronize(e.stream));
+    return nrt::implicit_check(e);
+  });
 }
 
 int nrt_batch_snapshot_all(nrt_batch *b, double *potential) {
-  if (!b || !potential) return nrt::fail(NRT_EINVAL, "null argument");
-  nrt::Engine &e = b->eng;
-  NRT_CUDA(cudaSetDevice(e.device));
-  int rc = e.fixup();
-  if (rc) return rc;
-  NRT_CUDA(cudaMemcpyAsync(potential, e.V[e.cur], sizeof(double) * e.host.ntot,
-                           cudaMemcpyDeviceToHost, e.stream));
-  NRT_CUDA(cudaStreamSynchronize(e.stream));
-  return nrt::implicit_check(e);
+  return nrt::guarded([&]() -> int {
+    if (!b || !potential) return nrt::fail(NRT_EINVAL, "null argument");
+    nrt::Engine &e = b->eng;
+    NRT_CUDA(cudaSetDevice(e.device));
+    int rc = e.fixup();
+    if (rc) return rc;
+    NRT_CUDA(cudaMemcpyAsync(potential, e.V[e.cur], sizeof(double) * e.host.ntot,
+                             cudaMemcpyDeviceToHost, e.stream));
+    NRT_CUDA(cudaStreamSynchronize(e.stream));
+    return nrt::implicit_check(e);
+  });
 }
 
 int nrt_batch_remaining(nrt_batch *b, int64_t *remaining) {
-  if (!b || !remaining) return nrt::fail(NRT_EINVAL, "null argument");
-  nrt::Engine &e = b->eng;
-  NRT_CUDA(cudaSetDevice(e.device));
-  std::vector<nrt::InstDev> in(e.pv.ninst);
-  NRT_CUDA(cudaMemcpyAsync(in.data(), e.pv.inst, sizeof(nrt::InstDev) * e.pv.ninst,
-                           cudaMemcpyDeviceToHost, e.stream));
-  NRT_CUDA(cudaStreamSynchronize(e.stream));
-  for (int32_t i = 0; i < e.pv.ninst; i++) remaining[i] = in[i].iend - in[i].base;
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!b || !remaining) return nrt::fail(NRT_EINVAL, "null argument");
+    nrt::Engine &e = b->eng;
+    NRT_CUDA(cudaSetDevice(e.device));
+    std::vector<nrt::InstDev> in(e.pv.ninst);
+    NRT_CUDA(cudaMemcpyAsync(in.data(), e.pv.inst, sizeof(nrt::InstDev) * e.pv.ninst,
+                             cudaMemcpyDeviceToHost, e.stream));
+    NRT_CUDA(cudaStreamSynchronize(e.stream));
+    for (int32_t i = 0; i < e.pv.ninst; i++) remaining[i] = in[i].iend - in[i].base;
+    return NRT_OK;
+  });
 }
 
 int nrt_batch_get_stats(nrt_batch *b, nrt_stats *st) {
-  if (!b || !st) return nrt::fail(NRT_EINVAL, "null argument");
-  return b->eng.get_stats(st);
+  return nrt::guarded([&]() -> int {
+    if (!b || !st) return nrt::fail(NRT_EINVAL, "null argument");
+    return b->eng.get_stats(st);
+  });
 }
 
 int nrt_batch_instance_stats(nrt_batch *b, int64_t *iters, int32_t *last_iters,
                              int32_t *nonconverged, double *last_residual) {
-  if (!b) return nrt::fail(NRT_EINVAL, "null batch");
-  NRT_CUDA(cudaSetDevice(b->eng.device));
-  return nrt::instance_stats(b->eng, iters, last_iters, nonconverged, last_residual);
+  return nrt::guarded([&]() -> int {
+    if (!b) return nrt::fail(NRT_EINVAL, "null batch");
+    NRT_CUDA(cudaSetDevice(b->eng.device));
+    return nrt::instance_stats(b->eng, iters, last_iters, nonconverged, last_residual);
+  });
 }
 
 int nrt_batch_pass_counts(nrt_batch *b, int64_t *residuals, int64_t *precond_applies,
                           int64_t *xupdates, int64_t *basis_reads) {
-  if (!b) return nrt::fail(NRT_EINVAL, "null batch");
-  NRT_CUDA(cudaSetDevice(b->eng.device));
-  return nrt::pass_counts(b->eng, residuals, precond_applies, xupdates, basis_reads);
+  return nrt::guarded([&]() -> int {
+    if (!b) return nrt::fail(NRT_EINVAL, "null batch");
+    NRT_CUDA(cudaSetDevice(b->eng.device));
+    return nrt::pass_counts(b->eng, residuals, precond_applies, xupdates, basis_reads);
+  });
 }
 
 int nrt_batch_destroy(nrt_batch *b) {
-  delete b;
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    delete b;
+    return NRT_OK;
+  });
 }
 
 int nrt_get_state(nrt_solver *s, double *V, double *V_other, double *m, double *h, double *n) {
-  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
-  NRT_CUDA(cudaSetDevice(s->eng.device));
-  int rc = s->eng.get_state(0, V, V_other, m, h, n);
-  return rc ? rc : nrt::implicit_check(s->eng);
+  return nrt::guarded([&]() -> int {
+    if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+    NRT_CUDA(cudaSetDevice(s->eng.device));
+    int rc = s->eng.get_state(0, V, V_other, m, h, n);
+    return rc ? rc : nrt::implicit_check(s->eng);
+  });
 }
 
 int nrt_set_state(nrt_solver *s, const double *V, const double *V_other, const double *m,
                   const double *h, const double *n) {
-  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
-  NRT_CUDA(cudaSetDevice(s->eng.device));
-  return s->eng.set_state(0, V, V_other, m, h, n);
+  return nrt::guarded([&]() -> int {
+    if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+    NRT_CUDA(cudaSetDevice(s->eng.device));
+    return s->eng.set_state(0, V, V_other, m, h, n);
+  });
 }
 
 int nrt_batch_get_state(nrt_batch *b, int32_t instance, double *V, double *V_other, double *m,
                         double *h, double *n) {
-  if (!b) return nrt::fail(NRT_EINVAL, "null batch");
-  if (instance < 0 || instance >= b->eng.pv.ninst) return nrt::fail(NRT_EINVAL, "instance out of range");
-  NRT_CUDA(cudaSetDevice(b->eng.device));
-  int rc = b->eng.get_state(instance, V, V_other, m, h, n);
-  return rc ? rc : nrt::implicit_check(b->eng);
+  return nrt::guarded([&]() -> int {
+    if (!b) return nrt::fail(NRT_EINVAL, "null batch");
+    if (instance < 0 || instance >= b->eng.pv.ninst) return nrt::fail(NRT_EINVAL, "instance out of range");
+    NRT_CUDA(cudaSetDevice(b->eng.device));
+    int rc = b->eng.get_state(instance, V, V_other, m, h, n);
+    return rc ? rc : nrt::implicit_check(b->eng);
+  });
 }
 
 int nrt_batch_set_state(nrt_batch *b, int32_t instance, const double *V, const double *V_other,
                         const double *m, const double *h, const double *n) {
-  if (!b) return nrt::fail(NRT_EINVAL, "null batch");
-  if (instance < 0 || instance >= b->eng.pv.ninst) return nrt::fail(NRT_EINVAL, "instance out of range");
-  NRT_CUDA(cudaSetDevice(b->eng.device));
-  return b->eng.set_state(instance, V, V_other, m, h, n);
+  return nrt::guarded([&]() -> int {
+    if (!b) return nrt::fail(NRT_EINVAL, "null batch");
+    if (instance < 0 || instance >= b->eng.pv.ninst) return nrt::fail(NRT_EINVAL, "instance out of range");
+    NRT_CUDA(cudaSetDevice(b->eng.device));
+    return b->eng.set_state(instance, V, V_other, m, h, n);
+  });
 }
 
 int nrt_set_strain(nrt_solver *s, const nrt_strain_config *cfg) {
-  if (!s || !cfg) return nrt::fail(NRT_EINVAL, "null argument");
-  if (cfg->instance)
-    for (int32_t q = 0; q < cfg->num_elem; q++)
-      if (cfg->instance[q] != 0) return nrt::fail(NRT_EINVAL, "a solver has only instance 0");
-  NRT_CUDA(cudaSetDevice(s->eng.device));
-  return s->eng.strain_config(cfg);
+  return nrt::guarded([&]() -> int {
+    if (!s || !cfg) return nrt::fail(NRT_EINVAL, "null argument");
+    if (cfg->instance)
+      for (int32_t q = 0; q < cfg->num_elem; q++)
+        if (cfg->instance[q] != 0) return nrt::fail(NRT_EINVAL, "a solver has only instance 0");
+    NRT_CUDA(cudaSetDevice(s->eng.device));
+    return s->eng.strain_config(cfg);
+  });
 }
 
 int nrt_batch_set_strain(nrt_batch *b, const nrt_strain_config *cfg) {
-  if (!b || !cfg) return nrt::fail(NRT_EINVAL, "null argument");
-  NRT_CUDA(cudaSetDevice(b->eng.device));
-  return b->eng.strain_config(cfg);
+  return nrt::guarded([&]() -> int {
+    if (!b || !cfg) return nrt::fail(NRT_EINVAL, "null argument");
+    NRT_CUDA(cudaSetDevice(b->eng.device));
+    return b->eng.strain_config(cfg);
+  });
 }
 
 int nrt_record(nrt_solver *s, const nrt_record_config *cfg) {
-  if (!s || !cfg) return nrt::fail(NRT_EINVAL, "null argument");
-  if (cfg->instance)
-    for (int32_t p = 0; p < cfg->num_probes; p++)
-      if (cfg->instance[p] != 0) return nrt::fail(NRT_EINVAL, "a solver has only instance 0");
-  NRT_CUDA(cudaSetDevice(s->eng.device));
-  return s->eng.record_config(cfg);
+  return nrt::guarded([&]() -> int {
+    if (!s || !cfg) return nrt::fail(NRT_EINVAL, "null argument");
+    if (cfg->instance)
+      for (int32_t p = 0; p < cfg->num_probes; p++)
+        if (cfg->instance[p] != 0) return nrt::fail(NRT_EINVAL, "a solver has only instance 0");
+    NRT_CUDA(cudaSetDevice(s->eng.device));
+    return s->eng.record_config(cfg);
+  });
 }
 
 int nrt_batch_record(nrt_batch *b, const nrt_record_config *cfg) {
-  if (!b || !cfg) return nrt::fail(NRT_EINVAL, "null argument");
-  NRT_CUDA(cudaSetDevice(b->eng.device));
-  return b->eng.record_config(cfg);
+  return nrt::guarded([&]() -> int {
+    if (!b || !cfg) return nrt::fail(NRT_EINVAL, "null argument");
+    NRT_CUDA(cudaSetDevice(b->eng.device));
+    return b->eng.record_config(cfg);
+  });
 }
 
 int nrt_record_read(nrt_solver *s, int64_t *num_samples, double *times, double *values,
                     int32_t *num_spikes, double *spike_times) {
-  if (!s) return nrt::fail(NRT_EINVAL, "null solver");
-  NRT_CUDA(cudaSetDevice(s->eng.device));
-  int rc = s->eng.record_read(num_samples, times, values, num_spikes, spike_times);
-  return rc ? rc : nrt::implicit_check(s->eng);
+  return nrt::guarded([&]() -> int {
+    if (!s) return nrt::fail(NRT_EINVAL, "null solver");
+    NRT_CUDA(cudaSetDevice(s->eng.device));
+    int rc = s->eng.record_read(num_samples, times, values, num_spikes, spike_times);
+    return rc ? rc : nrt::implicit_check(s->eng);
+  });
 }
 
 int nrt_batch_record_read(nrt_batch *b, int64_t *num_samples, double *times, double *values,
                           int32_t *num_spikes, double *spike_times) {
-  if (!b) return nrt::fail(NRT_EINVAL, "null batch");
-  NRT_CUDA(cudaSetDevice(b->eng.device));
-  int rc = b->eng.record_read(num_samples, times, values, num_spikes, spike_times);
-  return rc ? rc : nrt::implicit_check(b->eng);
+  return nrt::guarded([&]() -> int {
+    if (!b) return nrt::fail(NRT_EINVAL, "null batch");
+    NRT_CUDA(cudaSetDevice(b->eng.device));
+    int rc = b->eng.record_read(num_samples, times, values, num_spikes, spike_times);
+    return rc ? rc : nrt::implicit_check(b->eng);
+  });
 }
 
 }  // extern "C"

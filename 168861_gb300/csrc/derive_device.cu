@@ -123,70 +123,72 @@ extern "C" int nrt_derive_batch(int32_t count, const int64_t *offsets, const int
                                 const double *dspec, const int32_t *myelin, const double *e_max,
                                 double *eparam, int32_t *hh_elem, double *hparam,
                                 int64_t *hh_offsets, double *dT_crit) {
-  using namespace nrt;
-  if (count < 1 || !offsets || !ispec || !dspec || !myelin || !e_max || !eparam ||
-      !hh_offsets || !dT_crit) {
-    set_error("null argument or count < 1");
-    return NRT_EINVAL;
-  }
-  if (offsets[0] != 0) {
-    set_error("offsets[0] must be 0");
-    return NRT_EINVAL;
-  }
-  for (int32_t t = 0; t < count; t++)
-    if (offsets[t + 1] - offsets[t] < 4) {
-      set_error("tree " + std::to_string(t) + " has fewer than 4 elements");
+  return nrt::guarded([&]() -> int {
+    using namespace nrt;
+    if (count < 1 || !offsets || !ispec || !dspec || !myelin || !e_max || !eparam ||
+        !hh_offsets || !dT_crit) {
+      set_error("null argument or count < 1");
       return NRT_EINVAL;
     }
-  const int64_t T = offsets[count];
-  // HH counts per tree (the kind row is on the host already)
-  std::vector<int64_t> cnt(count, 0);
-  parallel_for(count, [&](int64_t t) {
-    int64_t c = 0;
-    for (int64_t i = offsets[t]; i < offsets[t + 1]; i++) c += ispec[i] == 1;
-    cnt[t] = c;
+    if (offsets[0] != 0) {
+      set_error("offsets[0] must be 0");
+      return NRT_EINVAL;
+    }
+    for (int32_t t = 0; t < count; t++)
+      if (offsets[t + 1] - offsets[t] < 4) {
+        set_error("tree " + std::to_string(t) + " has fewer than 4 elements");
+        return NRT_EINVAL;
+      }
+    const int64_t T = offsets[count];
+    // HH counts per tree (the kind row is on the host already)
+    std::vector<int64_t> cnt(count, 0);
+    parallel_for(count, [&](int64_t t) {
+      int64_t c = 0;
+      for (int64_t i = offsets[t]; i < offsets[t + 1]; i++) c += ispec[i] == 1;
+      cnt[t] = c;
+    });
+    hh_offsets[0] = 0;
+    for (int32_t t = 0; t < count; t++) hh_offsets[t + 1] = hh_offsets[t] + cnt[t];
+    const int64_t H = hh_offsets[count];
+    if (H > 0 && (!hh_elem || !hparam)) {
+      set_error("null HH output");
+      return NRT_EINVAL;
+    }
+    cudaStream_t st;
+    NRT_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    struct StreamGuard {
+      cudaStream_t s;
+      ~StreamGuard() { cudaStreamDestroy(s); }
+    } guard{st};
+    DevBufs d;
+    int64_t *d_off = d.take<int64_t>(count + 1), *d_hoff = d.take<int64_t>(count + 1);
+    int32_t *d_kind = d.take<int32_t>(T), *d_my = d.take<int32_t>(count),
+            *d_hh = d.take<int32_t>(H);
+    double *d_ds = d.take<double>(12 * (size_t)T), *d_em = d.take<double>(count),
+           *d_ep = d.take<double>(6 * (size_t)T), *d_hp = d.take<double>(12 * (size_t)H),
+           *d_dt = d.take<double>(count);
+    if (!d_off || !d_hoff || !d_kind || !d_my || !d_hh || !d_ds || !d_em || !d_ep || !d_hp ||
+        !d_dt) {
+      cudaGetLastError();
+      set_error("device allocation for the derivation");
+      return NRT_ENOMEM;
+    }
+    NRT_CUDA(cudaMemcpyAsync(d_off, offsets, 8 * (size_t)(count + 1), cudaMemcpyHostToDevice, st));
+    NRT_CUDA(cudaMemcpyAsync(d_hoff, hh_offsets, 8 * (size_t)(count + 1), cudaMemcpyHostToDevice, st));
+    NRT_CUDA(cudaMemcpyAsync(d_kind, ispec, 4 * (size_t)T, cudaMemcpyHostToDevice, st));
+    NRT_CUDA(cudaMemcpyAsync(d_my, myelin, 4 * (size_t)count, cudaMemcpyHostToDevice, st));
+    NRT_CUDA(cudaMemcpyAsync(d_ds, dspec, 8 * 12 * (size_t)T, cudaMemcpyHostToDevice, st));
+    NRT_CUDA(cudaMemcpyAsync(d_em, e_max, 8 * (size_t)count, cudaMemcpyHostToDevice, st));
+    DeriveArgs a{d_off, d_hoff, d_kind, d_ds, d_my, d_em, d_ep, d_hh, d_hp, d_dt, T, H};
+    derive_trees<<<count, kDThreads, 0, st>>>(a);
+    NRT_CUDA(cudaGetLastError());
+    NRT_CUDA(cudaMemcpyAsync(eparam, d_ep, 8 * 6 * (size_t)T, cudaMemcpyDeviceToHost, st));
+    if (H > 0) {
+      NRT_CUDA(cudaMemcpyAsync(hh_elem, d_hh, 4 * (size_t)H, cudaMemcpyDeviceToHost, st));
+      NRT_CUDA(cudaMemcpyAsync(hparam, d_hp, 8 * 12 * (size_t)H, cudaMemcpyDeviceToHost, st));
+    }
+    NRT_CUDA(cudaMemcpyAsync(dT_crit, d_dt, 8 * (size_t)count, cudaMemcpyDeviceToHost, st));
+    NRT_CUDA(cudaStreamSynchronize(st));
+    return NRT_OK;
   });
-  hh_offsets[0] = 0;
-  for (int32_t t = 0; t < count; t++) hh_offsets[t + 1] = hh_offsets[t] + cnt[t];
-  const int64_t H = hh_offsets[count];
-  if (H > 0 && (!hh_elem || !hparam)) {
-    set_error("null HH output");
-    return NRT_EINVAL;
-  }
-  cudaStream_t st;
-  NRT_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  struct StreamGuard {
-    cudaStream_t s;
-    ~StreamGuard() { cudaStreamDestroy(s); }
-  } guard{st};
-  DevBufs d;
-  int64_t *d_off = d.take<int64_t>(count + 1), *d_hoff = d.take<int64_t>(count + 1);
-  int32_t *d_kind = d.take<int32_t>(T), *d_my = d.take<int32_t>(count),
-          *d_hh = d.take<int32_t>(H);
-  double *d_ds = d.take<double>(12 * (size_t)T), *d_em = d.take<double>(count),
-         *d_ep = d.take<double>(6 * (size_t)T), *d_hp = d.take<double>(12 * (size_t)H),
-         *d_dt = d.take<double>(count);
-  if (!d_off || !d_hoff || !d_kind || !d_my || !d_hh || !d_ds || !d_em || !d_ep || !d_hp ||
-      !d_dt) {
-    cudaGetLastError();
-    set_error("device allocation for the derivation");
-    return NRT_ENOMEM;
-  }
-  NRT_CUDA(cudaMemcpyAsync(d_off, offsets, 8 * (size_t)(count + 1), cudaMemcpyHostToDevice, st));
-  NRT_CUDA(cudaMemcpyAsync(d_hoff, hh_offsets, 8 * (size_t)(count + 1), cudaMemcpyHostToDevice, st));
-  NRT_CUDA(cudaMemcpyAsync(d_kind, ispec, 4 * (size_t)T, cudaMemcpyHostToDevice, st));
-  NRT_CUDA(cudaMemcpyAsync(d_my, myelin, 4 * (size_t)count, cudaMemcpyHostToDevice, st));
-  NRT_CUDA(cudaMemcpyAsync(d_ds, dspec, 8 * 12 * (size_t)T, cudaMemcpyHostToDevice, st));
-  NRT_CUDA(cudaMemcpyAsync(d_em, e_max, 8 * (size_t)count, cudaMemcpyHostToDevice, st));
-  DeriveArgs a{d_off, d_hoff, d_kind, d_ds, d_my, d_em, d_ep, d_hh, d_hp, d_dt, T, H};
-  derive_trees<<<count, kDThreads, 0, st>>>(a);
-  NRT_CUDA(cudaGetLastError());
-  NRT_CUDA(cudaMemcpyAsync(eparam, d_ep, 8 * 6 * (size_t)T, cudaMemcpyDeviceToHost, st));
-  if (H > 0) {
-    NRT_CUDA(cudaMemcpyAsync(hh_elem, d_hh, 4 * (size_t)H, cudaMemcpyDeviceToHost, st));
-    NRT_CUDA(cudaMemcpyAsync(hparam, d_hp, 8 * 12 * (size_t)H, cudaMemcpyDeviceToHost, st));
-  }
-  NRT_CUDA(cudaMemcpyAsync(dT_crit, d_dt, 8 * (size_t)count, cudaMemcpyDeviceToHost, st));
-  NRT_CUDA(cudaStreamSynchronize(st));
-  return NRT_OK;
 }

@@ -9,6 +9,7 @@
 #include <thread>
 #include <vector>
 
+#include "guard.h"
 #include "neurite_gb300.h"
 
 namespace nrt {

@@ -20,12 +20,14 @@
 #include <map>
 #include <mutex>
 #include <new>
+#include <stdexcept>
 #include <string>
 #include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
 
+#include "guard.h"
 #include "neurite_gb300.h"
 
 namespace {
@@ -111,6 +113,7 @@ struct MicroBatch {
   size_t bytes = 0;
   size_t open = 0;
   int64_t per_tick = 0;            // steps per tick, adapted to the target tick time
+  int adv_rc = NRT_OK;             // first failure of nrt_batch_advance: ends every open request
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaStream_t stream = nullptr;
 };
@@ -280,14 +283,15 @@ void nrt_server::loop() {
     // one tick: every resident batch advances on its own stream (all enqueued first)
     for (MicroBatch *mb : active) {
       cudaEventRecord(mb->ev0, mb->stream);
-      nrt_batch_advance(mb->b, mb->per_tick);
+      const int arc = nrt_batch_advance(mb->b, mb->per_tick);
+      if (arc != NRT_OK && mb->adv_rc == NRT_OK) mb->adv_rc = arc;
       cudaEventRecord(mb->ev1, mb->stream);
     }
     // collect finished requests
     std::vector<int64_t> rem;
     for (MicroBatch *mb : active) {
       rem.assign(mb->reqs.size(), 0);
-      int rc = nrt_batch_remaining(mb->b, rem.data());
+      int rc = mb->adv_rc != NRT_OK ? mb->adv_rc : nrt_batch_remaining(mb->b, rem.data());
       float ms = 0;
       if (cudaEventElapsedTime(&ms, mb->ev0, mb->ev1) == cudaSuccess && ms > 0) {
         // steps per tick toward the target tick time (explicit steps are ~1000x cheaper)
@@ -362,7 +366,9 @@ void nrt_server::loop() {
         a++;
       }
     }
-    busy += std::chrono::duration<double>(Clock::now() - t0).count();
+    const double tick_s = std::chrono::duration<double>(Clock::now() - t0).count();
+    std::lock_guard<std::mutex> lk(mu);  // nrt_server_get_stats reads it
+    busy += tick_s;
   }
 }
 
@@ -380,17 +386,22 @@ static int submit_request(nrt_server *s, const nrt_problem *p, int implicit,
   }
   Request *r = new (std::nothrow) Request();
   if (!r) return NRT_ENOMEM;
-  r->implicit = implicit != 0;
-  r->prob.copy(*p);
-  r->run = *run;
-  if (rec && rec->num_probes > 0) {  // complete before the worker can see the request
-    r->rec.on = true;
-    r->rec.origin = rec->origin;
-    r->rec.interval = rec->interval;
-    r->rec.capacity = rec->capacity;
-    r->rec.threshold = rec->threshold;
-    r->rec.max_spikes = rec->max_spikes;
-    r->probes.assign(rec->element, rec->element + rec->num_probes);
+  try {  // host copies of the request: no exception crosses the C boundary
+    r->implicit = implicit != 0;
+    r->prob.copy(*p);
+    r->run = *run;
+    if (rec && rec->num_probes > 0) {  // complete before the worker can see the request
+      r->rec.on = true;
+      r->rec.origin = rec->origin;
+      r->rec.interval = rec->interval;
+      r->rec.capacity = rec->capacity;
+      r->rec.threshold = rec->threshold;
+      r->rec.max_spikes = rec->max_spikes;
+      r->probes.assign(rec->element, rec->element + rec->num_probes);
+    }
+  } catch (const std::exception &) {
+    delete r;
+    return NRT_ENOMEM;
   }
   r->bytes = estimate_bytes(*p, s->opt[r->implicit ? 1 : 0]);
   r->t_submit = Clock::now();
@@ -414,106 +425,127 @@ extern "C" {
 
 int nrt_server_create(const nrt_server_config *cfg, const nrt_options *explicit_opt,
                       const nrt_options *implicit_opt, nrt_server **out) {
-  if (!cfg || !out || cfg->budget_bytes <= 0) return NRT_EINVAL;
-  nrt_server *s = new (std::nothrow) nrt_server();
-  if (!s) return NRT_ENOMEM;
-  s->cfg = *cfg;
-  if (s->cfg.chunk_steps <= 0) s->cfg.chunk_steps = 64;
-  if (s->cfg.max_batch <= 0) s->cfg.max_batch = 4096;
-  if (s->cfg.max_wait_us < 0) s->cfg.max_wait_us = 0;
-  nrt_options_default(&s->opt[0]);
-  nrt_options_default(&s->opt[1]);
-  if (explicit_opt) s->opt[0] = *explicit_opt;
-  if (implicit_opt) s->opt[1] = *implicit_opt;
-  s->opt[0].mode = NRT_EXPLICIT;
-  s->opt[1].mode = NRT_IMPLICIT_BE;
-  s->opt[1].schedule = 1;  // block per instance: resident batches share the GPU
-  s->worker = std::thread([s] { s->loop(); });
-  *out = s;
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!cfg || !out || cfg->budget_bytes <= 0) return NRT_EINVAL;
+    nrt_server *s = new (std::nothrow) nrt_server();
+    if (!s) return NRT_ENOMEM;
+    s->cfg = *cfg;
+    if (s->cfg.chunk_steps <= 0) s->cfg.chunk_steps = 64;
+    if (s->cfg.max_batch <= 0) s->cfg.max_batch = 4096;
+    if (s->cfg.max_wait_us < 0) s->cfg.max_wait_us = 0;
+    nrt_options_default(&s->opt[0]);
+    nrt_options_default(&s->opt[1]);
+    if (explicit_opt) s->opt[0] = *explicit_opt;
+    if (implicit_opt) s->opt[1] = *implicit_opt;
+    s->opt[0].mode = NRT_EXPLICIT;
+    s->opt[1].mode = NRT_IMPLICIT_BE;
+    s->opt[1].schedule = 1;  // block per instance: resident batches share the GPU
+    try {
+      s->worker = std::thread([s] { s->loop(); });
+    } catch (const std::exception &) {
+      delete s;
+      return NRT_ENOMEM;
+    }
+    *out = s;
+    return NRT_OK;
+  });
 }
 
 int nrt_server_submit(nrt_server *s, const nrt_problem *p, int implicit,
                       const nrt_instance_run *run, int64_t *request_id) {
-  return submit_request(s, p, implicit, run, nullptr, request_id);
+  return nrt::guarded([&]() -> int {
+    return submit_request(s, p, implicit, run, nullptr, request_id);
+  });
 }
 
 int nrt_server_submit_recorded(nrt_server *s, const nrt_problem *p, int implicit,
                                const nrt_instance_run *run, const nrt_record_config *rec,
                                int64_t *request_id) {
-  if (!rec) return NRT_EINVAL;
-  return submit_request(s, p, implicit, run, rec, request_id);
+  return nrt::guarded([&]() -> int {
+    if (!rec) return NRT_EINVAL;
+    return submit_request(s, p, implicit, run, rec, request_id);
+  });
 }
 
 int nrt_server_recording(nrt_server *s, int64_t id, int64_t *num_samples, double *times,
                          double *values, int32_t *num_spikes, double *spike_times) {
-  if (!s) return NRT_EINVAL;
-  std::lock_guard<std::mutex> lk(s->mu);
-  auto it = s->reqs.find(id);
-  if (it == s->reqs.end()) return NRT_ESTATE;
-  Request *r = it->second;
-  if (!r->done) return NRT_ENOTREADY;
-  if (!r->rec.on) return NRT_ESTATE;
-  if (r->rec_ns.size() != r->probes.size()) return r->status != NRT_OK ? r->status : NRT_EDEVICE;
-  if (num_samples) std::copy(r->rec_ns.begin(), r->rec_ns.end(), num_samples);
-  if (num_spikes) std::copy(r->rec_nk.begin(), r->rec_nk.end(), num_spikes);
-  if (times) std::copy(r->rec_t.begin(), r->rec_t.end(), times);
-  if (values) std::copy(r->rec_v.begin(), r->rec_v.end(), values);
-  if (spike_times) std::copy(r->rec_sp.begin(), r->rec_sp.end(), spike_times);
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!s) return NRT_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return NRT_ESTATE;
+    Request *r = it->second;
+    if (!r->done) return NRT_ENOTREADY;
+    if (!r->rec.on) return NRT_ESTATE;
+    if (r->rec_ns.size() != r->probes.size()) return r->status != NRT_OK ? r->status : NRT_EDEVICE;
+    if (num_samples) std::copy(r->rec_ns.begin(), r->rec_ns.end(), num_samples);
+    if (num_spikes) std::copy(r->rec_nk.begin(), r->rec_nk.end(), num_spikes);
+    if (times) std::copy(r->rec_t.begin(), r->rec_t.end(), times);
+    if (values) std::copy(r->rec_v.begin(), r->rec_v.end(), values);
+    if (spike_times) std::copy(r->rec_sp.begin(), r->rec_sp.end(), spike_times);
+    return NRT_OK;
+  });
 }
 
 int nrt_server_result(nrt_server *s, int64_t id, double *potential) {
-  if (!s || !potential) return NRT_EINVAL;
-  std::lock_guard<std::mutex> lk(s->mu);
-  auto it = s->reqs.find(id);
-  if (it == s->reqs.end()) return NRT_ESTATE;
-  Request *r = it->second;
-  if (!r->done) return NRT_ENOTREADY;
-  const int status = r->status;
-  if (!r->result.empty()) memcpy(potential, r->result.data(), sizeof(double) * r->result.size());
-  s->reqs.erase(it);
-  delete r;
-  return status;
+  return nrt::guarded([&]() -> int {
+    if (!s || !potential) return NRT_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return NRT_ESTATE;
+    Request *r = it->second;
+    if (!r->done) return NRT_ENOTREADY;
+    const int status = r->status;
+    if (!r->result.empty()) memcpy(potential, r->result.data(), sizeof(double) * r->result.size());
+    s->reqs.erase(it);
+    delete r;
+    return status;
+  });
 }
 
 int nrt_server_drain(nrt_server *s) {
-  if (!s) return NRT_EINVAL;
-  std::unique_lock<std::mutex> lk(s->mu);
-  s->cv_done.wait(lk, [&] { return s->outstanding == 0; });
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!s) return NRT_EINVAL;
+    std::unique_lock<std::mutex> lk(s->mu);
+    s->cv_done.wait(lk, [&] { return s->outstanding == 0; });
+    return NRT_OK;
+  });
 }
 
 int nrt_server_get_stats(nrt_server *s, nrt_server_stats *st) {
-  if (!s || !st) return NRT_EINVAL;
-  std::lock_guard<std::mutex> lk(s->mu);
-  *st = s->st;
-  std::vector<double> l = s->lat_ms;
-  std::sort(l.begin(), l.end());
-  auto pct = [&](double q) {
-    if (l.empty()) return 0.0;
-    const size_t k = (size_t)std::min<double>(l.size() - 1, floor(q * (l.size() - 1) + 0.5));
-    return l[k];
-  };
-  st->p50_ms = pct(0.50);
-  st->p99_ms = pct(0.99);
-  st->max_ms = l.empty() ? 0.0 : l.back();
-  st->busy_seconds = s->busy;
-  st->peak_bytes = (int64_t)s->peak;
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!s || !st) return NRT_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *st = s->st;
+    std::vector<double> l = s->lat_ms;
+    std::sort(l.begin(), l.end());
+    auto pct = [&](double q) {
+      if (l.empty()) return 0.0;
+      const size_t k = (size_t)std::min<double>(l.size() - 1, floor(q * (l.size() - 1) + 0.5));
+      return l[k];
+    };
+    st->p50_ms = pct(0.50);
+    st->p99_ms = pct(0.99);
+    st->max_ms = l.empty() ? 0.0 : l.back();
+    st->busy_seconds = s->busy;
+    st->peak_bytes = (int64_t)s->peak;
+    return NRT_OK;
+  });
 }
 
 int nrt_server_destroy(nrt_server *s) {
-  if (!s) return NRT_EINVAL;
-  {
-    std::lock_guard<std::mutex> lk(s->mu);
-    s->stop = true;
-  }
-  s->cv_work.notify_all();
-  if (s->worker.joinable()) s->worker.join();
-  for (auto &kv : s->reqs) delete kv.second;
-  delete s;
-  return NRT_OK;
+  return nrt::guarded([&]() -> int {
+    if (!s) return NRT_EINVAL;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->stop = true;
+    }
+    s->cv_work.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    for (auto &kv : s->reqs) delete kv.second;
+    delete s;
+    return NRT_OK;
+  });
 }
 
 }  // extern "C"

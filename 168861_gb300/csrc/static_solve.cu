@@ -281,75 +281,77 @@ extern "C" int nrt_solve_csr_static(int32_t n, const int32_t *row_ptr, const int
                                     int32_t restart, double tol, int32_t tol_mode,
                                     int32_t max_iter, void *stream, int32_t *iters_out,
                                     double *residual_out) {
-  using namespace nrt;
-  if (n < 1 || !row_ptr || !col || !val || !b || !x || !(tol > 0) || max_iter < 0 ||
-      (tol_mode != NRT_TOL_ABS && tol_mode != NRT_TOL_REL)) {
-    set_error("nrt_solve_csr_static: bad argument");
-    return NRT_EINVAL;
-  }
-  if (restart < 1 || restart > kM) {
-    set_error("nrt_solve_csr_static: restart must be in [1, NRT_STATIC_MAX_RESTART]");
-    return NRT_EINVAL;
-  }
-  const Layout L = layout(n, restart);
-  if (L.total * sizeof(double) > (size_t)NRT_STATIC_SCRATCH_BYTES) {
-    set_error("nrt_solve_csr_static: n * (2 * restart + 5) doubles exceed the static scratch "
-              "(NRT_STATIC_SCRATCH_BYTES); use a smaller restart or the handle API");
-    return NRT_EBUDGET;
-  }
-  int dev = 0;
-  NRT_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) {
-    set_error("nrt_solve_csr_static: device ordinal out of range");
-    return NRT_EDEVICE;
-  }
-  double *scratch;
-  {
-    // Once per device, with that device current: the device address of the static array.
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
-      void *p = nullptr;
-      NRT_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
-      g_scratch_ptr[dev] = (double *)p;
+  return nrt::guarded([&]() -> int {
+    using namespace nrt;
+    if (n < 1 || !row_ptr || !col || !val || !b || !x || !(tol > 0) || max_iter < 0 ||
+        (tol_mode != NRT_TOL_ABS && tol_mode != NRT_TOL_REL)) {
+      set_error("nrt_solve_csr_static: bad argument");
+      return NRT_EINVAL;
     }
-    scratch = g_scratch_ptr[dev];
-  }
-  int sms = 0, per_sm = 0;
-  NRT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  NRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, static_gmres, kT, 0));
-  if (per_sm < 1) {
-    set_error("nrt_solve_csr_static: kernel does not fit on an SM");
-    return NRT_EDEVICE;
-  }
-  // rows per CTA: whole preconditioner blocks, at least 4 rows per thread
-  int G = (int)std::min<long long>((long long)sms * per_sm, kMaxG);
-  int rows = (((n + G - 1) / G + kBlk - 1) / kBlk) * kBlk;
-  rows = std::max(rows, 4 * kBlk);
-  G = (n + rows - 1) / rows;
-  Args a;
-  a.n = n;
-  a.m = restart;
-  a.tol = tol;
-  a.tol_mode = tol_mode;
-  a.max_iter = max_iter;
-  a.rows_per_cta = rows;
-  a.row_ptr = row_ptr;
-  a.col = col;
-  a.val = val;
-  a.b = b;
-  a.x = x;
-  a.scratch = scratch;
-  void *args[] = {&a};
-  cudaStream_t st = (cudaStream_t)stream;
-  NRT_CUDA(cudaLaunchCooperativeKernel((const void *)static_gmres, dim3(G), dim3(kT), args, 0, st));
-  double res[3];
-  NRT_CUDA(cudaMemcpyAsync(res, scratch + L.result, sizeof(res), cudaMemcpyDeviceToHost, st));
-  NRT_CUDA(cudaStreamSynchronize(st));
-  if (iters_out) *iters_out = (int32_t)res[0];
-  if (residual_out) *residual_out = res[1];
-  if (res[2] == 0.0) {
-    set_error("nrt_solve_csr_static: iteration budget reached");
-    return NRT_ENOCONV;
-  }
-  return NRT_OK;
+    if (restart < 1 || restart > kM) {
+      set_error("nrt_solve_csr_static: restart must be in [1, NRT_STATIC_MAX_RESTART]");
+      return NRT_EINVAL;
+    }
+    const Layout L = layout(n, restart);
+    if (L.total * sizeof(double) > (size_t)NRT_STATIC_SCRATCH_BYTES) {
+      set_error("nrt_solve_csr_static: n * (2 * restart + 5) doubles exceed the static scratch "
+                "(NRT_STATIC_SCRATCH_BYTES); use a smaller restart or the handle API");
+      return NRT_EBUDGET;
+    }
+    int dev = 0;
+    NRT_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+      set_error("nrt_solve_csr_static: device ordinal out of range");
+      return NRT_EDEVICE;
+    }
+    double *scratch;
+    {
+      // Once per device, with that device current: the device address of the static array.
+      std::lock_guard<std::mutex> lk(g_setup_mu);
+      if (!g_scratch_ptr[dev]) {
+        void *p = nullptr;
+        NRT_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
+        g_scratch_ptr[dev] = (double *)p;
+      }
+      scratch = g_scratch_ptr[dev];
+    }
+    int sms = 0, per_sm = 0;
+    NRT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    NRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, static_gmres, kT, 0));
+    if (per_sm < 1) {
+      set_error("nrt_solve_csr_static: kernel does not fit on an SM");
+      return NRT_EDEVICE;
+    }
+    // rows per CTA: whole preconditioner blocks, at least 4 rows per thread
+    int G = (int)std::min<long long>((long long)sms * per_sm, kMaxG);
+    int rows = (((n + G - 1) / G + kBlk - 1) / kBlk) * kBlk;
+    rows = std::max(rows, 4 * kBlk);
+    G = (n + rows - 1) / rows;
+    Args a;
+    a.n = n;
+    a.m = restart;
+    a.tol = tol;
+    a.tol_mode = tol_mode;
+    a.max_iter = max_iter;
+    a.rows_per_cta = rows;
+    a.row_ptr = row_ptr;
+    a.col = col;
+    a.val = val;
+    a.b = b;
+    a.x = x;
+    a.scratch = scratch;
+    void *args[] = {&a};
+    cudaStream_t st = (cudaStream_t)stream;
+    NRT_CUDA(cudaLaunchCooperativeKernel((const void *)static_gmres, dim3(G), dim3(kT), args, 0, st));
+    double res[3];
+    NRT_CUDA(cudaMemcpyAsync(res, scratch + L.result, sizeof(res), cudaMemcpyDeviceToHost, st));
+    NRT_CUDA(cudaStreamSynchronize(st));
+    if (iters_out) *iters_out = (int32_t)res[0];
+    if (residual_out) *residual_out = res[1];
+    if (res[2] == 0.0) {
+      set_error("nrt_solve_csr_static: iteration budget reached");
+      return NRT_ENOCONV;
+    }
+    return NRT_OK;
+  });
 }
