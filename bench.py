@@ -232,26 +232,25 @@ def algorithmic_bytes_explicit(probs, precision: str) -> float:
     fb = 8 if precision == "fp64" else 4
     total = 0.0
     for p in probs:
-        a = p.arrays
         n, n_hh = p.num_elem, int(p.struct.num_hh)
-        geo = 2 * fb if (_varies(a["c_m"] * a["dx"]) or _varies(a["r_a"] * a["dx"])) else 0
-        chan = sum(fb for k in ("g_Na", "g_K", "G_L", "E_Na", "E_K", "E_L", "ls_Na", "ls_K")
-                   if _varies(a[k]))
-        passive = np.ones(n, bool)
-        passive[a["hh_elem"]] = False
-        wk = 2 * fb if (_varies(a["W"][passive]) or _varies(a["K"][passive])) else 0
-        total += n_hh * (16 + 6 * fb + 4 + geo + chan) + (n - n_hh) * (16 + 4 + geo + wk)
+        ph, pp = _param_bytes(p, fb)
+        total += n_hh * (16 + 6 * fb + 4 + ph) + (n - n_hh) * (16 + 4 + pp)
     return total
 
 
 def _param_bytes(p, fb: int):
     """Per-compartment parameter bytes the rule counts (where they vary within the tree):
-    (HH compartments, passive compartments)."""
+    (HH compartments, passive compartments).  Variation is judged over the compartments a
+    step computes: the terminals (the fictitious root and the sealed ends) are copies of
+    their neighbours and stream no coefficients."""
     a = p.arrays
-    geo = 2 * fb if (_varies(a["c_m"] * a["dx"]) or _varies(a["r_a"] * a["dx"])) else 0
+    core = np.ones(p.num_elem, bool)
+    core[np.asarray(a["terminals"], np.int64)] = False
+    geo = 2 * fb if (_varies((a["c_m"] * a["dx"])[core]) or
+                     _varies((a["r_a"] * a["dx"])[core])) else 0
     chan = sum(fb for k in ("g_Na", "g_K", "G_L", "E_Na", "E_K", "E_L", "ls_Na", "ls_K")
                if _varies(a[k]))
-    passive = np.ones(p.num_elem, bool)
+    passive = core.copy()
     passive[a["hh_elem"]] = False
     wk = 2 * fb if (_varies(a["W"][passive]) or _varies(a["K"][passive])) else 0
     return geo + chan, geo + wk
