@@ -43,7 +43,8 @@ class Options(ctypes.Structure):
         ("tol", ctypes.c_double), ("max_iter", ctypes.c_int32), ("device", ctypes.c_int32),
         ("use_graphs", ctypes.c_int32), ("schedule", ctypes.c_int32),
         ("tiled", ctypes.c_int32), ("scheme", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 4),
+        ("tile_ctas_per_sm", ctypes.c_int32), ("step_threads", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 2),
     ]
 
 

@@ -428,7 +428,8 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   NRT_CUDA(cudaMemsetAsync(err, 0, 16, st));
   pv.err = err;
   pv.tile_blocks = (mixed && opt.mode == NRT_EXPLICIT && opt.tiled != 0)
-                       ? explicit_tile_blocks(device, N) : 0;
+                       ? explicit_tile_blocks(device, N, opt.tile_ctas_per_sm) : 0;
+  pv.step_threads = opt.step_threads;
   if (mixed) {
     auto f32 = [&](const std::vector<double> &v) {
       hostf.emplace_back(v.size());
@@ -718,6 +719,10 @@ static int check_options(const nrt_options *o, std::string &why) {
   if (o->max_iter < 0) return (why = "max_iter must be >= 0", NRT_EINVAL);
   if (o->scheme != NRT_BACKWARD_EULER && o->scheme != NRT_CRANK_NICOLSON)
     return (why = "bad scheme", NRT_EINVAL);
+  if (o->tile_ctas_per_sm < 0 || o->tile_ctas_per_sm > 64)
+    return (why = "tile_ctas_per_sm must be in [0, 64]", NRT_EINVAL);
+  if (o->step_threads != 0 && (o->step_threads < 32 || o->step_threads > 256 || o->step_threads % 32))
+    return (why = "step_threads must be 0 or a multiple of 32 in [32, 256]", NRT_EINVAL);
   return NRT_OK;
 }
 

@@ -478,6 +478,7 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
   // SM, not memory, bounds a small block); large packs: 256-thread blocks.
   int threads = 256;
   while (threads > 32 && pv.ntot < (int64_t)threads * 2 * 152) threads >>= 1;
+  if (pv.step_threads > 0) threads = pv.step_threads;  // a tuned shape (same results)
   const unsigned blocks = (unsigned)((pv.ntot + threads - 1) / threads);
   if (precision == NRT_MIXED) {
     if (!general && pv.tile_blocks > 0 && pv.eflags && pv.err)
@@ -493,8 +494,10 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
   return NRT_OK;
 }
 
-// Persistent CTAs for the tiled mixed step on this device (0 if it cannot run).
-int explicit_tile_blocks(int device, int64_t ntot) {
+// Persistent CTAs for the tiled mixed step on this device (0 if it cannot run): as many
+// per SM as fit, or at most per_sm_cap when that is positive (a tuned shape; the kernel
+// strides over the tiles, so any grid gives the same results).
+int explicit_tile_blocks(int device, int64_t ntot, int per_sm_cap) {
   int sms = 0, per_sm = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, explicit_step_mixed_tiled,
@@ -503,6 +506,7 @@ int explicit_tile_blocks(int device, int64_t ntot) {
     cudaGetLastError();
     return 0;
   }
+  if (per_sm_cap > 0) per_sm = std::min(per_sm, per_sm_cap);
   const int64_t ntiles = (ntot + kTileE - 1) / kTileE;
   return (int)std::min<int64_t>((int64_t)sms * per_sm, ntiles);
 }

@@ -131,6 +131,7 @@ struct PackView {
   InstDev *inst;
   int *err;            // device error word (a bounded wait gave up), or null
   int tile_blocks;     // mixed explicit: persistent CTAs of the tiled step (0: untiled)
+  int step_threads;    // explicit, one thread per element: threads per block (0: by size)
 };
 
 // Device-side recording at probes (record.cu, record.cuh).  Probes are sorted by
@@ -218,7 +219,7 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
 int launch_terminal_fixup(const Topo *topo, const int64_t *terms, int64_t nterm, double *V,
                           float *Vf, cudaStream_t st);
 int launch_advance_base(InstDev *inst, int32_t ninst, int64_t steps, cudaStream_t st);
-int explicit_tile_blocks(int device, int64_t ntot);
+int explicit_tile_blocks(int device, int64_t ntot, int per_sm_cap);
 // Recording after explicit step k (record.cu); V is that step's output.
 int launch_record_step(const RecView &r, const InstDev *inst, int k, const double *V,
                        cudaStream_t st);

@@ -276,7 +276,8 @@ def make_options(mode: int, precision: str = "fp64", krylov: str = "gmres",
                  precond: str = "tree", restart: int = 30, tol: float = 1e-14,
                  tol_mode: str = "abs", max_iter: int = 0, use_graphs: bool = True,
                  device: int = -1, schedule: int = 0, tiled: bool = True,
-                 scheme: str = "be") -> _lib.Options:
+                 scheme: str = "be", tile_ctas_per_sm: int = 0,
+                 step_threads: int = 0) -> _lib.Options:
     lib = _lib.load()
     o = _lib.Options()
     check(lib.nrt_options_default(ctypes.byref(o)), "nrt_options_default")
@@ -293,6 +294,8 @@ def make_options(mode: int, precision: str = "fp64", krylov: str = "gmres",
     o.schedule = int(schedule)
     o.tiled = int(bool(tiled))
     o.scheme = {"be": _lib.NRT_BACKWARD_EULER, "cn": _lib.NRT_CRANK_NICOLSON}[scheme]
+    o.tile_ctas_per_sm = int(tile_ctas_per_sm)
+    o.step_threads = int(step_threads)
     return o
 
 
@@ -422,9 +425,22 @@ class SolverIm(Solver):
 class Batch(_Recorder):
     """Many independent trees advanced together (one launch per step for all of them)."""
 
-    def __init__(self, problems: list[ProblemArrays], mode: int = _lib.NRT_EXPLICIT, **opts):
+    def __init__(self, problems: list[ProblemArrays], mode: int = _lib.NRT_EXPLICIT,
+                 autotune=False, **opts):
+        """opts: make_options keywords.  autotune: True, or a dict of autotune.tune
+        keywords (cache, steps, sample_elements, restarts ...), picks the launch shape by
+        timing the candidates on this workload (cached per device and workload size);
+        options given here win over the tuned ones.  The choice is in self.tuning."""
         self.lib = _lib.load()
         self.problems = problems
+        self.tuning = None
+        if autotune:
+            from .autotune import tune
+            kw = dict(autotune) if isinstance(autotune, dict) else {}
+            rest = {k: v for k, v in opts.items() if k != "precision"}
+            self.tuning = tune(problems, mode, opts.get("precision", "fp64"), **kw, **rest)
+            for k, v in self.tuning["options"].items():
+                opts.setdefault(k, v)
         arr = (_lib.Problem * len(problems))(*[p.struct for p in problems])
         self._arr = arr
         self.options = make_options(mode, **opts)

@@ -1,0 +1,91 @@
+"""The launch-shape autotuner's host logic (168861_gb300/autotune.py) with a fake timer:
+candidate sets, the choice, the sample, and the per-device cache."""
+import importlib
+import json
+
+import pytest
+
+at = importlib.import_module("168861_gb300.autotune")
+lib = importlib.import_module("168861_gb300._lib")
+
+
+class Tree:
+    def __init__(self, n):
+        self.num_elem = n
+
+
+def test_candidates():
+    mixed = at.candidates(lib.NRT_EXPLICIT, "mixed")
+    assert {c["tile_ctas_per_sm"] for c in mixed if c["tiled"]} == {1, 2, 3, 4}
+    assert {c["step_threads"] for c in mixed if not c["tiled"]} == {64, 128, 256}
+    assert [c["step_threads"] for c in at.candidates(lib.NRT_EXPLICIT, "fp64")] == [32, 64, 128, 256]
+    assert at.candidates(lib.NRT_IMPLICIT_BE, "mixed") == [{}]
+    assert at.candidates(lib.NRT_IMPLICIT_BE, "mixed", [16, 20]) == [{"restart": 16}, {"restart": 20}]
+
+
+def test_choose():
+    assert at.choose([3.0, 1.0, 2.0]) == 1
+    assert at.choose([2.0, 1.0, 1.0]) == 1  # first of a tie
+    assert at.choose([None, float("inf"), float("nan"), 5.0]) == 3
+    with pytest.raises(ValueError):
+        at.choose([None, float("inf")])
+
+
+def test_sample():
+    trees = [Tree(n) for n in (1000, 3000, 5000, 100)]
+    assert [t.num_elem for t in at.sample(trees, 4000)] == [1000, 3000]
+    assert [t.num_elem for t in at.sample(trees, 10)] == [1000]  # at least one tree
+    assert len(at.sample(trees, 1e9)) == 4
+
+
+def test_key_separates_devices_modes_and_sizes():
+    a = [Tree(1000)] * 64
+    k = at.workload_key("GB300", lib.NRT_EXPLICIT, "mixed", a)
+    assert k != at.workload_key("B200", lib.NRT_EXPLICIT, "mixed", a)
+    assert k != at.workload_key("GB300", lib.NRT_EXPLICIT, "fp64", a)
+    assert k != at.workload_key("GB300", lib.NRT_IMPLICIT_BE, "mixed", a)
+    assert k != at.workload_key("GB300", lib.NRT_EXPLICIT, "mixed", [Tree(1000)] * 4096)
+    assert k == at.workload_key("GB300", lib.NRT_EXPLICIT, "mixed", [Tree(1100)] * 64)
+
+
+def test_tune_picks_the_fastest_and_caches(tmp_path):
+    cache = str(tmp_path / "tune.json")
+    trees = [Tree(20000)] * 300
+    seen = []
+
+    def timer(ps, mode, prec, ov):
+        seen.append(dict(ov))
+        assert sum(p.num_elem for p in ps) <= 4e6  # a sample, not the whole workload
+        if ov.get("tile_ctas_per_sm") == 3:
+            raise lib.NeuriteError(1, "nrt_batch_create")  # skipped, not fatal
+        return {1: 5.0, 2: 2.0, 4: 3.0}.get(ov.get("tile_ctas_per_sm"), 4.0)
+
+    r = at.tune(trees, lib.NRT_EXPLICIT, "mixed", cache=cache, timer=timer, device_key="dev")
+    assert r["options"] == {"tiled": True, "tile_ctas_per_sm": 2}
+    assert r["times"][2] is None and len(seen) == 7
+    stored = json.load(open(cache))
+    assert stored[r["key"]]["options"] == r["options"]
+    # served from the cache: no timing
+    r2 = at.tune(trees, lib.NRT_EXPLICIT, "mixed", cache=cache, timer=timer, device_key="dev")
+    assert r2["options"] == r["options"] and r2["times"] is None and len(seen) == 7
+    # another device is tuned on its own
+    at.tune(trees, lib.NRT_EXPLICIT, "mixed", cache=cache, timer=timer, device_key="other")
+    assert len(seen) == 14
+
+
+def test_tune_ignores_a_stale_cache_entry(tmp_path):
+    cache = tmp_path / "tune.json"
+    trees = [Tree(5000)] * 8
+    key = at.workload_key("dev", lib.NRT_EXPLICIT, "fp64", trees)
+    cache.write_text(json.dumps({key: {"options": {"step_threads": 96}}}))  # not a candidate
+    r = at.tune(trees, lib.NRT_EXPLICIT, "fp64", cache=str(cache), device_key="dev",
+                timer=lambda ps, m, p, ov: 1.0 / ov["step_threads"])
+    assert r["options"] == {"step_threads": 256} and r["times"] is not None
+
+
+def test_nothing_to_tune_needs_no_timer(tmp_path):
+    def timer(*a):
+        raise AssertionError("no candidate to time")
+    r = at.tune([Tree(1000)], lib.NRT_IMPLICIT_BE, "mixed", cache=str(tmp_path / "c.json"),
+                timer=timer, device_key="dev")
+    assert r["options"] == {}

@@ -66,11 +66,25 @@ def test_create_rejects_bad_topology_without_device(pkg, lib, mode):
 def test_create_rejects_bad_options_without_device(pkg, lib):
     g = load_golden("ytree_d3_strain")
     p = _problem(pkg, g)
-    for field, val in [("restart", 0), ("restart", 999), ("tol", -1.0), ("precision", 7)]:
+    for field, val in [("restart", 0), ("restart", 999), ("tol", -1.0), ("precision", 7),
+                       ("step_threads", 48), ("step_threads", 512), ("step_threads", -32),
+                       ("tile_ctas_per_sm", -1), ("tile_ctas_per_sm", 65)]:
         opts = pkg.solver.make_options(1)
         setattr(opts, field, val)
         h = ctypes.c_void_p()
         assert lib.nrt_create(ctypes.byref(p.struct), ctypes.byref(opts), ctypes.byref(h)) == 1
+
+
+def test_options_struct_matches_the_header(pkg, lib):
+    """The Python mirror of nrt_options has the C layout: nrt_options_default fills every
+    field the header documents, and the launch-shape fields sit where the header puts them."""
+    import ctypes as ct
+    o = pkg._lib.Options()
+    ct.memset(ct.byref(o), 0x7f, ct.sizeof(o))
+    assert lib.nrt_options_default(ct.byref(o)) == 0
+    assert ct.sizeof(o) == 4 * 6 + 8 + 4 * 10  # 6 ints, the double, 10 ints (2 reserved)
+    assert (o.tiled, o.use_graphs, o.tile_ctas_per_sm, o.step_threads) == (1, 1, 0, 0)
+    assert list(o.reserved) == [0, 0]
 
 
 def test_implicit_requires_reference_numbering(pkg, lib, model):
