@@ -66,6 +66,9 @@ def parse():
                     help="implicit workloads: GMRES preconditioner")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain-FP64 single-tree comparison run")
+    ap.add_argument("--autotune", action="store_true",
+                    help="explicit workloads: run on the launch shape the autotuner picks "
+                         "(tuned before the timed regions; default: the automatic shapes)")
     return ap.parse_args()
 
 
@@ -359,6 +362,11 @@ def run_ours(args, rank: int, world: int):
         opts.update(krylov="gmres", restart=20, tol=1e-10, tol_mode="rel", precond=args.precond,
                     max_iter=1000)
     mode = pkg._lib.NRT_IMPLICIT_BE if implicit else pkg._lib.NRT_EXPLICIT
+    launch_shape = "automatic"
+    if args.autotune and not implicit:  # outside every timed region
+        tuned = importlib.import_module(pkg.__name__ + ".autotune").tune(probs, mode, precision)
+        opts.update(tuned["options"])
+        launch_shape = tuned["options"]
     # loop ranges long enough for warm-up + timed steps
     runs = [(a, max(b, a + W + K + 1), c, d_) for a, b, c, d_ in runs]
 
@@ -450,7 +458,8 @@ def run_ours(args, rank: int, world: int):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if precision == "fp64" else "f32+f64",
         "data": "synthetic (seeded random trees)",
-        "config": workload_config(wl, count, args.precond), "elements": n_all,
+        "config": {**workload_config(wl, count, args.precond), "launch_shape": launch_shape},
+        "elements": n_all,
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d / K,
                 "d2h_bytes_per_step": d2h / K, "seconds": e2e_s},
         "roofline": roof, "roofline_passes": roof_passes, "gpu_launches": launches,
