@@ -6,8 +6,11 @@
 // system and the solution vector in their own device memory; every temporary (Krylov
 // basis, preconditioned basis, SpMV result, preconditioner factors, reduction partials,
 // the result record) lives in one file-scope static __device__ array of
-// NRT_STATIC_SCRATCH_BYTES, which every GPU that loads the library holds until the
-// process exits.
+// NRT_STATIC_SCRATCH_BYTES.  The array is reserved on a device when this file's module is
+// loaded there: under CUDA's default lazy module loading that is the first call of the
+// entry point on that device (or a process-wide start-up load with
+// CUDA_MODULE_LOADING=EAGER).  From then on the device holds it until the process exits,
+// and no later call changes the device's free memory.
 //
 // Method: right-preconditioned GMRES(m) with classical Gram-Schmidt and Givens rotations,
 // FP64 throughout, with fixed-order grid reductions.  It is the method of the solver
@@ -43,7 +46,7 @@ static __device__ __align__(256) unsigned char g_static_scratch[NRT_STATIC_SCRAT
 
 // Offsets (in doubles) of the regions inside the scratch array.
 struct Layout {
-  size_t W, Z, y, pd, pc, partials, result, total;
+  size_t W, Z, y, pd, pc, pl, partials, result, total;
 };
 
 __host__ __device__ inline Layout layout(int n, int m) {
@@ -54,7 +57,8 @@ __host__ __device__ inline Layout layout(int n, int m) {
   L.y = L.Z + N * (m + 1);
   L.pd = L.y + N;
   L.pc = L.pd + N;
-  L.partials = L.pc + N;
+  L.pl = L.pc + N;
+  L.partials = L.pl + N;
   L.result = L.partials + 2 * (size_t)kMaxG * (kM + 1);
   L.total = L.result + kResult;
   return L;
@@ -87,16 +91,15 @@ __device__ __forceinline__ void tri(const Args &a, int j, double &d, double &lo,
   }
 }
 
-// z = M^-1 v over this CTA's blocks.
-__device__ void precond(const Args &a, const double *pd, const double *pc, const double *v,
+// z = M^-1 v over this CTA's blocks (pl: each row's block-local sub-diagonal entry, kept
+// by the factorisation so that no application scans the CSR rows again).
+__device__ void precond(const double *pd, const double *pc, const double *pl, const double *v,
                         double *z, int r0, int r1) {
   for (int b0 = r0 + threadIdx.x * kBlk; b0 < r1; b0 += kT * kBlk) {
     const int e = min(r1, b0 + kBlk);
     double y = 0;
     for (int j = b0; j < e; j++) {
-      double d, lo, hi;
-      tri(a, j, d, lo, hi);
-      y = (v[j] - lo * y) * pd[j];
+      y = (v[j] - pl[j] * y) * pd[j];
       z[j] = y;
     }
     for (int j = e - 2; j >= b0; j--) {
@@ -143,7 +146,8 @@ __global__ void __launch_bounds__(kT) static_gmres(Args a) {
   const int n = a.n, m = a.m;
   const Layout L = layout(n, m);
   double *W = a.scratch + L.W, *Z = a.scratch + L.Z, *Y = a.scratch + L.y;
-  double *pd = a.scratch + L.pd, *pc = a.scratch + L.pc, *partials = a.scratch + L.partials;
+  double *pd = a.scratch + L.pd, *pc = a.scratch + L.pc, *pl = a.scratch + L.pl;
+  double *partials = a.scratch + L.partials;
   const int r0 = min(n, (int)blockIdx.x * a.rows_per_cta);
   const int r1 = min(n, r0 + a.rows_per_cta);
   int parity = 0;
@@ -158,24 +162,31 @@ __global__ void __launch_bounds__(kT) static_gmres(Args a) {
       cprev = hi * dd;
       pd[j] = dd;
       pc[j] = cprev;
+      pl[j] = lo;
     }
   }
   double acc[kM + 1];
-  acc[0] = 0;
+  acc[0] = acc[1] = 0;
   for (int j = r0 + threadIdx.x; j < r1; j += kT) {
     // ||b|| over coupled rows only: a decoupled row (the reference's identity rows) is
     // solved exactly by the block preconditioner and would otherwise dominate the norm
     bool coupled = false;
     for (int p = a.row_ptr[j]; p < a.row_ptr[j + 1]; p++) coupled |= a.col[p] != j;
     if (coupled) acc[0] += a.b[j] * a.b[j];
+    acc[1] += a.b[j] * a.b[j];
   }
-  grid_sums(grid, acc, 1, partials, parity, warp_part, red);
-  const double target = a.tol_mode == NRT_TOL_REL ? a.tol * sqrt(red[0]) : a.tol;
+  grid_sums(grid, acc, 2, partials, parity, warp_part, red);
+  // relative mode: against ||b|| over the coupled rows; over all rows when those are zero;
+  // against the first residual when b is zero everywhere (x = 0 is then the solution and
+  // an exact zero residual need never come)
+  const double bref = red[0] > 0 ? sqrt(red[0]) : sqrt(red[1]);
+  double target = a.tol_mode == NRT_TOL_REL ? a.tol * bref : a.tol;
+  const bool target_from_r0 = a.tol_mode == NRT_TOL_REL && !(bref > 0);
   const int budget = a.max_iter > 0 ? a.max_iter : n;
   int iters = 0;
   double res = 0;
-  bool converged = false;
-  for (;;) {
+  int status = 0;  // 1 converged, 2 a non-finite residual or basis norm ended the solve
+  for (int cycle = 0;; cycle++) {
     // residual of the current x; W_0 = r, Z_0 = M^-1 r
     acc[0] = 0;
     for (int j = r0 + threadIdx.x; j < r1; j += kT) {
@@ -184,11 +195,16 @@ __global__ void __launch_bounds__(kT) static_gmres(Args a) {
       acc[0] += r * r;
     }
     __syncthreads();
-    precond(a, pd, pc, W, Z, r0, r1);
+    precond(pd, pc, pl, W, Z, r0, r1);
     grid_sums(grid, acc, 1, partials, parity, warp_part, red);  // also publishes Z_0
     res = sqrt(red[0]);
+    if (!isfinite(res)) {  // NaN or Inf in the system or in x: no iteration can recover
+      status = 2;
+      break;
+    }
+    if (cycle == 0 && target_from_r0) target = a.tol * res;
     if (res <= target) {
-      converged = true;
+      status = 1;
       break;
     }
     if (iters >= budget) break;
@@ -219,7 +235,7 @@ __global__ void __launch_bounds__(kT) static_gmres(Args a) {
         acc[0] += v * v;
       }
       __syncthreads();
-      precond(a, pd, pc, Wn, Z + (size_t)(j + 1) * n, r0, r1);
+      precond(pd, pc, pl, Wn, Z + (size_t)(j + 1) * n, r0, r1);
       grid_sums(grid, acc, 1, partials, parity, warp_part, red);  // publishes Z_{j+1}
       if (threadIdx.x == 0) {
         const double hn = sqrt(red[0]);
@@ -236,12 +252,17 @@ __global__ void __launch_bounds__(kT) static_gmres(Args a) {
         H[j * m + j] = den;
         g[j + 1] = -sn[j] * g[j];
         g[j] = cs[j] * g[j];
-        flag = (fabs(g[j + 1]) <= target || hn == 0) ? 1 : 0;
+        flag = !isfinite(hn) ? 2 : ((fabs(g[j + 1]) <= target || hn == 0) ? 1 : 0);
       }
       __syncthreads();
+      if (flag == 2) break;  // every CTA read the same sums: a uniform exit
       k = j + 1;
       iters++;
       if (flag || iters >= budget) break;
+    }
+    if (flag == 2) {  // leave x at the cycle's start, which was finite
+      status = 2;
+      break;
     }
     if (threadIdx.x == 0) {
       for (int i = k - 1; i >= 0; i--) {
@@ -265,7 +286,7 @@ __global__ void __launch_bounds__(kT) static_gmres(Args a) {
     double *out = a.scratch + L.result;
     out[0] = iters;
     out[1] = res;
-    out[2] = converged ? 1.0 : 0.0;
+    out[2] = status;
   }
 }
 
@@ -294,7 +315,7 @@ extern "C" int nrt_solve_csr_static(int32_t n, const int32_t *row_ptr, const int
     }
     const Layout L = layout(n, restart);
     if (L.total * sizeof(double) > (size_t)NRT_STATIC_SCRATCH_BYTES) {
-      set_error("nrt_solve_csr_static: n * (2 * restart + 5) doubles exceed the static scratch "
+      set_error("nrt_solve_csr_static: n * (2 * restart + 6) doubles exceed the static scratch "
                 "(NRT_STATIC_SCRATCH_BYTES); use a smaller restart or the handle API");
       return NRT_EBUDGET;
     }
@@ -322,7 +343,7 @@ extern "C" int nrt_solve_csr_static(int32_t n, const int32_t *row_ptr, const int
       set_error("nrt_solve_csr_static: kernel does not fit on an SM");
       return NRT_EDEVICE;
     }
-    // rows per CTA: whole preconditioner blocks, at least 4 rows per thread
+    // rows per CTA: whole preconditioner blocks, at least 4 of them per CTA
     int G = (int)std::min<long long>((long long)sms * per_sm, kMaxG);
     int rows = (((n + G - 1) / G + kBlk - 1) / kBlk) * kBlk;
     rows = std::max(rows, 4 * kBlk);
@@ -348,6 +369,11 @@ extern "C" int nrt_solve_csr_static(int32_t n, const int32_t *row_ptr, const int
     NRT_CUDA(cudaStreamSynchronize(st));
     if (iters_out) *iters_out = (int32_t)res[0];
     if (residual_out) *residual_out = res[1];
+    if (res[2] == 2.0) {
+      set_error("nrt_solve_csr_static: a residual or Krylov basis norm is not finite (NaN or "
+                "Inf in the system, the right-hand side or the initial guess)");
+      return NRT_EINVAL;
+    }
     if (res[2] == 0.0) {
       set_error("nrt_solve_csr_static: iteration budget reached");
       return NRT_ENOCONV;

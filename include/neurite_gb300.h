@@ -453,13 +453,22 @@ int nrt_server_destroy(nrt_server *s);
  * iteration count: it returns after the work on `stream` (a cudaStream_t; NULL = legacy
  * default stream) has finished.
  *
- * Memory: nothing is allocated, by this function or by anything it calls.  Every
- * temporary lives in one static device array of NRT_STATIC_SCRATCH_BYTES, present on
- * every GPU that loads the library until the process exits.  It must hold
- * n * (2*restart + 5) + 2*1024*(NRT_STATIC_MAX_RESTART + 1) + 4 doubles (about 110,000 rows
- * at restart 16, 180,000 at restart 8); larger systems are refused with NRT_EBUDGET.
- * The first call on a device looks up the array's device address (a one-time set-up with
- * that device current), so make that first call before any stream capture.
+ * Memory: nothing is allocated by this function or by anything it calls.  Every
+ * temporary lives in one static device array of NRT_STATIC_SCRATCH_BYTES.  CUDA reserves
+ * that array on a device when it loads this code onto the device, which under CUDA's
+ * default lazy module loading happens at the first call on that device (with
+ * CUDA_MODULE_LOADING=EAGER, when the process first uses CUDA).  A host that will later
+ * claim the device's whole memory pool must therefore make one call per device before it
+ * does; from then on the device holds the array until the process exits, and later calls
+ * leave the device's free memory unchanged.  The array must hold
+ * n * (2*restart + 6) + 2*1024*(NRT_STATIC_MAX_RESTART + 1) + 4 doubles (about 109,000 rows
+ * at restart 16, 189,000 at restart 8); larger systems are refused with NRT_EBUDGET.
+ * The first call on a device also looks up the array's device address (a one-time set-up
+ * with that device current), so make that first call before any stream capture.
+ * A system, right-hand side or initial guess holding NaN or Inf ends the solve with
+ * NRT_EINVAL (x keeps its last finite iterate).  In relative mode a right-hand side that is
+ * zero on every coupled row is measured over all rows, and one that is zero everywhere
+ * against the first residual.
  * Every call shares the one array and leaves its contents behind; each region is written
  * before it is read within a call, so nothing needs clearing, but calls that overlap on the
  * GPU (other streams or host threads without ordering) race on it. */
