@@ -44,7 +44,7 @@ class Options(ctypes.Structure):
         ("use_graphs", ctypes.c_int32), ("schedule", ctypes.c_int32),
         ("tiled", ctypes.c_int32), ("scheme", ctypes.c_int32),
         ("tile_ctas_per_sm", ctypes.c_int32), ("step_threads", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 2),
+        ("inner_tol", ctypes.c_double),
     ]
 
 

@@ -717,6 +717,7 @@ static int check_options(const nrt_options *o, std::string &why) {
   if (o->restart < 1 || o->restart > nrt::kMaxRestart) return (why = "restart must be in [1, 32]", NRT_EINVAL);
   if (!(o->tol > 0)) return (why = "tol must be > 0", NRT_EINVAL);
   if (o->max_iter < 0) return (why = "max_iter must be >= 0", NRT_EINVAL);
+  if (!(o->inner_tol >= 0 && o->inner_tol < 1)) return (why = "inner_tol must be in [0, 1)", NRT_EINVAL);
   if (o->scheme != NRT_BACKWARD_EULER && o->scheme != NRT_CRANK_NICOLSON)
     return (why = "bad scheme", NRT_EINVAL);
   if (o->tile_ctas_per_sm < 0 || o->tile_ctas_per_sm > 64)

@@ -101,6 +101,7 @@ struct ImView {
   int tol_mode;
   double tol;
   int max_iter;      // per step per instance; 0 -> instance size; < 0 -> assembly only
+  double inner_rel;  // a refinement cycle's inner target relative to its starting residual
   int ninst;
   int tile_rows;     // rows per shared-memory tile (segment preconditioner)
   const uint8_t *rowf;
@@ -1452,7 +1453,7 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
     if (!kGrid) __syncthreads();
   }
   const int budget = iv.max_iter > 0 ? iv.max_iter : (iv.max_iter < 0 ? 0 : (int)inst_n);
-  const double inner_rel = sizeof(T) == 4 ? 1e-5 : 0.0;
+  const double inner_rel = iv.inner_rel;
   int iters = 0, n_res = 0, n_app = 0, n_xup = 0, n_basis = 0;
   double res = 0;
   bool converged = false;
@@ -2166,6 +2167,7 @@ int Engine::implicit_init() {
   iv.tol_mode = opt.tol_mode;
   iv.tol = opt.tol;
   iv.max_iter = opt.max_iter;
+  iv.inner_rel = !mixed ? 0.0 : (opt.inner_tol > 0 ? opt.inner_tol : NRT_INNER_TOL_DEFAULT);
   iv.ninst = ni;
   iv.tile_rows = S.tile_rows;
   uint8_t *pr;

@@ -277,7 +277,7 @@ def make_options(mode: int, precision: str = "fp64", krylov: str = "gmres",
                  tol_mode: str = "abs", max_iter: int = 0, use_graphs: bool = True,
                  device: int = -1, schedule: int = 0, tiled: bool = True,
                  scheme: str = "be", tile_ctas_per_sm: int = 0,
-                 step_threads: int = 0) -> _lib.Options:
+                 step_threads: int = 0, inner_tol: float = 0.0) -> _lib.Options:
     lib = _lib.load()
     o = _lib.Options()
     check(lib.nrt_options_default(ctypes.byref(o)), "nrt_options_default")
@@ -296,6 +296,7 @@ def make_options(mode: int, precision: str = "fp64", krylov: str = "gmres",
     o.scheme = {"be": _lib.NRT_BACKWARD_EULER, "cn": _lib.NRT_CRANK_NICOLSON}[scheme]
     o.tile_ctas_per_sm = int(tile_ctas_per_sm)
     o.step_threads = int(step_threads)
+    o.inner_tol = float(inner_tol)
     return o
 
 

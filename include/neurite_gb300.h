@@ -130,8 +130,17 @@ typedef struct nrt_options {
   int32_t step_threads;          /* explicit, one thread per element: threads per block, a
                                     multiple of 32 up to 256 (0 = chosen from the tree size).
                                     Launch shapes only: results do not depend on them */
-  int32_t reserved[2];
+  double inner_tol;              /* implicit, mixed precision: each FP64 refinement cycle's
+                                    inner FP32 Krylov solve stops once its residual estimate
+                                    is below inner_tol times the cycle's starting residual
+                                    (0 = the default, NRT_INNER_TOL_DEFAULT).  FP64 mode
+                                    solves each cycle to the outer tolerance and ignores it */
 } nrt_options;
+
+/* One FP32 cycle cannot reduce the true residual by much more than 1e-4 on a stiff
+ * cable (its preconditioner and products are FP32), so a tighter inner target buys
+ * Krylov iterations that the next FP64 residual does not see. */
+#define NRT_INNER_TOL_DEFAULT 1e-3
 
 typedef struct nrt_stats {
   int64_t steps;                 /* calculate() calls so far */
