@@ -220,7 +220,25 @@ enum { TO_FL = 0, TO_F = kR4, TO_GAX = 2 * kR4, TO_V = 3 * kR4, TO_CDT = 3 * kR4
        TO_CLS = 4 * kR4 + kR8, TO_G0 = 5 * kR4 + kR8, TO_G1 = 6 * kR4 + kR8,
        TO_G2 = 7 * kR4 + kR8, kTileBufBytes = 8 * kR4 + kR8 };
 
-// Staged windows (stage_bytes, stage, staged): tma.cuh.
+// Bytes of the bulk copy of elements [o, o + n) of an array (16-byte aligned base): the
+// window rounded out to 16-byte boundaries.
+template <typename X>
+__device__ __forceinline__ uint32_t stage_bytes(int64_t o, int64_t n) {
+  const uint64_t lo = ((uint64_t)o * sizeof(X)) & ~(uint64_t)15;
+  const uint64_t hi = ((uint64_t)(o + n) * sizeof(X) + 15) & ~(uint64_t)15;
+  return (uint32_t)(hi - lo);
+}
+template <typename X>
+__device__ __forceinline__ void stage(unsigned char *dst, const X *a, int64_t o, int64_t n,
+                                      uint64_t *bar) {
+  const uint64_t lo = ((uint64_t)o * sizeof(X)) & ~(uint64_t)15;
+  bulk_load(dst, (const char *)a + lo, stage_bytes<X>(o, n), bar);
+}
+// The shared-memory copy of element o of a staged array.
+template <typename X>
+__device__ __forceinline__ const X *staged(const unsigned char *dst, int64_t o) {
+  return (const X *)(dst + (((uint64_t)o * sizeof(X)) & 15));
+}
 
 struct TileWin {
   int64_t s, cnt, of, ngax, nf;  // first element, count, F window start, window lengths

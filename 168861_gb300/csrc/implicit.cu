@@ -50,7 +50,6 @@
 #include <memory>
 #include <vector>
 
-#include "ff.cuh"
 #include "hh.cuh"
 #include "nrt_solver.h"
 #include "record.cuh"
@@ -139,16 +138,6 @@ struct ImView {
   void *sinv, *se, *sy;           // T per slot: 1 / pivot, g / pivot, eliminated right side
   void *exp_d, *exp_b;            // T per segment: what it passes to its parent row
   int tree_cap;                   // staging slots per tree tile (multiple of 16)
-  // mixed precision, GMRES with the tree preconditioner (the double-float step, see
-  // implicit_one_step_ff): FP32 pairs of the static coefficients, the per-step c and
-  // f = b - A V^n, and two buffers of the step's correction to V
-  int ff;                         // 1: that step runs
-  const float2 *cm2;              // c_m dX / dT
-  const float2 *g2;               // 1 / (r_a dX)
-  const float2 *wdx2, *kdx2;      // W dX, K dX of cables
-  float *clo;                     // c - cdiag
-  float2 *fp2;                    // f
-  float2 *dp2[2];                 // correction of V (ping-pong)
 };
 
 template <typename T>
@@ -159,15 +148,14 @@ struct Work {
 struct Shared {
   double *H, *cs, *sn, *g, *s, *y, *red, *warp;
   void *coef;      // T[kMaxDots]: update / solution coefficients
-  int *flag;       // [0] convergence, [1] queue slot, [2] tree tile barrier phase,
-                   // [3] row tile barriers' phases (bit b: buffer b)
-  uint64_t *bar;   // mbarriers: [0] tree tiles, [1], [2] the two row tile buffers
+  int *flag;       // [0] convergence, [1] queue slot, [2] tile barrier phase
+  uint64_t *bar;   // mbarrier of the tile bulk copies
   void *tile;      // staging area
 };
 
 __host__ __device__ inline size_t shared_fixed_bytes(int m) {
   return sizeof(double) * ((size_t)(m + 1) * m + 2 * m + 2 * (m + 1) + m + kMaxDots +
-                           kWarps * kMaxDots + kMaxDots) + 64;
+                           kWarps * kMaxDots + kMaxDots) + 32;
 }
 
 // The dynamic shared memory of the launch.
@@ -1438,751 +1426,6 @@ __device__ __noinline__ int2 bicgstab_cycle(Ctx<T, kGrid> c, int parity, double 
   return make_int2(parity, iters);
 }
 
-// ---------------------------------------------------------------- the double-float step
-//
-// Mixed precision, GMRES with the exact tree preconditioner.  The step solves for the
-// correction d = V^{n+1} - V^n of A V^{n+1} = b, i.e. A d = f with f = b - A V^n:
-//   backward Euler   f = W dX V + K dX + I - sum_q g_q (V - V_q),   A = c + L,
-//                    c = c_m dX / dT - W dX;
-//   Crank-Nicolson   f and c as the doubled trapezoidal system gives them: 2 f_BE and
-//                    2 c_m dX / dT - W dX,
-// with L d = sum_q g_q (d - d_q) the tree's conductances.  f holds the currents that
-// b - A x would otherwise form by cancelling the large c_m dX / dT V terms, so everything
-// the refinement residual r = f - A d needs fits FP32 pairs (ff.cuh): the neighbour
-// differences of V^n come from FP64 subtractions, d is a pair, c, g and f are pairs, and
-// r is formed with about 46 significant bits.  The FP64 arithmetic of a row is
-// V^n = V^{n-1} + d^{n-1} and the differences V^n - V^{n-1} and V^n - V^n_mother: four
-// FP64 additions, where the plain form of the assembly and the residuals needs about 40
-// FP64 operations and conversions (the GB300 runs them at 1/70 of its FP32 rate).
-//
-// Passes of a step (two refinement cycles of one Arnoldi step each on the batched
-// workload): the assembly (gates, c, f, the predictor d0 = V^n - V^{n-1}, r0 = f - A d0,
-// and V^n itself, written a step late: the previous step left V^{n-1} and its correction),
-// the factorisation, and per cycle the preconditioner, one SpMV fused with <y, W_0> and
-// ||y||^2 accumulated as pairs (which give ||W_1|| without the update pass when the cycle
-// stops there), and the next residual pass, which first applies the cycle's solution
-// update d += sum_i y_i Z_i to the row and its neighbours.  The potential of the last
-// step of a launch is written at the launch's end.
-//
-// The predictor is V^n - V^{n-1} formed from the FP64 potentials both inside a launch and
-// at its start, so a run gives the same numbers however it is split into launches.
-
-constexpr float kNormScale = 1152921504606846976.0f;  // 2^60: squares of A-scale values
-constexpr double kNormUnscale = 1.0 / 1152921504606846976.0;
-
-// V at the start of the step and the predicted correction for row q.  first: va = V^n,
-// vb = V^{n-1}; otherwise va = V^{n-1} and d the last step's correction (the same bits
-// whether they come from global memory or a staged tile).
-struct RowV {
-  double vc;
-  ff dp;
-};
-
-__device__ __forceinline__ RowV row_start_v(bool first, double va, double vb, float2 d) {
-  RowV o;
-  double vp;
-  if (first) {
-    o.vc = va;
-    vp = vb;
-  } else {
-    vp = va;
-    o.vc = add_ff(vp, ff{d.x, d.y});
-  }
-  o.dp = ff_of(o.vc - vp);
-  return o;
-}
-// The same from global memory: Vb is V^{n-1} (first) and D the correction (otherwise).
-__device__ __forceinline__ RowV row_start(bool first, const double *Va, const double *Vb,
-                                          const float2 *D, int64_t q) {
-  return first ? row_start_v(true, Va[q], Vb[q], make_float2(0.f, 0.f))
-               : row_start_v(false, Va[q], 0.0, D[q]);
-}
-
-__device__ __forceinline__ ff pair(float2 v) { return ff{v.x, v.y}; }
-
-// ---- row tiles staged into shared memory (the double-float passes)
-//
-// A pass walks its group's rows [r0, r1) in tiles.  Thread 0 issues the bulk copies of
-// tile t + 1 into one of two buffers, each completed on its own mbarrier (S.bar[1],
-// S.bar[2]), while the CTA works on tile t from the other; the __syncthreads that ends a
-// tile frees its buffer.  Each array's window is the tile's rows plus the halo the pass
-// reads (the row before and the row after), rounded out to 16-byte boundaries (stage /
-// staged, tma.cuh); every array lies 256-byte aligned in the arena with slack behind it, so
-// a rounded window never leaves the arena.  Every copy issued is waited for within the
-// pass (bounded wait: a copy that never lands raises the error word).
-// The threads only read what the copies bring in (what they compute from it goes to a
-// scratch area behind the copy regions, which no copy writes), so the barrier that ends a
-// tile is all the ordering the next copy into its buffer needs: no proxy fence, which
-// would also wait for the issuing thread's outstanding global stores.
-
-constexpr int kRowsAsm = 254;  // rows per tile, assembly: its window (+-1) one per thread
-constexpr int kRowsRes = 512;  // rows per tile, residual: two per thread
-
-// Bytes a window of n elements of s bytes may take in shared memory (the copy rounds both
-// ends out to 16 bytes).
-__host__ __device__ constexpr int win_bytes(int n, int s) { return ((n * s + 30 + 15) / 16) * 16; }
-
-// assembly tile: flags, V (8 B), V^{n-1} or correction (8 B), gates or cable W dX / K dX
-// pairs, class index, c_m dX / dT pair, conductance pair (tile + 1), and the scratch
-enum : int {
-  AO_FL = 0,
-  AO_VA = AO_FL + win_bytes(kRowsAsm + 2, 1),
-  AO_VB = AO_VA + win_bytes(kRowsAsm + 2, 8),
-  AO_X = AO_VB + win_bytes(kRowsAsm + 2, 8),  // gates: 3 x (n, 4); cables: 2 x (n, 8)
-  AO_CLS = AO_X + 2 * win_bytes(kRowsAsm, 8),
-  AO_CM = AO_CLS + win_bytes(kRowsAsm, 4),
-  AO_G = AO_CM + win_bytes(kRowsAsm, 8),
-  AO_SCR = AO_G + win_bytes(kRowsAsm + 1, 8),  // scratch: V and predictor per window row
-  kAsmBuf = AO_SCR + (kRowsAsm + 2) * 16,
-};
-// residual tile: flags, correction (+-1), Z_0 (+-1), f, c high and low parts, conductance
-// pair (tile + 1)
-enum : int {
-  RO_FL = 0,
-  RO_D = RO_FL + win_bytes(kRowsRes, 1),
-  RO_Z = RO_D + win_bytes(kRowsRes + 2, 8),
-  RO_F = RO_Z + win_bytes(kRowsRes + 2, 4),
-  RO_CH = RO_F + win_bytes(kRowsRes, 8),
-  RO_CL = RO_CH + win_bytes(kRowsRes, 4),
-  RO_G = RO_CL + win_bytes(kRowsRes, 4),
-  kResBuf = RO_G + win_bytes(kRowsRes + 1, 8),
-};
-static_assert(3 * win_bytes(kRowsAsm, 4) <= 2 * win_bytes(kRowsAsm, 8), "gate windows");
-static_assert(2 * kAsmBuf <= kTileBytes && 2 * kResBuf <= kTileBytes, "row tiles fit the staging area");
-static_assert(kRowsAsm + 2 == kThreads, "the assembly window has one row per thread");
-
-// Halo window of a tile [a, a + cnt): [lo, hi) = [a - 1, a + cnt + 1) inside [0, N).
-struct RowWin {
-  int64_t a, cnt, lo, hi;
-};
-__device__ __forceinline__ RowWin row_win(int64_t a, int64_t cnt, int64_t N) {
-  RowWin w;
-  w.a = a;
-  w.cnt = cnt;
-  w.lo = a > 0 ? a - 1 : 0;
-  w.hi = a + cnt + 1 < N ? a + cnt + 1 : N;
-  return w;
-}
-
-// Walks the tiles of [r0, r1) with kRows rows each: issue(w, buf, bar) (thread 0) expects
-// and issues a tile's copies; body(w, buf) works on it.
-template <int kRows, class Issue, class Body>
-__device__ __forceinline__ void row_tiles(Shared &S, int64_t r0, int64_t r1, int64_t N, int *err,
-                                          Issue issue, Body body) {
-  const int64_t nt = (r1 - r0 + kRows - 1) / kRows;
-  unsigned char *buf[2] = {(unsigned char *)S.tile, (unsigned char *)S.tile + kTileBytes / 2};
-  uint32_t par = (uint32_t)S.flag[3];
-  auto win = [&](int64_t t) {
-    const int64_t a = r0 + t * kRows;
-    return row_win(a, r1 - a < kRows ? r1 - a : kRows, N);
-  };
-  if (threadIdx.x == 0 && nt > 0) issue(win(0), buf[0], S.bar + 1);
-  for (int64_t t = 0; t < nt; t++) {
-    const int b = (int)(t & 1);
-    // buffer b ^ 1 was last read by tile t - 1, which the barrier below that tile ended
-    if (threadIdx.x == 0 && t + 1 < nt) issue(win(t + 1), buf[b ^ 1], S.bar + 1 + (b ^ 1));
-    mbar_wait(S.bar + 1 + b, (par >> b) & 1u, err);
-    par ^= 1u << b;
-    body(win(t), buf[b]);
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) S.flag[3] = (int)par;
-}
-
-// Assembly of the double-float step (see above).  Reads the correction from buffer dc
-// (unless first) and writes the predictor to buffer dc ^ 1 -- the other rows' threads
-// still read the old one -- and V at the start of the step to Vb (unless first).
-// Returns the thread's parts of ||b||^2 and ||r0||^2, scaled by kNormScale^2.
-template <bool kGrid>
-__device__ __noinline__ float2 ph_assemble_ff(Ctx<float, kGrid> c, const double *Va, double *Vb,
-                                              bool first, int active, int inst, int dc) {
-  const PackView &pv = *c.pv;
-  const ImView &iv = *c.iv;
-  Shared S = carve(dyn_smem(), iv.m);
-  const int64_t N = pv.ntot;
-  const bool cn = iv.scheme == NRT_CRANK_NICOLSON;
-  const bool dense = pv.hh_dense != 0;
-  const float2 *Din = iv.dp2[dc];
-  float2 *Dout = iv.dp2[dc ^ 1];
-  float *gate = pv.gatef;
-  float *cdiag = (float *)iv.cdiag;
-  // the second V-sized input: V^{n-1} (first step of a launch) or the last correction
-  const void *B = first ? (const void *)Vb : (const void *)Din;
-  float bacc = 0.f, racc = 0.f;
-  auto issue = [&](const RowWin &w, unsigned char *buf, uint64_t *bar) {
-    const int64_t nw = w.hi - w.lo;
-    uint32_t bytes = stage_bytes<uint8_t>(w.lo, nw) + 2 * stage_bytes<double>(w.lo, nw) +
-                     stage_bytes<float2>(w.a, w.cnt) + stage_bytes<float2>(w.a, w.cnt + 1);
-    if (pv.hp_cls) bytes += stage_bytes<uint32_t>(w.a, w.cnt);
-    if (dense)
-      bytes += stage_bytes<float>(w.a, w.cnt) + stage_bytes<float>(N + w.a, w.cnt) +
-               stage_bytes<float>(2 * N + w.a, w.cnt);
-    else
-      bytes += 2 * stage_bytes<float2>(w.a, w.cnt);
-    mbar_expect_tx(bar, bytes);
-    stage(buf + AO_FL, iv.rowf, w.lo, nw, bar);
-    stage(buf + AO_VA, Va, w.lo, nw, bar);
-    stage(buf + AO_VB, (const double *)B, w.lo, nw, bar);
-    if (dense) {
-      stage(buf + AO_X, gate, w.a, w.cnt, bar);
-      stage(buf + AO_X + win_bytes(kRowsAsm, 4), gate, N + w.a, w.cnt, bar);
-      stage(buf + AO_X + 2 * win_bytes(kRowsAsm, 4), gate, 2 * N + w.a, w.cnt, bar);
-    } else {
-      stage(buf + AO_X, iv.wdx2, w.a, w.cnt, bar);
-      stage(buf + AO_X + win_bytes(kRowsAsm, 8), iv.kdx2, w.a, w.cnt, bar);
-    }
-    if (pv.hp_cls) stage(buf + AO_CLS, pv.hp_cls, w.a, w.cnt, bar);
-    stage(buf + AO_CM, iv.cm2, w.a, w.cnt, bar);
-    stage(buf + AO_G, iv.g2, w.a, w.cnt + 1, bar);
-  };
-  auto body = [&](const RowWin &w, unsigned char *buf) {
-    const uint8_t *sfl = staged<uint8_t>(buf + AO_FL, w.lo) - w.lo;
-    const double *sva = staged<double>(buf + AO_VA, w.lo) - w.lo;
-    const double *svb = staged<double>(buf + AO_VB, w.lo) - w.lo;
-    const float2 *sdi = staged<float2>(buf + AO_VB, w.lo) - w.lo;  // the same bytes as svb
-    double *xv = (double *)(buf + AO_SCR) - w.lo;                  // V at the start, by row
-    float2 *xd = (float2 *)(buf + AO_SCR + (kRowsAsm + 2) * 8) - w.lo;  // the predictor
-    // 1: V at the start of the step and the predictor of every row of the window
-    for (int64_t q = w.lo + threadIdx.x; q < w.hi; q += blockDim.x) {
-      if (sfl[q] & R_IDENT) continue;
-      const RowV o = first ? row_start_v(true, sva[q], svb[q], make_float2(0.f, 0.f))
-                           : row_start_v(false, sva[q], 0.0, sdi[q]);
-      xv[q] = o.vc;
-      xd[q] = make_float2(o.dp.hi, o.dp.lo);
-    }
-    __syncthreads();
-    // 2: the tile's rows; the difference to the mother in FP64, the DR neighbour's from
-    //    the next lane (its own mother difference; the last lane of a warp forms it itself)
-    const int64_t r = w.a + threadIdx.x;
-    const bool inside = r < w.a + w.cnt;
-    const uint8_t f = inside ? sfl[r] : (uint8_t)R_IDENT;
-    double dmo = 0.0, vmo = 0.0;
-    ff dpm{0.f, 0.f};
-    Topo t{};
-    if (!(f & R_IDENT) && (f & (R_FAR | R_DOWNL))) t = pv.topo[r];
-    if (!(f & R_IDENT) && (f & R_UP)) {
-      if (f & R_FAR) {
-        const RowV o = row_start(first, Va, Vb, Din, t.mother);
-        vmo = o.vc;
-        dpm = o.dp;
-      } else {
-        vmo = xv[r - 1];
-        dpm = pair(xd[r - 1]);
-      }
-      dmo = xv[r] - vmo;
-    }
-    const double dmo_next = __shfl_down_sync(0xffffffffu, dmo, 1);
-    if (!inside) return;
-    if (f & R_IDENT) {
-      c.w.y[r] = 0.f;
-      c.w.Wb[r] = 0.f;
-      return;
-    }
-    const int64_t k = r - w.a;
-    const double vc = xv[r];
-    const ff dp = pair(xd[r]);
-    const ff vcf = ff_of(vc);
-    ff wdx, kdx;
-    if (f & R_HH) {
-      float g0, g1, g2;
-      if (dense) {
-        g0 = staged<float>(buf + AO_X, w.a)[k];
-        g1 = staged<float>(buf + AO_X + win_bytes(kRowsAsm, 4), N + w.a)[k];
-        g2 = staged<float>(buf + AO_X + 2 * win_bytes(kRowsAsm, 4), 2 * N + w.a)[k];
-      } else {
-        g0 = gate[r];
-        g1 = gate[N + r];
-        g2 = gate[2 * N + r];
-      }
-      const int64_t hc = pv.hp_cls ? (int64_t)staged<uint32_t>(buf + AO_CLS, w.a)[k]
-                                   : (pv.hp_inst ? (int64_t)inst : r);
-      const HHParams32 q = hh_params32(pv.hpq, hc);
-      const float dv = fadd(fsub(vcf.hi, q.v[HP_REST]), vcf.lo);
-      GateStep32 g = hh_step32(dv + q.v[HP_LSNA], dv + q.v[HP_LSK], g0, g1, g2, q.v[HP_DTMS],
-                               q.v[HP_GNA], q.v[HP_GK], q.v[HP_GL], q.v[HP_ENA], q.v[HP_EK],
-                               q.v[HP_EL]);
-      gate[r] = g.m;
-      gate[N + r] = g.h;
-      gate[2 * N + r] = g.n;
-      const float dx = q.v[HP_DX];
-      wdx = ff_from(g.W * dx);
-      kdx = ff_from(g.K * dx);
-    } else if (!dense) {
-      wdx = pair(staged<float2>(buf + AO_X, w.a)[k]);
-      kdx = pair(staged<float2>(buf + AO_X + win_bytes(kRowsAsm, 8), w.a)[k]);
-    } else {
-      wdx = pair(iv.wdx2[r]);
-      kdx = pair(iv.kdx2[r]);
-    }
-    const float2 *sg = staged<float2>(buf + AO_G, w.a) - w.a;
-    double ddr = 0.0;
-    ff dpp{0.f, 0.f};
-    if (f & R_DOWNR) {  // row r + 1 is r's DR child: its mother difference is V_{r+1} - V_r
-      ddr = ((threadIdx.x & 31) == 31 || r + 1 >= w.a + w.cnt) ? xv[r + 1] - vc : dmo_next;
-      dpp = pair(xd[r + 1]);
-    }
-    // f = W dX V + K dX + I - g_j (V_j - V_mo) + g_DR (V_DR - V_j) - g_DL (V_j - V_DL)
-    ff fv = ff_add(ff_mul(vcf, wdx), kdx);
-    if (active && (f & R_INP)) fv = ff_add(fv, ff_of(iv.inp64[r]));
-    const ff gj = pair(sg[r]);
-    const ff gp = (f & R_DOWNR) ? pair(sg[r + 1]) : ff{0.f, 0.f};
-    const ff dmo_f = ff_of(dmo), ddr_f = ff_of(ddr);
-    float gdv = 0.f;  // sum_q g (V_j - V_q) in FP32, for ||b||
-    if (f & R_UP) {
-      fv = ff_sub(fv, ff_mul(gj, dmo_f));
-      gdv += gj.hi * dmo_f.hi;
-    }
-    if (f & R_DOWNR) {
-      fv = ff_add(fv, ff_mul(gp, ddr_f));
-      gdv -= gp.hi * ddr_f.hi;
-    }
-    ff gl{0.f, 0.f}, dpl{0.f, 0.f};
-    if (f & R_DOWNL) {
-      const RowV o = row_start(first, Va, Vb, Din, t.dl);
-      gl = pair(iv.g2[t.dl]);
-      const ff dl_f = ff_of(vc - o.vc);
-      fv = ff_sub(fv, ff_mul(gl, dl_f));
-      gdv += gl.hi * dl_f.hi;
-      dpl = o.dp;
-    }
-    ff cm = pair(staged<float2>(buf + AO_CM, w.a)[k]);
-    if (cn) {
-      fv = ff_scale2(fv);
-      cm = ff_scale2(cm);
-    }
-    const ff cj = ff_sub(cm, wdx);
-    cdiag[r] = cj.hi;
-    iv.clo[r] = cj.lo;
-    iv.fp2[r] = make_float2(fv.hi, fv.lo);
-    Dout[r] = make_float2(dp.hi, dp.lo);
-    if (!first) Vb[r] = vc;
-    // r0 = f - c d0 - sum_q g (d0_j - d0_q)
-    ff rr = ff_sub(fv, ff_mul(cj, dp));
-    if (f & R_UP) rr = ff_sub(rr, ff_mul(gj, ff_sub(dp, dpm)));
-    if (f & R_DOWNR) rr = ff_sub(rr, ff_mul(gp, ff_sub(dp, dpp)));
-    if (f & R_DOWNL) rr = ff_sub(rr, ff_mul(gl, ff_sub(dp, dpl)));
-    c.w.Wb[r] = rr.hi;
-    const float bs = (cj.hi * vcf.hi + gdv + fv.hi) * kNormScale;
-    const float rs = rr.hi * kNormScale;
-    bacc = fmaf(bs, bs, bacc);
-    racc = fmaf(rs, rs, racc);
-  };
-  row_tiles<kRowsAsm>(S, c.r0, c.r1, N, iv.err, issue, body);
-  return make_float2(bacc, racc);
-}
-
-// d + sum_{i < k} coef_i Z_i at row q (the cycle's solution update), Z_0 at q given.
-__device__ __forceinline__ ff updated_d(float2 d, float z0, const float *Z, int64_t N, int k,
-                                        const float *coef, int64_t q) {
-  float a = fmaf(coef[0], z0, 0.f);
-  for (int i = 1; i < k; i++) a = fmaf(coef[i], Z[(size_t)i * N + q], a);
-  return ff_add_f(ff{d.x, d.y}, a);
-}
-
-// Refinement residual of the double-float step: applies the last cycle's update
-// (d += sum_{i<k} coef_i Z_i, from buffer dc into buffer dc ^ 1) and forms
-// r = f - c d - sum_q g (d_j - d_q) as a pair; W_0 = r rounded to FP32.  Returns the
-// thread's part of ||r||^2 scaled by kNormScale^2.
-template <bool kGrid>
-__device__ __noinline__ float ph_residual_ff(Ctx<float, kGrid> c, int k, const float *coef, int dc) {
-  const PackView &pv = *c.pv;
-  const ImView &iv = *c.iv;
-  Shared S = carve(dyn_smem(), iv.m);
-  const int64_t N = pv.ntot;
-  const float2 *Din = iv.dp2[dc];
-  float2 *Dout = iv.dp2[dc ^ 1];
-  const float *Z = c.w.Z;
-  float acc = 0.f;
-  auto issue = [&](const RowWin &w, unsigned char *buf, uint64_t *bar) {
-    const int64_t nw = w.hi - w.lo;
-    const uint32_t bytes = stage_bytes<uint8_t>(w.a, w.cnt) + stage_bytes<float2>(w.lo, nw) +
-                           stage_bytes<float>(w.lo, nw) + stage_bytes<float2>(w.a, w.cnt) +
-                           2 * stage_bytes<float>(w.a, w.cnt) + stage_bytes<float2>(w.a, w.cnt + 1);
-    mbar_expect_tx(bar, bytes);
-    stage(buf + RO_FL, iv.rowf, w.a, w.cnt, bar);
-    stage(buf + RO_D, Din, w.lo, nw, bar);
-    stage(buf + RO_Z, Z, w.lo, nw, bar);
-    stage(buf + RO_F, (const float2 *)iv.fp2, w.a, w.cnt, bar);
-    stage(buf + RO_CH, (const float *)iv.cdiag, w.a, w.cnt, bar);
-    stage(buf + RO_CL, (const float *)iv.clo, w.a, w.cnt, bar);
-    stage(buf + RO_G, iv.g2, w.a, w.cnt + 1, bar);
-  };
-  auto body = [&](const RowWin &w, unsigned char *buf) {
-    const uint8_t *sfl = staged<uint8_t>(buf + RO_FL, w.a);
-    const float2 *sd = staged<float2>(buf + RO_D, w.lo) - w.lo;
-    const float *sz = staged<float>(buf + RO_Z, w.lo) - w.lo;
-    const float2 *sg = staged<float2>(buf + RO_G, w.a) - w.a;
-    for (int u = 0; u < kRowsRes / kThreads; u++) {
-      const int64_t kk = threadIdx.x + (int64_t)u * blockDim.x;
-      if (kk >= w.cnt) break;
-      const int64_t r = w.a + kk;
-      const uint8_t f = sfl[kk];
-      if (f & R_IDENT) {
-        c.w.Wb[r] = 0.f;
-        continue;
-      }
-      const ff dn = updated_d(sd[r], sz[r], Z, N, k, coef, r);
-      const ff fv = pair(staged<float2>(buf + RO_F, w.a)[kk]);
-      const ff cj{staged<float>(buf + RO_CH, w.a)[kk], staged<float>(buf + RO_CL, w.a)[kk]};
-      ff rr = ff_sub(fv, ff_mul(cj, dn));
-      if (f & R_UP) {
-        ff dm;
-        if (f & R_FAR) {
-          const int64_t q = pv.topo[r].mother;
-          dm = updated_d(Din[q], Z[q], Z, N, k, coef, q);
-        } else {
-          dm = updated_d(sd[r - 1], sz[r - 1], Z, N, k, coef, r - 1);
-        }
-        rr = ff_sub(rr, ff_mul(pair(sg[r]), ff_sub(dn, dm)));
-      }
-      if (f & R_DOWNR) {
-        const ff dp = updated_d(sd[r + 1], sz[r + 1], Z, N, k, coef, r + 1);
-        rr = ff_sub(rr, ff_mul(pair(sg[r + 1]), ff_sub(dn, dp)));
-      }
-      if (f & R_DOWNL) {
-        const int64_t q = pv.topo[r].dl;
-        const ff dl = updated_d(Din[q], Z[q], Z, N, k, coef, q);
-        rr = ff_sub(rr, ff_mul(pair(iv.g2[q]), ff_sub(dn, dl)));
-      }
-      Dout[r] = make_float2(dn.hi, dn.lo);
-      c.w.Wb[r] = rr.hi;
-      const float rs = rr.hi * kNormScale;
-      acc = fmaf(rs, rs, acc);
-    }
-  };
-  row_tiles<kRowsRes>(S, c.r0, c.r1, N, iv.err, issue, body);
-  return acc;
-}
-
-// Adds the product a * b to the pair accumulator s (a * b formed exactly as a pair).
-__device__ __forceinline__ void acc_prod(ff &s, float a, float b) {
-  const float p = fmul(a, b);
-  s = ff_add(s, ff{p, ffma(a, b, -p)});
-}
-
-// First Arnoldi step of a cycle: y = s_0 A Z_0, with <y, W_0> and ||y||^2 accumulated as
-// pairs per thread (hi, lo of each), so that ||y - h W_0||^2 = ||y||^2 - h^2 can be
-// resolved far below FP32's rounding of the sums.
-template <bool kGrid>
-__device__ __noinline__ DotAcc<float> ph_spmv0_ff(Ctx<float, kGrid> c, float s0) {
-  const PackView &pv = *c.pv;
-  const ImView &iv = *c.iv;
-  const int64_t stride = blockDim.x;
-  const float *CT = (const float *)iv.cdiag;
-  const float *Z0 = c.w.Z, *W0 = c.w.Wb;
-  ff yw{0.f, 0.f}, yy{0.f, 0.f};
-  for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kU * stride) {
-    float y[kU], w[kU];
-    uint8_t fl[kU];
-#pragma unroll
-    for (int u = 0; u < kU; u++) {
-      const int64_t r = rb + u * stride;
-      w[u] = r < c.r1 ? W0[r] : 0.f;
-    }
-    apply_rows_c<kU>(pv, iv, CT, iv.gf, Z0, rb, stride, c.r1, y, fl);
-#pragma unroll
-    for (int u = 0; u < kU; u++) {
-      const int64_t r = rb + u * stride;
-      y[u] *= s0;
-      if (r < c.r1) {
-        c.w.y[r] = y[u];
-        acc_prod(yw, y[u], w[u]);
-        acc_prod(yy, y[u], y[u]);
-      }
-    }
-  }
-  DotAcc<float> a;
-#pragma unroll
-  for (int i = 0; i < kG; i++) a.v[i] = 0.f;
-  a.v[0] = yw.hi;
-  a.v[1] = yw.lo;
-  a.v[2] = yy.hi;
-  a.v[3] = yy.lo;
-  return a;
-}
-
-// V = V_start + d for this group's rows (the potential a step produced; identity rows
-// keep theirs).
-template <bool kGrid>
-__device__ __noinline__ void ph_write_v_ff(Ctx<float, kGrid> c, const double *Vs, double *Vo, int dc) {
-  const ImView &iv = *c.iv;
-  const float2 *D = iv.dp2[dc];
-  for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x)
-    if (!(iv.rowf[j] & R_IDENT)) Vo[j] = add_ff(Vs[j], pair(D[j]));
-}
-
-// One step of the double-float path for one group (CTA or grid).  first: Va = V^n,
-// Vb = V^{n-1}; otherwise Va = V^{n-1}, the last step's correction is in buffer dc, and V^n
-// is written to Vb.  On return the step's correction is in buffer dc (updated).
-template <bool kGrid>
-__device__ __forceinline__ void implicit_one_step_ff(Ctx<float, kGrid> &c, cg::grid_group &grid,
-                                                     Shared &S, int &parity, const double *Va,
-                                                     double *Vb, bool first, bool active,
-                                                     int64_t inst_n, int inst, int &dc) {
-  const ImView &iv = *c.iv;
-  const int m = iv.m;
-  float *coef = (float *)S.coef;
-  const float2 br = ph_assemble_ff(c, Va, Vb, first, active ? 1 : 0, inst, dc);
-  dc ^= 1;
-  __syncthreads();
-  level_sync<kGrid>(grid);  // c of every row visible before the elimination
-  tree_factor(c);
-  double target = iv.tol, res0 = 0;
-  {
-    double acc[2] = {(double)br.x, (double)br.y};
-    group_reduce<kGrid>(grid, acc, 2, S, iv.partials, parity);  // also publishes W_0, d0
-    if (iv.tol_mode == NRT_TOL_REL) target = iv.tol * sqrt(S.red[0]) * kNormUnscale;
-    res0 = sqrt(S.red[1]) * kNormUnscale;
-    if (!kGrid) __syncthreads();
-  }
-  const int budget = iv.max_iter > 0 ? iv.max_iter : (int)inst_n;
-  const double inner_rel = iv.inner_rel;
-  int iters = 0, n_res = 0, n_app = 0, n_basis = 0, kprev = 0;
-  double res = 0;
-  bool converged = false;
-  for (int cycle = 0;; cycle++) {
-    // ---- cycle start: apply the last cycle's update, then r = f - A d (pairs), W_0 = r
-    if (cycle == 0) {
-      res = res0;
-    } else {
-      double acc[1] = {(double)ph_residual_ff(c, kprev, coef, dc)};
-      dc ^= 1;
-      group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);
-      res = sqrt(S.red[0]) * kNormUnscale;
-      n_res++;
-    }
-    if (res <= target) {
-      converged = true;
-      break;
-    }
-    if (iters >= budget || !(res == res) || res > 1e300) break;  // budget spent, or not finite
-    apply_precond(c, c.w.Wb, c.w.Z);
-    n_app++;
-    group_sync<kGrid>(grid);  // Z_0 of every row visible before the SpMV
-    if (threadIdx.x == 0) {
-      S.g[0] = res;
-      for (int i = 1; i <= m; i++) S.g[i] = 0;
-      S.s[0] = 1.0 / res;
-    }
-    __syncthreads();
-    const double cycle_target = fmax(target, inner_rel * res);
-    int k = 0;
-    for (int j = 0; j < m; j++) {
-      bool need_update = true;
-      if (j == 0) {
-        // y = s_0 A Z_0 with <y, W_0> and ||y||^2 as pairs: when the cycle stops after
-        // this step, ||W_1|| = sqrt(||y||^2 - h_00^2) replaces the update pass
-        {
-          DotAcc<float> acc = ph_spmv0_ff(c, (float)S.s[0]);
-          group_reduce<kGrid>(grid, acc.v, 4, S, iv.partials, parity);
-        }
-        if (threadIdx.x == 0) {
-          const double h = S.s[0] * (S.red[0] + S.red[1]);
-          const double yy = S.red[2] + S.red[3];
-          // an upper bound of ||W_1||: the estimate plus the pair sums' rounding
-          const double hn = sqrt(fmax(yy - h * h, 0.0) + 1e-12 * yy);
-          const double den = sqrt(h * h + hn * hn);
-          const double sn = den == 0 ? 0.0 : hn / den;
-          if (fabs(sn * S.g[0]) <= cycle_target || !(yy == yy)) {
-            S.s[1] = hn > 0 ? 1.0 / hn : 0.0;
-            S.cs[0] = den == 0 ? 1.0 : h / den;
-            S.sn[0] = sn;
-            S.H[0] = den;
-            S.g[1] = -sn * S.g[0];
-            S.g[0] = S.cs[0] * S.g[0];
-            S.flag[0] = 1;
-          } else {
-            S.H[0] = h;
-            coef[0] = (float)(h * S.s[0]);
-            S.flag[0] = 0;
-          }
-        }
-        __syncthreads();
-        need_update = !S.flag[0];
-      } else {
-        const int g1 = min(j + 1, kG);
-        {
-          DotAcc<float> acc = ph_spmv(c, j, (float)S.s[j], g1);
-          group_reduce<kGrid>(grid, acc.v, g1, S, iv.partials, parity);
-        }
-        for (int i0 = kG; i0 <= j; i0 += kG) {
-          const int gk = min(j + 1 - i0, kG);
-          DotAcc<float> acc = ph_products(c, i0, gk);
-          group_reduce<kGrid>(grid, acc.v, gk, S, iv.partials, parity, i0);
-        }
-        if (threadIdx.x <= j) {
-          const double h = S.s[threadIdx.x] * S.red[threadIdx.x];
-          S.H[threadIdx.x * m + j] = h;
-          coef[threadIdx.x] = (float)(h * S.s[threadIdx.x]);
-        }
-        __syncthreads();
-      }
-      if (need_update) {
-        // w = y - sum_i h_ij s_i W_i -> W_{j+1}; ||w||^2; Givens rotations
-        float nacc[1] = {ph_update(c, j, coef)};
-        group_reduce<kGrid>(grid, nacc, 1, S, iv.partials, parity);  // publishes W_{j+1}
-        if (threadIdx.x == 0) {
-          const double hn = sqrt(S.red[0]);
-          S.s[j + 1] = hn > 0 ? 1.0 / hn : 0.0;
-          for (int i = 0; i < j; i++) {
-            const double a = S.H[i * m + j], b = S.H[(i + 1) * m + j];
-            S.H[i * m + j] = S.cs[i] * a + S.sn[i] * b;
-            S.H[(i + 1) * m + j] = -S.sn[i] * a + S.cs[i] * b;
-          }
-          const double a = S.H[j * m + j];
-          const double den = sqrt(a * a + hn * hn);
-          S.cs[j] = den == 0 ? 1.0 : a / den;
-          S.sn[j] = den == 0 ? 0.0 : hn / den;
-          S.H[j * m + j] = den;
-          S.g[j + 1] = -S.sn[j] * S.g[j];
-          S.g[j] = S.cs[j] * S.g[j];
-          S.flag[0] = (fabs(S.g[j + 1]) <= cycle_target || hn == 0) ? 1 : 0;
-        }
-        __syncthreads();
-      }
-      k = j + 1;
-      iters++;
-      n_basis += j + 1;
-      if (S.flag[0] || iters >= budget || k >= m) break;
-      // Z_{j+1} = M^-1 W_{j+1}, only when another Arnoldi step will use it
-      apply_precond(c, c.w.Wb + (size_t)(j + 1) * c.pv->ntot, c.w.Z + (size_t)(j + 1) * c.pv->ntot);
-      n_app++;
-      group_sync<kGrid>(grid);  // Z_{j+1} of every row visible before the next SpMV
-    }
-    // ---- the update's coefficients y_i s_i; the next residual pass applies them
-    if (threadIdx.x == 0) {
-      for (int i = k - 1; i >= 0; i--) {
-        double a = S.g[i];
-        for (int l = i + 1; l < k; l++) a -= S.H[i * m + l] * S.y[l];
-        S.y[i] = a / S.H[i * m + i];
-      }
-      for (int i = 0; i < k; i++) coef[i] = (float)(S.y[i] * S.s[i]);
-    }
-    __syncthreads();
-    kprev = k;
-  }
-  if (threadIdx.x == 0 && (!kGrid || blockIdx.x == 0)) {
-    InstStat &st = iv.stats[inst];
-    st.iters += iters;
-    st.last_iters = iters;
-    st.last_res = res;
-    if (!converged) st.nonconv += 1;
-    st.residuals += n_res;
-    st.applies += n_app;
-    st.xupdates += n_res;  // every update is applied by the next residual pass
-    st.basis += n_basis;
-  }
-  group_sync<kGrid>(grid);  // the correction complete before the next step reads it
-}
-
-// Recording after a step of the double-float path: V = V_start + d at each probe (the
-// value the step's potential gets when it is written), or the untouched buffer value on an
-// identity row.
-__device__ __noinline__ void ph_record_ff(const RecView *rp, const ImView *ivp, int inst, int64_t i,
-                                          const double *Vs, const double *Vo, int dc, double dT) {
-  const RecView r = *rp;
-  const ImView &iv = *ivp;
-  const int a = r.p0[inst], b = r.p0[inst + 1];
-  for (int p = a + threadIdx.x; p < b; p += blockDim.x) {
-    const int64_t q = r.src[p];
-    const double v = (iv.rowf[q] & R_IDENT) ? Vo[q] : add_ff(Vs[q], pair(iv.dp2[dc][q]));
-    record_probe(r, p, i, v, dT);
-  }
-}
-
-// The steps of one group (an instance of a batch, or the whole grid for one tree) on the
-// double-float path; on return V holds the potentials the plain path leaves.
-template <bool kGrid>
-__device__ __forceinline__ void run_steps_ff(Ctx<float, kGrid> &c, cg::grid_group &grid, Shared &S,
-                                             int &parity, const InstDev &in, int nsteps, int force,
-                                             double *V0, double *V1, int cur, const RecView *rec,
-                                             int inst, int64_t inst_n) {
-  auto buf = [&](int k) { return (k & 1) ? V1 : V0; };
-  int dc = 0, s = 0;
-  for (; s < nsteps; s++) {
-    const int64_t i = in.base + s;
-    if (i >= in.iend) break;
-    const bool active = force >= 0 ? force != 0 : (i >= in.ion && i <= in.ioff);
-    const bool first = s == 0;
-    // V at the start of step s: buf(cur) for the first, else written by this step to
-    // buf(cur + s) from buf(cur + s - 1) and the last correction
-    const double *Va = first ? buf(cur) : buf(cur + s - 1);
-    double *Vb = first ? buf(cur + 1) : buf(cur + s);
-    implicit_one_step_ff<kGrid>(c, grid, S, parity, Va, Vb, first, active, inst_n, inst, dc);
-    if (rec && (!kGrid || blockIdx.x == 0))
-      ph_record_ff(rec, c.iv, kGrid ? 0 : inst, i, buf(cur + s), buf(cur + s + 1), dc, in.dT);
-  }
-  if (s > 0) {
-    // the last step's potential: V at its start (buf(cur + s - 1)) plus its correction
-    ph_write_v_ff(c, buf(cur + s - 1), buf(cur + s), dc);
-    if ((nsteps - s) & 1) {  // the run ended inside the launch: move it where the others' is
-      __syncthreads();
-      double *dst = buf(cur + nsteps);
-      const double *src = buf(cur + s);
-      for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x) dst[j] = src[j];
-    }
-  } else if (nsteps & 1) {
-    double *dst = buf(cur + nsteps);
-    const double *src = buf(cur);
-    for (int64_t j = c.r0 + threadIdx.x; j < c.r1; j += blockDim.x) dst[j] = src[j];
-  }
-}
-
-template <bool kGrid>
-__global__ void __launch_bounds__(kThreads, 4) implicit_steps_ff(const PackView *pvp, const ImView *ivp,
-                                                              int nsteps, int force, double *V0,
-                                                              double *V1, int cur,
-                                                              const RecView *rec) {
-  const ImView &iv = *ivp;
-  Shared S = carve(dyn_smem(), iv.m);
-  cg::grid_group grid = cg::this_grid();
-  int parity = 0;
-  if (threadIdx.x == 0) {
-    mbar_init(S.bar, 1);
-    mbar_init(S.bar + 1, 1);
-    mbar_init(S.bar + 2, 1);
-    S.flag[2] = 0;
-    S.flag[3] = 0;
-  }
-  __syncthreads();
-  Ctx<float, kGrid> c;
-  c.pv = pvp;
-  c.iv = ivp;
-  c.w.Wb = (float *)iv.Wb;
-  c.w.Z = (float *)iv.Z;
-  c.w.y = (float *)iv.yv;
-  c.w.pd = (float *)iv.pcd;
-  c.w.pc = (float *)iv.pcc;
-  if (kGrid) {
-    c.r0 = iv.cta_row[blockIdx.x];
-    c.r1 = iv.cta_row[blockIdx.x + 1];
-    c.t0 = iv.cta_tile[blockIdx.x];
-    c.t1 = iv.cta_tile[blockIdx.x + 1];
-    c.l0 = iv.work_lev[blockIdx.x];
-    c.l1 = iv.work_lev[blockIdx.x + 1];
-    run_steps_ff<kGrid>(c, grid, S, parity, pvp->inst[0], nsteps, force, V0, V1, cur, rec, 0,
-                        iv.inst_row[1] - iv.inst_row[0]);
-  } else {
-    for (;;) {
-      if (threadIdx.x == 0) S.flag[1] = atomicAdd(iv.queue, 1);
-      __syncthreads();
-      const int q = S.flag[1];
-      __syncthreads();
-      if (q >= iv.ninst) break;
-      const int inst = iv.order[q];
-      c.r0 = iv.inst_row[inst];
-      c.r1 = iv.inst_row[inst + 1];
-      c.t0 = iv.inst_tile[inst];
-      c.t1 = iv.inst_tile[inst + 1];
-      c.l0 = iv.work_lev[inst];
-      c.l1 = iv.work_lev[inst + 1];
-      run_steps_ff<kGrid>(c, grid, S, parity, pvp->inst[inst], nsteps, force, V0, V1, cur, rec,
-                          inst, c.r1 - c.r0);
-      __syncthreads();
-    }
-  }
-}
-
 // One backward-Euler step of one group (CTA or grid) for instance `inst`.
 template <typename T, bool kGrid>
 __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_group &grid,
@@ -2419,16 +1662,6 @@ __global__ void __launch_bounds__(kThreads, 4) implicit_steps(const PackView *pv
       }
       __syncthreads();
     }
-  }
-}
-
-// hi = x rounded to FP32, lo = (x - hi) rounded: the pair form of a static FP64 array (set-up
-// only; its FP64 arithmetic runs once per handle).
-__global__ void split_pairs(const double *x, float2 *out, int64_t n) {
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
-       j += (int64_t)gridDim.x * blockDim.x) {
-    const float h = __double2float_rn(x[j]);
-    out[j] = make_float2(h, __double2float_rn(x[j] - (double)h));
   }
 }
 
@@ -2829,12 +2062,6 @@ int Engine::implicit_plan(size_t &bytes) {
     auto kern = mixed ? implicit_steps<float, true> : implicit_steps<double, true>;
     NRT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
     NRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, S.smem));
-    if (mixed) {  // the double-float step must fit the same cooperative grid
-      int per_sm_ff = 0;
-      NRT_CUDA(cudaFuncSetAttribute(implicit_steps_ff<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
-      NRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ff, implicit_steps_ff<true>, kThreads, S.smem));
-      per_sm = std::min(per_sm, per_sm_ff);
-    }
     if (per_sm < 1) {
       set_error("implicit kernel does not fit on an SM");
       return NRT_EDEVICE;
@@ -2875,8 +2102,6 @@ int Engine::implicit_plan(size_t &bytes) {
     auto kern = mixed ? implicit_steps<float, false> : implicit_steps<double, false>;
     NRT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
     NRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, S.smem));
-    if (mixed)
-      NRT_CUDA(cudaFuncSetAttribute(implicit_steps_ff<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
     S.grid_blocks = std::max(1, std::min<int>(dev_sms * std::max(per_sm, 1), ni));
     S.inst_tile.assign(ni + 1, 0);
     for (int32_t i = 0; i < ni; i++) {
@@ -2920,8 +2145,6 @@ int Engine::implicit_plan(size_t &bytes) {
     b += 4 * al256(tb * ns);                                // sg, sinv, se, sy
     b += 2 * al256(tb * nseg);                              // exp_d, exp_b
   }
-  if (mixed && opt.krylov == NRT_GMRES && tree)
-    b += 7 * al256(8 * N) + al256(4 * N);  // double-float step: cm, g, W dX, K dX, f, 2 d; c
   bytes = b + 4096;
   return NRT_OK;
 }
@@ -3058,31 +2281,6 @@ int Engine::implicit_init() {
     NRT_CUDA(cudaMemsetAsync(iv.se, 0, tb * ns, st));
     NRT_CUDA(cudaMemsetAsync(iv.sy, 0, tb * ns, st));
   }
-  iv.ff = (mixed && opt.krylov == NRT_GMRES && opt.precond == NRT_PRECOND_TREE) ? 1 : 0;
-  if (iv.ff) {
-    float2 *cm2 = (float2 *)arena.take(8 * N), *g2 = (float2 *)arena.take(8 * N);
-    float2 *wdx2 = (float2 *)arena.take(8 * N), *kdx2 = (float2 *)arena.take(8 * N);
-    iv.clo = (float *)arena.take(4 * N);
-    iv.fp2 = (float2 *)arena.take(8 * N);
-    iv.dp2[0] = (float2 *)arena.take(8 * N);
-    iv.dp2[1] = (float2 *)arena.take(8 * N);
-    if (!cm2 || !g2 || !wdx2 || !kdx2 || !iv.clo || !iv.fp2 || !iv.dp2[0] || !iv.dp2[1]) {
-      set_error("arena exhausted (double-float step)");
-      return NRT_ENOMEM;
-    }
-    int sms = 0;
-    NRT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    const int blocks = 4 * std::max(sms, 1);
-    split_pairs<<<blocks, 256, 0, st>>>(iv.cmdt, cm2, N);
-    split_pairs<<<blocks, 256, 0, st>>>(iv.g64, g2, N);
-    split_pairs<<<blocks, 256, 0, st>>>(iv.wdx64, wdx2, N);
-    split_pairs<<<blocks, 256, 0, st>>>(iv.kdx64, kdx2, N);
-    NRT_CUDA(cudaGetLastError());
-    iv.cm2 = cm2;
-    iv.g2 = g2;
-    iv.wdx2 = wdx2;
-    iv.kdx2 = kdx2;
-  }
   S.d_pv = (PackView *)arena.take(sizeof(PackView));
   S.d_iv = (ImView *)arena.take(sizeof(ImView));
   if (!S.d_pv || !S.d_iv) {
@@ -3107,15 +2305,11 @@ static int implicit_launch(Engine &e, int nsteps, int force) {
   const RecView *rec = force < 0 ? e.record_view() : nullptr;
   void *args[] = {&pv, &iv, &nsteps, &force, &V0, &V1, &cur, &rec};
   const bool mixed = e.opt.precision == NRT_MIXED;
-  // the double-float step, unless an assembly-only pass (export) is asked for
-  const bool ff = S.iv.ff && S.iv.max_iter >= 0;
   if (S.grid_mode) {
-    const void *k = ff ? (const void *)implicit_steps_ff<true>
-                       : (mixed ? (const void *)implicit_steps<float, true> : (const void *)implicit_steps<double, true>);
+    const void *k = mixed ? (const void *)implicit_steps<float, true> : (const void *)implicit_steps<double, true>;
     NRT_CUDA(cudaLaunchCooperativeKernel(k, dim3(S.grid_blocks), dim3(kThreads), args, S.smem, e.stream));
   } else {
-    const void *k = ff ? (const void *)implicit_steps_ff<false>
-                       : (mixed ? (const void *)implicit_steps<float, false> : (const void *)implicit_steps<double, false>);
+    const void *k = mixed ? (const void *)implicit_steps<float, false> : (const void *)implicit_steps<double, false>;
     NRT_CUDA(cudaLaunchKernel(k, dim3(S.grid_blocks), dim3(kThreads), args, S.smem, e.stream));
   }
   return NRT_OK;

@@ -49,26 +49,6 @@ __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async;" ::: "memory");
 }
 
-// Bytes of the bulk copy of elements [o, o + n) of an array (16-byte aligned base): the
-// window rounded out to 16-byte boundaries.
-template <typename X>
-__device__ __forceinline__ uint32_t stage_bytes(int64_t o, int64_t n) {
-  const uint64_t lo = ((uint64_t)o * sizeof(X)) & ~(uint64_t)15;
-  const uint64_t hi = ((uint64_t)(o + n) * sizeof(X) + 15) & ~(uint64_t)15;
-  return (uint32_t)(hi - lo);
-}
-template <typename X>
-__device__ __forceinline__ void stage(unsigned char *dst, const X *a, int64_t o, int64_t n,
-                                      uint64_t *bar) {
-  const uint64_t lo = ((uint64_t)o * sizeof(X)) & ~(uint64_t)15;
-  bulk_load(dst, (const char *)a + lo, stage_bytes<X>(o, n), bar);
-}
-// The shared-memory copy of element o of a staged array.
-template <typename X>
-__device__ __forceinline__ const X *staged(const unsigned char *dst, int64_t o) {
-  return (const X *)(dst + (((uint64_t)o * sizeof(X)) & 15));
-}
-
 // Waits for phase `phase` of the tile barrier; gives up after about two seconds of
 // clock (the copies it waits for are in bounds and always land, so giving up means a
 // device fault), raising the error word the host checks.
