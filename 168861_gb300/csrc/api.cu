@@ -430,6 +430,7 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   pv.tile_blocks = (mixed && opt.mode == NRT_EXPLICIT && opt.tiled != 0)
                        ? explicit_tile_blocks(device, N, opt.tile_ctas_per_sm) : 0;
   pv.step_threads = opt.step_threads;
+  NRT_CUDA(cudaDeviceGetAttribute(&pv.sms, cudaDevAttrMultiProcessorCount, device));
   if (mixed) {
     auto f32 = [&](const std::vector<double> &v) {
       hostf.emplace_back(v.size());

@@ -477,7 +477,7 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
   // Small trees: spread the elements over as many SMs as possible (the FP64 pipe of one
   // SM, not memory, bounds a small block); large packs: 256-thread blocks.
   int threads = 256;
-  while (threads > 32 && pv.ntot < (int64_t)threads * 2 * 152) threads >>= 1;
+  while (threads > 32 && pv.ntot < (int64_t)threads * 2 * (pv.sms > 0 ? pv.sms : 1)) threads >>= 1;
   if (pv.step_threads > 0) threads = pv.step_threads;  // a tuned shape (same results)
   const unsigned blocks = (unsigned)((pv.ntot + threads - 1) / threads);
   if (precision == NRT_MIXED) {

@@ -132,6 +132,7 @@ struct PackView {
   int *err;            // device error word (a bounded wait gave up), or null
   int tile_blocks;     // mixed explicit: persistent CTAs of the tiled step (0: untiled)
   int step_threads;    // explicit, one thread per element: threads per block (0: by size)
+  int sms;             // multiprocessors of the handle's device
 };
 
 // Device-side recording at probes (record.cu, record.cuh).  Probes are sorted by

@@ -60,8 +60,6 @@ def lib(pkg):
 @pytest.fixture(scope="session")
 def gpu(lib):
     """Requires a visible CUDA device; the GPU tests have no fallback."""
-    import ctypes
-    cudart = ctypes.CDLL("libcudart.so", mode=ctypes.RTLD_GLOBAL) if False else None  # noqa: F841
     import torch
     if not torch.cuda.is_available():
         pytest.fail("the -m gpu tests need a CUDA device")

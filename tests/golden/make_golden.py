@@ -69,7 +69,7 @@ def cases(ref_dir: str):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("NEURITE_REFERENCE", "/root/reference"))
     ap.add_argument("--only", default="")
     args = ap.parse_args()
     O.build(ref_dir=args.ref, with_ref=True)

@@ -9,7 +9,7 @@ import pytest
 from conftest import ROOT, load_golden
 
 DROPIN = os.path.join(ROOT, "tests", "dropin")
-REF_INC = "/root/reference/inc"
+REF_INC = os.path.join(os.environ.get("NEURITE_REFERENCE", "/root/reference"), "inc")
 
 
 def _compile(lib, out):
