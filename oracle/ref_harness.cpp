@@ -30,6 +30,7 @@
 #include "coupling.h"
 #include "solver.h"
 #include "solverEx-cpu.h"
+#include "space.h"
 #ifdef WITH_IMPLICIT
 #include "solverIm-cpu.h"
 #endif
@@ -69,8 +70,37 @@ static void expect(FILE *f, const char *key) {
   }
 }
 
+// Mode L: the reference's own loader of a segmented neuron (src/space.cpp:37-183, selected
+// by simulation=CT_segmented_neuron at src/init.cpp:120-121) reads <dir>/neuron_for_neurite.txt
+// (through the working_directory variable, as the reference's driver arranges it); the
+// elements it builds are written to <out.txt>: one line "n num_terminals", the terminals,
+// then per element "mother DR DL branching dX diameter input_current" (%.17g).
+static int dump_loader(const char *dir, const char *out_path) {
+  setenv("working_directory", dir, 1);
+  standard = stdout;
+  input in;
+  memset(&in, 0, sizeof(in));
+  discretization **element = NULL;
+  Cable **ct = NULL;
+  int num_ct = 0;
+  loading_neuron_passive_dendritic_tree(in, element, ct, num_ct);
+  FILE *o = fopen(out_path, "w");
+  if (!o) die("cannot open output");
+  fprintf(o, "%d %d\n", numStepsX, num_terminals);
+  for (int i = 0; i < num_terminals; i++) fprintf(o, "%d ", terminals[i]);
+  fprintf(o, "\n");
+  for (int i = 0; i < numStepsX; i++) {
+    discretization *e = element[i];
+    fprintf(o, "%d %d %d %d %.17g %.17g %.17g\n", e->get_mother(), e->get_DR(), e->get_DL(),
+            e->get_branching() ? 1 : 0, e->get_dX(), e->get_diameter(), e->get_input_current());
+  }
+  fclose(o);
+  return 0;
+}
+
 int main(int argc, char **argv) {
-  if (argc < 4) die("usage: ref_harness <spec.txt> <out.txt> <e|i>");
+  if (argc < 4) die("usage: ref_harness <spec.txt | dir> <out.txt> <e|i|L>");
+  if (argv[3][0] == 'L') return dump_loader(argv[1], argv[2]);
   FILE *f = fopen(argv[1], "r");
   if (!f) die("cannot open spec");
   bool implicit_mode = (argv[3][0] == 'i');

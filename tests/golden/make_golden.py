@@ -9,8 +9,10 @@ oracle/Makefile and oracle/ref_harness.cpp) and oracle/_ref/ref_harness_im (plus
 src/solverIm-cpu.cpp with the RCI shim), runs them on each case below and stores, per
 case, the tree description and the reference outputs: derived parameters, critical and
 chosen dT, a probe trace, the final potential and gates, and the reference's measurement
-point (src/init.cpp:339-358) for a few distances along the tree.  The GPU tests and the oracle
-tests read only these .npz files, so nothing at test time needs the reference tree.
+point (src/init.cpp:339-358) for a few distances along the tree.  loader_example8.npz holds
+what the reference's own loader (src/space.cpp:37-183) builds from its example-8 neuron file.
+The GPU tests and the oracle tests read only these .npz files, so nothing at test time needs
+the reference tree.
 """
 from __future__ import annotations
 
@@ -67,12 +69,45 @@ def cases(ref_dir: str):
     return out
 
 
+def loader_golden(ref_dir: str) -> None:
+    """loader_example8.npz: the reference's own loader (src/space.cpp:37-183, through the
+    harness's mode L) on applications/example_8/neuron_for_neurite.txt.  Stores the file's
+    seven columns as numbers (the input) and the elements the reference built from them."""
+    import shutil
+    import subprocess
+    src = os.path.join(ref_dir, "applications", "example_8", "neuron_for_neurite.txt")
+    text = open(src).read()
+    rows = [r.split() for r in text.strip().splitlines() if r.strip()]
+    ints = np.array([[int(x) for x in r[:5]] for r in rows], np.int32)
+    flts = np.array([[float(x) for x in r[5:7]] for r in rows], np.float64)
+    with tempfile.TemporaryDirectory() as td:
+        shutil.copy(src, os.path.join(td, "neuron_for_neurite.txt"))
+        out = os.path.join(td, "elements.txt")
+        subprocess.run([O.REF_BIN, td, out, "L"], check=True, capture_output=True)
+        lines = open(out).read().splitlines()
+    n, nterm = (int(x) for x in lines[0].split())
+    terms = np.array([int(x) for x in lines[1].split()], np.int32)
+    el = [ln.split() for ln in lines[2:2 + n]]
+    np.savez_compressed(
+        os.path.join(HERE, "loader_example8.npz"),
+        rows_int=ints, rows_float=flts, num_terminals=np.array(nterm), terminals=terms,
+        mother=np.array([int(e[0]) for e in el], np.int32),
+        dr=np.array([int(e[1]) for e in el], np.int32),
+        dl=np.array([int(e[2]) for e in el], np.int32),
+        branching=np.array([int(e[3]) for e in el], np.int32),
+        dX=np.array([float(e[4]) for e in el]), diameter=np.array([float(e[5]) for e in el]),
+        input_current=np.array([float(e[6]) for e in el]))
+    print(f"loader_example8: n={n} terminals={nterm}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("NEURITE_REFERENCE", "/root/reference"))
     ap.add_argument("--only", default="")
     args = ap.parse_args()
     O.build(ref_dir=args.ref, with_ref=True)
+    if args.only in ("", "loader_example8"):
+        loader_golden(args.ref)
     for name, spec, mode, rec, probes, cap in cases(args.ref):
         if args.only and args.only != name:
             continue
