@@ -7,10 +7,13 @@ Run with `-s` to see the per-configuration figures (one ACCURACY line each).
 Configurations (seeded, sizes as in the workload definitions, horizons cut where the oracle
 would take minutes):
   1. the 1 cm / 1000-compartment squid axon, explicit at 0.8 dT_crit, 10 ms;
-  2. the depth-10 random binary tree (2.6e5 compartments), implicit dt 0.01 ms, 6 ms;
+  2. the depth-10 random binary tree (2.6e5 compartments), implicit Crank-Nicolson as that
+     workload specifies, dt 0.01 ms, 6 ms;
   3. a scaled myelinated axon (6 nodes, 200 um internodes, 20% static strain), explicit,
      20000 steps (nanoseconds of simulated time: the internode step is ~5e-11 s);
-  4. eight trees of the batched population (implicit, dt 0.025 ms, 20 ms) in one batch.
+  4. six trees spanning the batched population's sizes (1e3 to 1e5 compartments, the
+     smallest and the largest included; implicit, dt 0.025 ms) in one batch over the full
+     50 ms horizon, probes recorded on the device every step.
 """
 import json
 
@@ -88,9 +91,9 @@ def test_config3_myelinated_explicit_mixed(gpu, pkg, orc, model):
                   "3 myelinated axon explicit mixed, 20000 steps")
 
 
-def implicit_oracle(orc, spec, steps, rec, probes):
+def implicit_oracle(orc, spec, steps, rec, probes, scheme=0):
     Vo, _, tr, _ = orc.implicit_run(spec, orc.derive(spec), spec.dt_abs, 1, 1 + steps,
-                                    linsolve=0, record_every=rec, probes=probes)
+                                    linsolve=0, record_every=rec, probes=probes, scheme=scheme)
     return Vo, tr
 
 
@@ -98,40 +101,43 @@ def test_config2_binary_tree_implicit_mixed(gpu, pkg, orc, model):
     spec = model.random_binary_tree(depth=10, seed=2, tspan=6e-3)
     steps, probes = 600, np.array([1, 500, spec.n // 2, spec.n - 2])
     s = pkg.SolverIm(pkg.ProblemArrays.from_spec(spec, pkg.derive(spec)), precision="mixed",
-                     restart=20, tol=1e-10, tol_mode="rel", precond="tree")
+                     restart=20, tol=1e-10, tol_mode="rel", precond="tree", scheme="cn")
     s.init_time, s.end_input = spec.init_time, spec.end_input
     g = record_gpu(s, 1 + steps, 1, probes)
     Vg = s.snapshot()
     s.close()
-    Vo, tr = implicit_oracle(orc, spec, steps, 1, probes)
+    Vo, tr = implicit_oracle(orc, spec, steps, 1, probes, scheme=1)
     tr = tr[: len(g)]
     t = tr[:, 0] * spec.dt_abs
     dv = max(float(np.abs(g - tr[:, 1:]).max()), float(np.abs(Vg - Vo).max()))
-    report("2 binary tree implicit mixed, 6 ms", dv, spike_times(t, g), spike_times(t, tr[:, 1:]))
+    report("2 binary tree implicit Crank-Nicolson mixed, 6 ms", dv, spike_times(t, g),
+           spike_times(t, tr[:, 1:]))
 
 
 def test_config4_batched_trees_implicit_mixed(gpu, pkg, orc, model):
-    sizes = model.log_uniform_sizes(8, 1e3, 2e4, 7)
-    specs = [model.random_tree(seed=900 + k, n_target=int(n), tspan=20e-3)
-             for k, n in enumerate(sizes)]
-    steps = 800
+    sizes = [1000, 100000] + [int(x) for x in model.log_uniform_sizes(4, 1e3, 1e5, 7)]
+    specs = [model.random_tree(seed=900 + k, n_target=n) for k, n in enumerate(sizes)]
+    steps = specs[0].num_steps(specs[0].dt_abs) - 2  # 50 ms at 0.025 ms
+    assert all(sp.dt_abs == specs[0].dt_abs and sp.tspan == 50e-3 for sp in specs)
     probes = [np.array([1, sp.n // 3, sp.n - 2]) for sp in specs]
     b = pkg.Batch([pkg.ProblemArrays.from_spec(sp, pkg.derive(sp)) for sp in specs], mode=1,
                   precision="mixed", restart=20, tol=1e-10, tol_mode="rel", precond="tree")
     b.set_runs([(1, 1 + steps, sp.init_time, sp.end_input) for sp in specs])
-    rows = [[] for _ in specs]
-    for _ in range(steps):
-        b.advance(1)
-        for k in range(len(specs)):
-            rows[k].append(b.snapshot(k)[probes[k]])
-    dv, ta, tb = 0.0, [], []
+    b.record([(k, e) for k, pr in enumerate(probes) for e in pr], interval=0, capacity=steps + 1)
+    b.advance(steps)
+    rec = b.recording()
+    finals = [b.snapshot(k) for k in range(len(specs))]
+    b.close()
+    dv, ta, tb, q = 0.0, [], [], 0
     for k, sp in enumerate(specs):
-        g = np.array(rows[k])
+        g = np.stack([rec.values[q + j] for j in range(len(probes[k]))], axis=1)
+        q += len(probes[k])
         Vo, tr = implicit_oracle(orc, sp, steps, 1, probes[k])
         tr = tr[: len(g)]
+        assert len(g) == steps and len(tr) == steps
         t = tr[:, 0] * sp.dt_abs
-        dv = max(dv, float(np.abs(g - tr[:, 1:]).max()), float(np.abs(b.snapshot(k) - Vo).max()))
+        dv = max(dv, float(np.abs(g - tr[:, 1:]).max()), float(np.abs(finals[k] - Vo).max()))
         ta.append(spike_times(t, g))
         tb.append(spike_times(t, tr[:, 1:]))
-    b.close()
-    report("4 eight batched trees implicit mixed, 20 ms", dv, np.concatenate(ta), np.concatenate(tb))
+    report(f"4 six batched trees of {min(sizes)}-{max(s.n for s in specs)} compartments "
+           "implicit mixed, 50 ms", dv, np.concatenate(ta), np.concatenate(tb))

@@ -112,6 +112,31 @@ def test_implicit_large_tree_cooperative(gpu, pkg, orc, model, precond):
     assert np.abs(s.snapshot() - Vo).max() < TOL_FP64
 
 
+def test_config2_fp64_crank_nicolson_full_size(gpu, pkg, orc, model):
+    """The Crank-Nicolson workload's tree at full size -- a depth-10 random binary tree
+    (2047 branches, about 2.6e5 compartments at dx 1 um, HH everywhere, 2 nA at the root,
+    dt 0.01 ms) -- in plain FP64 with that workload's solver settings (GMRES(30), tree
+    preconditioner, tolerance 1e-10 relative) against the oracle's exact Crank-Nicolson
+    solve, over 600 steps (6 ms: the stimulus and the first spikes), at 1e-9 V."""
+    spec = model.random_binary_tree(depth=10, seed=2, tspan=6e-3)
+    steps = 600
+    s = pkg.SolverIm(pkg.ProblemArrays.from_spec(spec, pkg.derive(spec)), precision="fp64",
+                     restart=30, tol=1e-10, tol_mode="rel", precond="tree", max_iter=2000,
+                     scheme="cn")
+    s.run(1, 1 + steps, spec.init_time, spec.end_input)
+    V = s.snapshot()
+    st = s.stats()
+    s.close()
+    Vo, _, _, _ = orc.implicit_run(spec, orc.derive(spec), spec.dt_abs, 1, 1 + steps,
+                                   linsolve=0, scheme=1)
+    assert spec.n > 250000
+    assert st.nonconverged_steps == 0
+    err = np.abs(V - Vo).max()
+    print(f"\nconfig 2 FP64 Crank-Nicolson, n={spec.n}, {steps} steps: max |dV| = {err:.3g} V")
+    assert np.nanmax(Vo) > 0.0  # the run spikes
+    assert err < TOL_FP64
+
+
 @pytest.mark.parametrize("steps,advance", [(15, 16), (15, 64), (14, 17)])
 def test_cooperative_run_ending_inside_a_launch(gpu, pkg, orc, model, steps, advance):
     """A one-tree batch on the cooperative launch whose run ends before the launch's step
