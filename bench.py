@@ -66,6 +66,9 @@ def parse():
                     help="implicit workloads: GMRES preconditioner")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain-FP64 single-tree comparison run")
+    ap.add_argument("--sub-results", choices=("auto", "on", "off"), default="auto",
+                    help="also measure the other workloads and attach them in compact form "
+                         "(auto: with the default workload on one GPU)")
     ap.add_argument("--autotune", action="store_true",
                     help="explicit workloads: run on the launch shape the autotuner picks "
                          "(tuned before the timed regions; default: the automatic shapes)")
@@ -100,15 +103,20 @@ def combine_ranks(dist, device, ms: float, e2e_s: float, n_elem: int, alg_bytes:
     return float(t[0]), float(t[1]), float(s[0]), float(s[1])
 
 
+_POPULATION = {}  # (count, seed, rank, world) -> [(spec, derived)]: built once per process
+
+
 def build_batch_problems(workload: str, count: int, seed: int, rank: int, world: int):
     pkg = importlib.import_module("168861_gb300")
     model = pkg.model
-    pop = shard(tree_population(count, seed), rank, world)
+    key = (count, seed, rank, world)
+    if key not in _POPULATION:
+        _POPULATION[key] = [(s, pkg.derive(s)) for s in
+                            (model.random_tree(seed=tseed, n_target=size)
+                             for tseed, size in shard(tree_population(count, seed), rank, world))]
     probs, runs = [], []
     n_elem = 0
-    for tseed, size in pop:
-        spec = model.random_tree(seed=tseed, n_target=size)
-        d = pkg.derive(spec)
+    for spec, d in _POPULATION[key]:
         if workload.startswith("batch-explicit"):
             dT = 0.8 * d.dT_crit
         else:
@@ -117,7 +125,6 @@ def build_batch_problems(workload: str, count: int, seed: int, rank: int, world:
         probs.append(p)
         runs.append((1, spec.num_steps(dT) - 1, spec.init_time, spec.end_input))
         n_elem += spec.n
-        del spec, d
     return probs, runs, n_elem
 
 
@@ -323,20 +330,16 @@ def plain_fp64_single(pkg, torch):
 
 # ------------------------------------------------------------------ our arm
 
-def run_ours(args, rank: int, world: int):
+def run_ours(args, rank: int, world: int, dist, wl: str, extras: bool = True, steps: int = 0):
+    """One workload on our arm; returns its JSON line (rank 0) or None.  extras: the plain
+    FP64 comparison (implicit) and the CPU baseline leg."""
     import torch
     pkg = importlib.import_module("168861_gb300")
     local = int(os.environ.get("LOCAL_RANK", 0))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    wl = args.workload
     count = args.trees or (4096 if wl.startswith("batch") else 1)
     precision = "fp64" if wl.endswith("fp64") else "mixed"
     implicit = wl.startswith("batch-implicit")
-    K = args.steps or (40 if implicit else 2048)
+    K = steps or args.steps or (40 if implicit else 2048)
     W = max(3, args.warmup)
 
     t_build = time.time()
@@ -468,7 +471,7 @@ def run_ours(args, rank: int, world: int):
         "krylov": krylov,
     }
     b.close()
-    if rank == 0:
+    if rank == 0 and extras:
         if implicit and not args.no_plain:
             try:
                 line["plain_fp64_single"] = plain_fp64_single(pkg, torch)
@@ -480,17 +483,24 @@ def run_ours(args, rank: int, world: int):
                 line["cpu_baseline"] = cpu_baseline(wl, args.seed, count)
             except Exception as exc:  # the GPU line is still reported
                 line["cpu_baseline"] = {"value": None, "error": repr(exc)[:300]}
-        print(json.dumps(line), flush=True)
-    if dist:
-        dist.destroy_process_group()
+    return line if rank == 0 else None
 
 
 # ------------------------------------------------------------------ serving
 
 def serve_requests(count: int, seed: int):
-    """Request stream: Poisson arrivals (mean 2000 req/s); half explicit squid axons of
-    the 1 cm / 1002-element kind, half implicit random trees of the batched population;
-    simulated time U(10, 100) ms."""
+    """Request stream: Poisson arrivals (mean 2000 req/s), drawn in turn from the four
+    workload shapes:
+      - explicit 1 cm / 1002-element squid axons (dt 0.8 dT_crit), simulated U(10, 100) ms;
+      - implicit random trees of the batched population (1e3-1e5 elements, dt 0.025 ms),
+        simulated U(10, 100) ms;
+      - implicit random binary trees of the Crank-Nicolson workload's shape (depth 6-9,
+        dx 1 um, 2 nA at the root, dt 0.01 ms), simulated U(10, 100) ms, stepped with the
+        server's implicit settings;
+      - explicit myelinated axons of that workload's shape (4-10 nodes of Ranvier, 1 mm
+        internodes, dx 1 um), simulated U(0.5, 2) us: their internode step is ~5e-11 s, so
+        10 ms would be 2e8 steps.
+    Returns (gap to the previous arrival, problem, implicit, run) per request."""
     pkg = importlib.import_module("168861_gb300")
     model = pkg.model
     rng = np.random.default_rng(seed)
@@ -498,41 +508,74 @@ def serve_requests(count: int, seed: int):
     out = []
     sizes = model.log_uniform_sizes(count, 1e3, 1e5, seed + 1)
     for q in range(count):
-        t_ms = rng.uniform(10.0, 100.0)
-        if q % 2 == 0:
-            spec = model.straight_axon(dtf=0.8, tspan=t_ms * 1e-3)
+        kind = q % 4
+        if kind == 0:
+            spec = model.straight_axon(dtf=0.8, tspan=rng.uniform(10.0, 100.0) * 1e-3)
             d = pkg.derive(spec)
-            dT = pkg.step_size(spec, d)
-            implicit = False
+            dT, implicit = pkg.step_size(spec, d), False
+        elif kind == 1:
+            spec = model.random_tree(seed=seed * 31 + q, n_target=int(sizes[q]),
+                                     tspan=rng.uniform(10.0, 100.0) * 1e-3)
+            d = pkg.derive(spec)
+            dT, implicit = spec.dt_abs, True
+        elif kind == 2:
+            spec = model.random_binary_tree(depth=int(rng.integers(6, 10)), seed=seed * 37 + q,
+                                            tspan=rng.uniform(10.0, 100.0) * 1e-3)
+            d = pkg.derive(spec)
+            dT, implicit = spec.dt_abs, True
         else:
-            spec = model.random_tree(seed=seed * 31 + q, n_target=int(sizes[q]), tspan=t_ms * 1e-3)
+            spec = model.myelinated_axon(n_nodes=int(rng.integers(4, 11)))
             d = pkg.derive(spec)
-            dT = spec.dt_abs
-            implicit = True
+            dT, implicit = 0.8 * d.dT_crit, False
+            spec.tspan = rng.uniform(0.5, 2.0) * 1e-6
         p = pkg.ProblemArrays.from_spec(spec, d, dT)
         out.append((float(gaps[q]), p, implicit,
                     (1, spec.num_steps(dT) - 1, spec.init_time, spec.end_input)))
     return out
 
 
-def run_serve(args, rank: int, world: int):
+SERVE_IMPLICIT = dict(restart=20, tol=1e-10, tol_mode="rel", max_iter=1000)
+
+
+def serve_plain_fp64(pkg, reqs, precond: str):
+    """The plain FP64 per-request path on the same arrival stream: one request at a time in
+    arrival order through the drop-in solvers (SolverEx / SolverIm in FP64, the implicit
+    ones with the served tolerance), each run as a whole.  Latency = completion - arrival."""
+    t0 = time.perf_counter()
+    arrive, lat, work = 0.0, [], 0.0
+    for gap, p, imp, run in reqs:
+        arrive += gap
+        now = time.perf_counter() - t0
+        if now < arrive:
+            time.sleep(arrive - now)
+        if imp:
+            s = pkg.SolverIm(p, precision="fp64", precond=precond, **SERVE_IMPLICIT)
+        else:
+            s = pkg.SolverEx(p, precision="fp64")
+        s.run(*run)
+        s.snapshot()
+        s.close()
+        lat.append(time.perf_counter() - t0 - arrive)
+        work += p.num_elem * max(0, run[1] - run[0])
+    wall = time.perf_counter() - t0
+    lat = np.array(lat) * 1e3
+    return {"value": work / wall, "unit": METRIC, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
+            "seconds": wall, "path": "one request at a time, FP64 drop-in solvers"}
+
+
+def run_serve(args, rank: int, world: int, dist, count: int = 0, plain: bool = True):
+    """The serving workload; returns its JSON line (rank 0) or None."""
     import torch
     pkg = importlib.import_module("168861_gb300")
-    local = int(os.environ.get("LOCAL_RANK", 0))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    count = args.trees or 64
+    count = count or args.trees or 64
     # each rank serves its own share of the arrival stream (one server per GPU)
     reqs = shard(serve_requests(count, args.seed), rank, world)
     ex = dict(precision="mixed")
-    im = dict(precision="mixed", restart=20, tol=1e-10, tol_mode="rel", precond=args.precond,
-              max_iter=1000)
+    im = dict(precision="mixed", precond=args.precond, **SERVE_IMPLICIT)
     # warm-up: one small request of each kind through a throwaway server
     w = pkg.Server(budget_bytes=8 << 30, explicit_opts=ex, implicit_opts=im)
-    for gap, p, imp, run in reqs[:2]:
+    for gap, p, imp, run in reqs[:4]:
         w.submit(p, imp, run[0], min(run[1], run[0] + 16), run[2], run[3])
     w.drain()
     w.close()
@@ -562,22 +605,30 @@ def run_serve(args, rank: int, world: int):
         dist.all_reduce(s_)
         wall, p50, p99, pmax = (float(x) for x in t)
         work, h2d, d2h = (float(x) for x in s_)
-        dist.destroy_process_group()
     if rank != 0:
-        return
+        return None
     line = {"metric": "serve compartment-steps/s", "value": work / wall,
-            "unit": "compartment-steps/s", "n_gpus": world, "steps": count, "warmup": 2,
+            "unit": "compartment-steps/s", "n_gpus": world, "steps": count, "warmup": 4,
             "ms_per_step": wall * 1e3 / count, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded requests)",
             "config": {"workload": "serve", "requests": count, "arrivals": "Poisson 2000/s",
-                       "mix": "50% explicit 1 cm axon (mixed), 50% implicit random tree 1e3-1e5 "
-                              "(mixed GMRES(20)+FP64 refinement)", "sim_time_ms": "U(10,100)"},
+                       "mix": "in turn: explicit 1 cm axon; implicit random tree 1e3-1e5; "
+                              "implicit random binary tree depth 6-9; explicit myelinated axon "
+                              "4-10 nodes (mixed precision; implicit GMRES(20) + FP64 "
+                              "refinement to 1e-10)",
+                       "sim_time": "U(10,100) ms (myelinated axons U(0.5,2) us)"},
             "p50_ms": p50, "p99_ms": p99, "max_ms": pmax,
             "batches": int(st.batches_created), "completed": int(st.completed),
             "clocks": clk.summary(),
             "e2e": {"value": work / wall, "unit": "compartment-steps/s",
                     "h2d_bytes_per_step": h2d / count, "d2h_bytes_per_step": d2h / count}}
-    print(json.dumps(line), flush=True)
+    if plain and world == 1:
+        try:
+            line["plain_fp64_per_request"] = serve_plain_fp64(pkg, reqs, args.precond)
+            line["speedup_vs_plain_fp64_per_request"] = line["value"] / line["plain_fp64_per_request"]["value"]
+        except Exception as exc:
+            line["plain_fp64_per_request"] = {"value": None, "error": repr(exc)[:300]}
+    return line
 
 
 # ------------------------------------------------------------------ CPU (reference) arm
@@ -676,16 +727,61 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def compact(line: dict) -> dict:
+    """The figures of a workload's line that a sub-result keeps."""
+    keep = ("value", "unit", "ms_per_step", "steps", "elements", "p50_ms", "p99_ms", "max_ms",
+            "completed", "plain_fp64_per_request", "speedup_vs_plain_fp64_per_request")
+    out = {k: line[k] for k in keep if k in line}
+    out["workload"] = line["config"]["workload"]
+    if line.get("roofline"):
+        r = line["roofline"]
+        out["roofline"] = {k: r[k] for k in ("achieved", "peak", "unit", "frac") if k in r}
+    if isinstance(line.get("e2e"), dict):
+        out["e2e"] = line["e2e"]["value"]
+    out["clocks"] = line.get("clocks")
+    return out
+
+
+SUB_WORKLOADS = ("batch-explicit-mixed", "axon-explicit-fp64", "myelin-explicit-mixed", "serve")
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus))
     if args.impl == "reference":
         run_reference(args, rank, world)
-    elif args.workload == "serve":
-        run_serve(args, rank, world)
+        return
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0))))
+    if args.workload == "serve":
+        line = run_serve(args, rank, world, dist)
     else:
-        run_ours(args, rank, world)
+        line = run_ours(args, rank, world, dist, args.workload)
+        subs = args.sub_results == "on" or (
+            args.sub_results == "auto" and args.workload == DEFAULT_WORKLOAD and world == 1
+            and not args.trees and not args.steps)
+        if subs:
+            # the other workloads the results quote, each measured as its own line would be
+            # (without a CPU leg), kept in compact form
+            sub = {}
+            for wl in SUB_WORKLOADS:
+                try:
+                    l2 = (run_serve(args, rank, world, dist) if wl == "serve"
+                          else run_ours(args, rank, world, dist, wl, extras=False))
+                    sub[wl] = compact(l2) if l2 else None
+                except Exception as exc:  # the headline line is still reported
+                    sub[wl] = {"error": repr(exc)[:300]}
+            if line is not None:
+                line["sub_results"] = sub
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
 
 
 if __name__ == "__main__":
