@@ -163,7 +163,7 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
   hp.cdt.resize(N); hp.gax.resize(N); hp.wdx.resize(N); hp.kdx.resize(N); hp.inp.resize(N);
   hp.V0.resize(N); hp.V1.resize(N);
   hp.c_m_dx.resize(N); hp.radx.resize(N); hp.Wfull.resize(N); hp.Kfull.resize(N);
-  hp.gate.assign(3 * N, 0.0);
+  hp.gate.resize(3 * N);  // zeroed per instance below, HH entries then set
   hp.inst.resize(count);
   hp.num_elem.resize(count);
   hp.hh_local.resize(hp.hh_off[count]);
@@ -223,6 +223,7 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
       hp.radx[o + j] = r_a * dx;
       hp.Wfull[o + j] = p.W[j];
       hp.Kfull[o + j] = p.K[j];
+      hp.gate[o + j] = hp.gate[N + o + j] = hp.gate[2 * N + o + j] = 0.0;
     }
     for (int32_t q = 0; q < p.num_term; q++) {
       const int32_t t = p.terminals[q];
@@ -432,7 +433,7 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   pv.step_threads = opt.step_threads;
   NRT_CUDA(cudaDeviceGetAttribute(&pv.sms, cudaDevAttrMultiProcessorCount, device));
   if (mixed) {
-    auto f32 = [&](const std::vector<double> &v) {
+    auto f32 = [&](const auto &v) {
       hostf.emplace_back(v.size());
       float *d = hostf.back().data();
       const double *src = v.data();
@@ -916,10 +917,14 @@ int nrt_batch_create(const nrt_problem *problems, int32_t count, const nrt_optio
     std::string why;
     int rc = check_options(&o, why);
     if (rc) return nrt::fail(rc, why);
-    for (int32_t i = 0; i < count; i++) {
-      rc = nrt::validate_problem(&problems[i], o.mode == NRT_IMPLICIT_BE, why);
-      if (rc) return nrt::fail(rc, "instance " + std::to_string(i) + ": " + why);
-    }
+    // every instance checked on the host's cores; the first failing one is reported
+    std::vector<int> vrc(count, NRT_OK);
+    std::vector<std::string> vwhy(count);
+    nrt::parallel_for(count, [&](int64_t i) {
+      vrc[i] = nrt::validate_problem(&problems[i], o.mode == NRT_IMPLICIT_BE, vwhy[i]);
+    });
+    for (int32_t i = 0; i < count; i++)
+      if (vrc[i]) return nrt::fail(vrc[i], "instance " + std::to_string(i) + ": " + vwhy[i]);
     std::unique_ptr<nrt_batch> b(new (std::nothrow) nrt_batch());
     if (!b) return nrt::fail(NRT_ENOMEM, "host allocation");
     rc = b->eng.init(problems, count, &o);

@@ -5,6 +5,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <memory>
+#include <utility>
 #include <string>
 #include <thread>
 #include <vector>
@@ -169,20 +171,43 @@ int cuda_fail(cudaError_t e, const char *what);
     if (_e != cudaSuccess) return ::nrt::cuda_fail(_e, #call); \
   } while (0)
 
+// An allocator whose construct() leaves trivially constructible elements uninitialised, so
+// that resize() does not zero-fill (on one thread) arrays that a parallel pass then writes
+// in full: the writers touch the pages first.
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = NoInitAlloc<U>;
+  };
+  NoInitAlloc() = default;
+  template <class U>
+  NoInitAlloc(const NoInitAlloc<U> &) {}
+  template <class U>
+  void construct(U *) noexcept {}
+  template <class U, class... A>
+  void construct(U *p, A &&...a) {
+    ::new ((void *)p) U(std::forward<A>(a)...);
+  }
+};
+// Element-indexed host arrays that are written in full after they are sized.
+template <class T>
+using hvec = std::vector<T, NoInitAlloc<T>>;
+
 // Host mirror of the packed trees: built from nrt_problem arrays.
 struct HostPack {
   int64_t ntot = 0;
   int32_t ninst = 0;
   std::vector<int64_t> off;         // element offset per instance (ninst + 1)
-  std::vector<Topo> topo;
-  std::vector<double> cdt, gax, wdx, kdx, inp, V0, V1;
-  std::vector<double> gate;         // [3][ntot]
+  hvec<Topo> topo;
+  hvec<double> cdt, gax, wdx, kdx, inp, V0, V1;
+  hvec<double> gate;                // [3][ntot]
   std::vector<double> hp;           // [HP_ROWS][hp_ld]
   bool hp_inst = false;             // one HH parameter column per instance
   std::vector<uint32_t> hp_cls;     // column per element when classes are used
   int64_t hp_ld = 0;
-  std::vector<double> c_m_dx, radx; // c_m dX and r_a dX per element (implicit assembly)
-  std::vector<double> Wfull, Kfull; // W, K per element as given
+  hvec<double> c_m_dx, radx;        // c_m dX and r_a dX per element (implicit assembly)
+  hvec<double> Wfull, Kfull;        // W, K per element as given
   std::vector<InstDev> inst;
   std::vector<int32_t> hh_local;    // per instance: HH element indices (local), concatenated
   std::vector<int64_t> hh_off;      // per instance offsets into hh_local (ninst + 1)

@@ -35,7 +35,7 @@ struct Engine {
   bool terminals_dirty = false;
   bool general_next = false;  // explicit: the next step runs in the general form
   cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};  // one per starting buffer parity
-  std::vector<std::vector<float>> hostf;  // staging for FP32 uploads
+  std::vector<hvec<float>> hostf;  // staging for FP32 uploads
   ImplicitState *im = nullptr;
   RecState *rec = nullptr;                // recording at probes, or null
   StrainState *strain = nullptr;          // time-varying strain of some elements, or null
