@@ -483,6 +483,14 @@ def run_ours(args, rank: int, world: int, dist, wl: str, extras: bool = True, st
                 line["cpu_baseline"] = cpu_baseline(wl, args.seed, count)
             except Exception as exc:  # the GPU line is still reported
                 line["cpu_baseline"] = {"value": None, "error": repr(exc)[:300]}
+            if implicit:
+                # the same CPU with the exact tree solve instead of the reference's
+                # unpreconditioned GMRES: splits the GPU's lead into algorithm and hardware
+                try:
+                    line["cpu_tree_solve"] = cpu_baseline(wl, args.seed, count, linsolve=0)
+                    line["speedup_vs_cpu_tree_solve"] = value / line["cpu_tree_solve"]["value"]
+                except Exception as exc:
+                    line["cpu_tree_solve"] = {"value": None, "error": repr(exc)[:300]}
     return line if rank == 0 else None
 
 
@@ -634,8 +642,9 @@ def run_serve(args, rank: int, world: int, dist, count: int = 0, plain: bool = T
 # ------------------------------------------------------------------ CPU (reference) arm
 
 def _oracle_job(job):
-    """One oracle run in a worker process (spawned; no CUDA here)."""
-    wl, tseed, size, steps = job
+    """One oracle run in a worker process (spawned; no CUDA here).  Implicit: linsolve 2 is
+    the reference's method (unpreconditioned GMRES(150) to 1e-14), 0 the exact tree solve."""
+    wl, tseed, size, steps, linsolve = job
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     model = importlib.import_module("168861_gb300.model")
@@ -649,21 +658,27 @@ def _oracle_job(job):
     d = orc.derive(spec)
     t0 = time.perf_counter()
     if wl.startswith("batch-implicit"):
-        orc.implicit_run(spec, d, spec.dt_abs, 1, 1 + steps, linsolve=2)
+        orc.implicit_run(spec, d, spec.dt_abs, 1, 1 + steps, linsolve=linsolve)
     else:
         dT = O.spec_dT(spec, d.dT_crit) if wl == "axon-explicit-fp64" else 0.8 * d.dT_crit
         orc.explicit_run(spec, d, dT, 1, 1 + steps)
     return spec.n * steps, time.perf_counter() - t0
 
 
-def _sample_jobs(wl: str, seed: int, count: int, cores: int):
+def _sample_jobs(wl: str, seed: int, count: int, cores: int, linsolve: int = 2):
     """About 10-20 s of CPU work spread over `cores` processes."""
     if wl == "axon-explicit-fp64":
-        return [(wl, 0, 1002, 12000)] * cores, "1002-element axon, 12000 steps per process"
+        return [(wl, 0, 1002, 12000, 2)] * cores, "1002-element axon, 12000 steps per process"
     if wl == "myelin-explicit-mixed":
-        return ([(wl, 0, 0, 200000)] * cores,
+        return ([(wl, 0, 0, 200000, 2)] * cores,
                 "20-node myelinated axon (~2e4 elements, no strain ramp), 2e5 steps per process")
     pop = tree_population(count, seed)
+    if wl.startswith("batch-implicit") and linsolve == 0:
+        # the exact tree (Hines) solve: the first trees of the population, as drawn
+        pick = pop[: 2 * cores]
+        jobs = [(wl, s, n, 200, 0) for s, n in pick]
+        return jobs, (f"first {len(jobs)} trees of the workload, 200 steps each, exact tree "
+                      "(Hines) solve in FP64")
     if wl.startswith("batch-implicit"):
         # unpreconditioned GMRES(150) to 1e-14 (the reference's solve) on the smallest trees,
         # which converge fastest per compartment: a conservative (CPU-favouring) sample
@@ -674,7 +689,7 @@ def _sample_jobs(wl: str, seed: int, count: int, cores: int):
         per = 600
         pick = pop[: 2 * cores]
         what = "first"
-    jobs = [(wl, s, n, per) for s, n in pick]
+    jobs = [(wl, s, n, per, 2) for s, n in pick]
     return jobs, f"{what} {len(jobs)} trees of the workload, {per} steps each"
 
 
@@ -686,13 +701,14 @@ def _warm(_):
     return os.getpid()
 
 
-def cpu_baseline(wl: str, seed: int, count: int):
-    """The oracle port timed on the host cores (one process per core, spawned, warmed)."""
+def cpu_baseline(wl: str, seed: int, count: int, linsolve: int = 2):
+    """The oracle port timed on the host cores (one process per core, spawned, warmed).
+    Implicit workloads: linsolve 2 runs the reference's method, 0 the exact tree solve."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
     cores = os.cpu_count() or 1
-    jobs, sample = _sample_jobs(wl, seed, count, cores)
+    jobs, sample = _sample_jobs(wl, seed, count, cores, linsolve)
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
         pool.map(_warm, range(cores))
