@@ -13,9 +13,11 @@ trees (the first ones, up to `sample_elements` compartments) in a batch of its o
 caller's state is never touched. It keeps the fastest. Results are cached in a JSON file
 per device, mode, precision and workload size, so a workload is tuned once per machine.
 
-The implicit kernel's shape is fixed by its register budget (256 threads, 4 CTAs per SM).
-Its tunable is the GMRES restart length, which changes the iteration count but leaves the
-answer within the solve tolerance. It is searched only when `restarts` is given.
+The implicit block-per-instance kernel (batches) has one shape-only knob: how many of its
+persistent CTAs run per SM (`tile_ctas_per_sm`, 1 .. 4; its register budget allows 4). Each
+instance is one CTA's from start to end, so the trees come out bit for bit the same. Its other
+tunable, the GMRES restart length, changes the iteration count but leaves the answer within
+the solve tolerance; it is searched (with every CTA count) only when `restarts` is given.
 """
 from __future__ import annotations
 
@@ -37,9 +39,10 @@ def candidates(mode: int, precision: str, restarts=None) -> list[dict]:
             return ([{"tiled": True, "tile_ctas_per_sm": c} for c in (1, 2, 3, 4)] +
                     [{"tiled": False, "step_threads": t} for t in (64, 128, 256)])
         return [{"step_threads": t} for t in (32, 64, 128, 256)]
+    shapes = [{"tile_ctas_per_sm": c} for c in (2, 3, 4)]
     if restarts:
-        return [{"restart": int(r)} for r in restarts]
-    return [{}]
+        return [{"restart": int(r), **s} for r in restarts for s in shapes]
+    return shapes
 
 
 def choose(times: list[float]) -> int:

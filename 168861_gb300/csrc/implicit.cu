@@ -2102,6 +2102,9 @@ int Engine::implicit_plan(size_t &bytes) {
     auto kern = mixed ? implicit_steps<float, false> : implicit_steps<double, false>;
     NRT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
     NRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, S.smem));
+    // persistent CTAs: as many per SM as fit, or at most tile_ctas_per_sm (a tuned shape;
+    // each instance is one CTA's from start to end, so results do not depend on it)
+    if (opt.tile_ctas_per_sm > 0) per_sm = std::min(per_sm, opt.tile_ctas_per_sm);
     S.grid_blocks = std::max(1, std::min<int>(dev_sms * std::max(per_sm, 1), ni));
     S.inst_tile.assign(ni + 1, 0);
     for (int32_t i = 0; i < ni; i++) {

@@ -70,7 +70,7 @@ def parse():
                     help="also measure the other workloads and attach them in compact form "
                          "(auto: with the default workload on one GPU)")
     ap.add_argument("--autotune", action="store_true",
-                    help="explicit workloads: run on the launch shape the autotuner picks "
+                    help="run on the launch shape the autotuner picks "
                          "(tuned before the timed regions; default: the automatic shapes)")
     return ap.parse_args()
 
@@ -330,9 +330,11 @@ def plain_fp64_single(pkg, torch):
 
 # ------------------------------------------------------------------ our arm
 
-def run_ours(args, rank: int, world: int, dist, wl: str, extras: bool = True, steps: int = 0):
+def run_ours(args, rank: int, world: int, dist, wl: str, extras: bool = True, steps: int = 0,
+             autotune: bool | None = None):
     """One workload on our arm; returns its JSON line (rank 0) or None.  extras: the plain
-    FP64 comparison (implicit) and the CPU baseline leg."""
+    FP64 comparison (implicit) and the CPU baseline leg.  autotune: run on the shape the
+    autotuner picks (default: --autotune)."""
     import torch
     pkg = importlib.import_module("168861_gb300")
     local = int(os.environ.get("LOCAL_RANK", 0))
@@ -366,10 +368,13 @@ def run_ours(args, rank: int, world: int, dist, wl: str, extras: bool = True, st
                     max_iter=1000)
     mode = pkg._lib.NRT_IMPLICIT_BE if implicit else pkg._lib.NRT_EXPLICIT
     launch_shape = "automatic"
-    if args.autotune and not implicit:  # outside every timed region
-        tuned = importlib.import_module(pkg.__name__ + ".autotune").tune(probs, mode, precision)
+    if (args.autotune if autotune is None else autotune):  # outside every timed region
+        rest = {k: v for k, v in opts.items() if k != "precision"}
+        tuned = importlib.import_module(pkg.__name__ + ".autotune").tune(probs, mode, precision,
+                                                                         **rest)
         opts.update(tuned["options"])
-        launch_shape = tuned["options"]
+        launch_shape = {"tuned": tuned["options"], "candidates": tuned["candidates"],
+                        "seconds_per_step": tuned["times"]}
     # loop ranges long enough for warm-up + timed steps
     runs = [(a, max(b, a + W + K + 1), c, d_) for a, b, c, d_ in runs]
 
@@ -758,7 +763,8 @@ def compact(line: dict) -> dict:
     return out
 
 
-SUB_WORKLOADS = ("batch-explicit-mixed", "axon-explicit-fp64", "myelin-explicit-mixed", "serve")
+SUB_WORKLOADS = ("batch-implicit-mixed-tuned", "batch-explicit-mixed", "axon-explicit-fp64",
+                 "myelin-explicit-mixed", "serve")
 
 
 def main():
@@ -787,9 +793,16 @@ def main():
             sub = {}
             for wl in SUB_WORKLOADS:
                 try:
-                    l2 = (run_serve(args, rank, world, dist) if wl == "serve"
-                          else run_ours(args, rank, world, dist, wl, extras=False))
+                    if wl == "serve":
+                        l2 = run_serve(args, rank, world, dist)
+                    elif wl.endswith("-tuned"):  # the headline on the autotuner's launch shape
+                        l2 = run_ours(args, rank, world, dist, wl[: -len("-tuned")],
+                                      extras=False, autotune=True)
+                    else:
+                        l2 = run_ours(args, rank, world, dist, wl, extras=False)
                     sub[wl] = compact(l2) if l2 else None
+                    if l2 and isinstance(l2["config"].get("launch_shape"), dict):
+                        sub[wl]["launch_shape"] = l2["config"]["launch_shape"]
                 except Exception as exc:  # the headline line is still reported
                     sub[wl] = {"error": repr(exc)[:300]}
             if line is not None:

@@ -125,8 +125,9 @@ typedef struct nrt_options {
                                     thread per element loading its own (same results) */
   int32_t scheme;                /* implicit: NRT_BACKWARD_EULER (default, the reference's)
                                     or NRT_CRANK_NICOLSON */
-  int32_t tile_ctas_per_sm;      /* mixed explicit, tiled: persistent CTAs per SM, 1 .. as many
-                                    as fit (0 = as many as fit, the default) */
+  int32_t tile_ctas_per_sm;      /* persistent CTAs per SM, 1 .. as many as fit (0 = as many
+                                    as fit, the default): of the mixed explicit tiled step,
+                                    and of the implicit block-per-instance kernel (batches) */
   int32_t step_threads;          /* explicit, one thread per element: threads per block, a
                                     multiple of 32 up to 256 (0 = chosen from the tree size).
                                     Launch shapes only: results do not depend on them */

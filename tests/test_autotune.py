@@ -19,8 +19,9 @@ def test_candidates():
     assert {c["tile_ctas_per_sm"] for c in mixed if c["tiled"]} == {1, 2, 3, 4}
     assert {c["step_threads"] for c in mixed if not c["tiled"]} == {64, 128, 256}
     assert [c["step_threads"] for c in at.candidates(lib.NRT_EXPLICIT, "fp64")] == [32, 64, 128, 256]
-    assert at.candidates(lib.NRT_IMPLICIT_BE, "mixed") == [{}]
-    assert at.candidates(lib.NRT_IMPLICIT_BE, "mixed", [16, 20]) == [{"restart": 16}, {"restart": 20}]
+    assert at.candidates(lib.NRT_IMPLICIT_BE, "mixed") == [{"tile_ctas_per_sm": c} for c in (2, 3, 4)]
+    both = at.candidates(lib.NRT_IMPLICIT_BE, "mixed", [16, 20])
+    assert both == [{"restart": r, "tile_ctas_per_sm": c} for r in (16, 20) for c in (2, 3, 4)]
 
 
 def test_choose():
@@ -83,9 +84,14 @@ def test_tune_ignores_a_stale_cache_entry(tmp_path):
     assert r["options"] == {"step_threads": 256} and r["times"] is not None
 
 
-def test_nothing_to_tune_needs_no_timer(tmp_path):
-    def timer(*a):
-        raise AssertionError("no candidate to time")
-    r = at.tune([Tree(1000)], lib.NRT_IMPLICIT_BE, "mixed", cache=str(tmp_path / "c.json"),
-                timer=timer, device_key="dev")
-    assert r["options"] == {}
+def test_implicit_tunes_its_cta_count(tmp_path):
+    """The implicit batch kernel's shape: CTAs per SM, the fastest by the timer; the restart
+    length joins the search only when asked for."""
+    r = at.tune([Tree(1000)] * 4, lib.NRT_IMPLICIT_BE, "mixed", cache=str(tmp_path / "c.json"),
+                timer=lambda ps, m, p, ov: abs(ov["tile_ctas_per_sm"] - 3) + 1.0,
+                device_key="dev")
+    assert r["options"] == {"tile_ctas_per_sm": 3} and len(r["times"]) == 3
+    r = at.tune([Tree(1000)] * 4, lib.NRT_IMPLICIT_BE, "mixed", cache=str(tmp_path / "d.json"),
+                timer=lambda ps, m, p, ov: ov["restart"] + ov["tile_ctas_per_sm"] / 10,
+                device_key="dev", restarts=[16, 20])
+    assert r["options"] == {"restart": 16, "tile_ctas_per_sm": 2}
