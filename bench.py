@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--workload", choices=WORKLOADS, default=DEFAULT_WORKLOAD)
     ap.add_argument("--trees", type=int, default=0, help="override the tree count (probes only)")
+    ap.add_argument("--uniform-size", type=int, default=0,
+                    help="every tree of about this many elements instead of the log-uniform "
+                         "sizes (probes only: a population whose CTAs finish together)")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the CPU baseline leg (profiling runs)")
@@ -77,9 +80,14 @@ def parse():
 
 # ------------------------------------------------------------------ workloads
 
+UNIFORM_SIZE = 0  # --uniform-size (probes only)
+
+
 def tree_population(count: int, seed: int):
     model = importlib.import_module("168861_gb300.model")
     sizes = model.log_uniform_sizes(count, 1e3, 1e5, seed)
+    if UNIFORM_SIZE:
+        sizes = [UNIFORM_SIZE] * count
     return [(seed * 7919 + i, int(sizes[i])) for i in range(count)]
 
 
@@ -768,7 +776,9 @@ SUB_WORKLOADS = ("batch-implicit-mixed-tuned", "batch-explicit-mixed", "axon-exp
 
 
 def main():
+    global UNIFORM_SIZE
     args = parse()
+    UNIFORM_SIZE = args.uniform_size
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus))
     if args.impl == "reference":
@@ -786,7 +796,7 @@ def main():
         line = run_ours(args, rank, world, dist, args.workload)
         subs = args.sub_results == "on" or (
             args.sub_results == "auto" and args.workload == DEFAULT_WORKLOAD and world == 1
-            and not args.trees and not args.steps)
+            and not args.trees and not args.steps and not args.uniform_size)
         if subs:
             # the other workloads the results quote, each measured as its own line would be
             # (without a CPU leg), kept in compact form
