@@ -41,11 +41,12 @@ sys.path.insert(0, ROOT)
 METRIC = "compartment-steps/s"
 
 # DRAM bytes (read + write) per compartment-step of the dominant kernel, from ncu captures
-# of a 1024-tree case (21.9M elements, above L2; profiles/ gives the commands): the
-# explicit step moved 1391.1 MB per launch, the implicit launch 28.63 GB over 3 steps.
-# The traffic of a full-size step is scaled from these by the compartments it processes.
-TRAFFIC_PER_ELEMENT_STEP = {"batch-explicit-mixed": 1391.1e6 / 21910344,
-                            "batch-implicit-mixed": 28.63e9 / (3 * 21910344)}
+# above L2 (profiles/ gives the commands): the explicit step on 1024 trees (21.9M elements)
+# moved 1.394 GB per launch; the implicit launch on 256 trees of 20k elements (5.12M)
+# moved 5.418 GB over 3 steps.  The traffic of a full-size step is scaled from these by the
+# compartments it processes.
+TRAFFIC_PER_ELEMENT_STEP = {"batch-explicit-mixed": 1.394e9 / 21910344,
+                            "batch-implicit-mixed": 5.418e9 / (3 * 5120180)}
 WORKLOADS = ("batch-implicit-mixed", "batch-explicit-mixed", "batch-explicit-fp64",
              "axon-explicit-fp64", "myelin-explicit-mixed", "serve")
 DEFAULT_WORKLOAD = "batch-implicit-mixed"
@@ -453,7 +454,8 @@ def run_ours(args, rank: int, world: int, dist, wl: str, extras: bool = True, st
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
             "algorithmic_bytes_per_step": alg_all,
-            "traffic_note": "DRAM bytes per step, ncu on 1024 trees scaled by compartments"
+            "traffic_note": "DRAM bytes per step from an ncu capture above L2 (1024 trees "
+                            "explicit, 256 trees of 20k elements implicit), scaled by compartments"
                             if per_el else None}
     roof_passes = None
     if passes is not None:
