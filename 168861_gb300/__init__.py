@@ -7,5 +7,5 @@ importlib.import_module("168861_gb300") (the directory name starts with a digit)
 from . import model  # noqa: F401  (tree descriptions in the reference numbering)
 from ._lib import LIB_PATH, NeuriteError, load  # noqa: F401
 from .solver import (Batch, Derived, ProblemArrays, Recording, Server, SolverEx,  # noqa: F401
-                     SolverIm, State, derive, derive_batch, measurement_point, simulate,
-                     step_size)
+                     SolverIm, State, derive, derive_batch, kernel_launches, measurement_point,
+                     simulate, step_size)

@@ -44,7 +44,8 @@ class Options(ctypes.Structure):
         ("use_graphs", ctypes.c_int32), ("schedule", ctypes.c_int32),
         ("tiled", ctypes.c_int32), ("scheme", ctypes.c_int32),
         ("tile_ctas_per_sm", ctypes.c_int32), ("step_threads", ctypes.c_int32),
-        ("inner_tol", ctypes.c_double),
+        ("inner_tol", ctypes.c_double), ("step_launch", ctypes.c_int32),
+        ("refinement", ctypes.c_int32),
     ]
 
 
@@ -103,7 +104,7 @@ EXPORTS = (
     "nrt_batch_record_read", "nrt_batch_pass_counts", "nrt_get_state", "nrt_set_state",
     "nrt_batch_get_state", "nrt_batch_set_state", "nrt_batch_snapshot_all",
     "nrt_server_submit_recorded", "nrt_server_recording", "nrt_derive_batch",
-    "nrt_set_strain", "nrt_batch_set_strain",
+    "nrt_set_strain", "nrt_batch_set_strain", "nrt_kernel_launches",
 )
 
 _lib = None
@@ -165,7 +166,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "nrt_server_destroy": [vp],
         "nrt_measurement_point": [ctypes.c_int32, _f64p, ctypes.c_double,
                                   ctypes.POINTER(ctypes.c_int32)],
-        "nrt_batch_pass_counts": [vp, _i64p, _i64p, _i64p, _i64p],
+        "nrt_batch_pass_counts": [vp, _i64p, _i64p, _i64p, _i64p, _i64p],
         "nrt_get_state": [vp, _f64p, _f64p, _f64p, _f64p, _f64p],
         "nrt_set_state": [vp, _f64p, _f64p, _f64p, _f64p, _f64p],
         "nrt_batch_get_state": [vp, ctypes.c_int32, _f64p, _f64p, _f64p, _f64p, _f64p],
@@ -188,6 +189,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.nrt_status_string.restype = ctypes.c_char_p
     lib.nrt_last_error.argtypes = []
     lib.nrt_last_error.restype = ctypes.c_char_p
+    lib.nrt_kernel_launches.argtypes = []
+    lib.nrt_kernel_launches.restype = ctypes.c_int64
     _lib = lib
     return lib
 

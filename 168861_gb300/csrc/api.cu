@@ -14,12 +14,17 @@
 
 #include "nrt_internal.h"
 #include "nrt_solver.h"
+#include "strain.cuh"
 
 namespace nrt {
 
 namespace {
 thread_local std::string g_last_error;
+std::atomic<long long> g_launches{0};  // kernels launched by this library (all threads)
 }
+
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launches_total() { return g_launches.load(std::memory_order_relaxed); }
 
 void set_error(const std::string &msg) { g_last_error = msg; }
 
@@ -424,10 +429,12 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   }
   pv.topo = topo;
   pv.inst = inst;
+  // [0] the device error word; [4..7] the explicit chunk kernel's barrier words
   int *err = nullptr;
-  TRY(upload(arena, err, (const int *)nullptr, 4, st));
-  NRT_CUDA(cudaMemsetAsync(err, 0, 16, st));
+  TRY(upload(arena, err, (const int *)nullptr, 8, st));
+  NRT_CUDA(cudaMemsetAsync(err, 0, 32, st));
   pv.err = err;
+  gbar = (GridBar *)(err + 4);
   pv.tile_blocks = (mixed && opt.mode == NRT_EXPLICIT && opt.tiled != 0)
                        ? explicit_tile_blocks(device, N, opt.tile_ctas_per_sm) : 0;
   pv.step_threads = opt.step_threads;
@@ -601,8 +608,16 @@ int Engine::fixup() {
   return NRT_OK;
 }
 
+// The explicit time loop runs a chunk of steps per cooperative launch (nrt_options.
+// step_launch), in the fused form, with the strain (if any) derived ahead per chunk.
+bool Engine::chunk_kernel() const {
+  if (opt.mode != NRT_EXPLICIT || !host.fusable || !gbar || opt.step_launch != 1) return false;
+  return !strain || strain_tabled(*this);
+}
+
 // Runs `steps` loop iterations from every instance's current base (device-side loop
-// indices), replaying a captured graph of kChunk steps where possible.
+// indices): chunks of up to kChunk steps per launch when asked for, otherwise a captured
+// graph of kChunk steps where possible.
 int Engine::advance(int64_t steps) {
   if (opt.mode == NRT_IMPLICIT_BE) return implicit_advance(*this, steps);
   int64_t left = steps;
@@ -612,6 +627,24 @@ int Engine::advance(int64_t steps) {
     if (rec) TRY(launch_record_step(rec_view_host(), pv.inst, 0, V[cur], stream));
     TRY(launch_advance_base(pv.inst, pv.ninst, 1, stream));
     left--;
+  }
+  if (left > 0 && chunk_kernel()) {
+    const RecView none_r{};
+    const StrainView none_s{};
+    const StrainView *sv = strain_view(*this);
+    while (left > 0) {
+      const int nk = (int)std::min<int64_t>(left, kChunk);
+      if (sv) TRY(launch_strain_derive(*this, nk, stream));
+      TRY(launch_explicit_chunk(pv, opt.precision, nk, V[cur], V[cur ^ 1], Vf[cur], Vf[cur ^ 1],
+                                rec ? rec_view_host() : none_r, sv ? *sv : none_s, gbar,
+                                opt.tile_ctas_per_sm, stream));
+      TRY(launch_advance_base(pv.inst, pv.ninst, nk, stream));
+      cur ^= nk & 1;
+      steps_done += nk;
+      left -= nk;
+      terminals_dirty = true;
+    }
+    return NRT_OK;
   }
   const bool graphs = opt.use_graphs != 0 && opt.mode == NRT_EXPLICIT && host.fusable;
   if (graphs && left >= kChunk) {
@@ -635,12 +668,15 @@ int Engine::advance(int64_t steps) {
       cudaError_t e = cudaStreamEndCapture(stream, &g);
       if (rc != NRT_OK) return rc;
       NRT_CUDA(e);
+      size_t nodes = 0;  // every node of the captured chunk is a kernel of this library
+      if (cudaGraphGetNodes(g, nullptr, &nodes) == cudaSuccess) graph_nodes[cur] = (int64_t)nodes;
       e = cudaGraphInstantiate(&graph_exec[cur], g, 0);
       cudaGraphDestroy(g);
       NRT_CUDA(e);
     }
     while (left >= kChunk) {
       NRT_CUDA(cudaGraphLaunch(graph_exec[cur], stream));
+      count_launches(graph_nodes[cur]);
       steps_done += kChunk;  // kChunk is even: cur is unchanged
       left -= kChunk;
       terminals_dirty = true;
@@ -690,6 +726,8 @@ const char *nrt_status_string(int s) {
 
 const char *nrt_last_error(void) { return nrt::g_last_error.c_str(); }
 
+int64_t nrt_kernel_launches(void) { return (int64_t)nrt::launches_total(); }
+
 int nrt_options_default(nrt_options *o) {
   return nrt::guarded([&]() -> int {
     if (!o) return NRT_EINVAL;
@@ -720,12 +758,14 @@ static int check_options(const nrt_options *o, std::string &why) {
   if (!(o->tol > 0)) return (why = "tol must be > 0", NRT_EINVAL);
   if (o->max_iter < 0) return (why = "max_iter must be >= 0", NRT_EINVAL);
   if (!(o->inner_tol >= 0 && o->inner_tol < 1)) return (why = "inner_tol must be in [0, 1)", NRT_EINVAL);
+  if (o->refinement != 0 && o->refinement != 1) return (why = "refinement must be 0 or 1", NRT_EINVAL);
   if (o->scheme != NRT_BACKWARD_EULER && o->scheme != NRT_CRANK_NICOLSON)
     return (why = "bad scheme", NRT_EINVAL);
   if (o->tile_ctas_per_sm < 0 || o->tile_ctas_per_sm > 64)
     return (why = "tile_ctas_per_sm must be in [0, 64]", NRT_EINVAL);
   if (o->step_threads != 0 && (o->step_threads < 32 || o->step_threads > 256 || o->step_threads % 32))
     return (why = "step_threads must be 0 or a multiple of 32 in [32, 256]", NRT_EINVAL);
+  if (o->step_launch != 0 && o->step_launch != 1) return (why = "step_launch must be 0 or 1", NRT_EINVAL);
   return NRT_OK;
 }
 
@@ -1034,11 +1074,12 @@ int nrt_batch_instance_stats(nrt_batch *b, int64_t *iters, int32_t *last_iters,
 }
 
 int nrt_batch_pass_counts(nrt_batch *b, int64_t *residuals, int64_t *precond_applies,
-                          int64_t *xupdates, int64_t *basis_reads) {
+                          int64_t *xupdates, int64_t *basis_reads, int64_t *richardson_steps) {
   return nrt::guarded([&]() -> int {
     if (!b) return nrt::fail(NRT_EINVAL, "null batch");
     NRT_CUDA(cudaSetDevice(b->eng.device));
-    return nrt::pass_counts(b->eng, residuals, precond_applies, xupdates, basis_reads);
+    return nrt::pass_counts(b->eng, residuals, precond_applies, xupdates, basis_reads,
+                            richardson_steps);
   });
 }
 

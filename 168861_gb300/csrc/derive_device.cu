@@ -15,6 +15,7 @@
 
 #include "derive_elem.h"
 #include "nrt_internal.h"
+#include "pdl.cuh"
 
 namespace nrt {
 
@@ -181,6 +182,7 @@ extern "C" int nrt_derive_batch(int32_t count, const int64_t *offsets, const int
     NRT_CUDA(cudaMemcpyAsync(d_em, e_max, 8 * (size_t)count, cudaMemcpyHostToDevice, st));
     DeriveArgs a{d_off, d_hoff, d_kind, d_ds, d_my, d_em, d_ep, d_hh, d_hp, d_dt, T, H};
     derive_trees<<<count, kDThreads, 0, st>>>(a);
+    count_launch_on(st);
     NRT_CUDA(cudaGetLastError());
     NRT_CUDA(cudaMemcpyAsync(eparam, d_ep, 8 * 6 * (size_t)T, cudaMemcpyDeviceToHost, st));
     if (H > 0) {

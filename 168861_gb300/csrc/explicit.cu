@@ -30,6 +30,8 @@
 #include "hh.cuh"
 #include "nrt_internal.h"
 #include "pdl.cuh"
+#include "record.cuh"
+#include "strain.cuh"
 #include "tma.cuh"
 
 namespace nrt {
@@ -46,14 +48,10 @@ __device__ __forceinline__ int64_t ghost_source(const Topo &t, int64_t j) {
   return (t.flags & F_ROOT) ? j + 1 : (int64_t)t.mother;
 }
 
+// Element j of step k in FP64 (the body of explicit_step_f64 and of the chunk kernel).
 template <bool kGeneral>
-__global__ void __launch_bounds__(256) explicit_step_f64(PackView p, int k, int force,
-                                                         const double *__restrict__ Vin,
-                                                         double *__restrict__ Vout) {
-  chain_acquire();  // the previous launch of the time loop has finished
-  chain_release();
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= p.ntot) return;
+__device__ __forceinline__ void f64_element(const PackView &p, int k, int force, int64_t j,
+                                            const double *Vin, double *Vout) {
   const Topo tj = p.topo[j];
   const InstDev in = p.inst[tj.flags >> INST_SHIFT];
   const int64_t i = in.base + k;
@@ -100,22 +98,28 @@ __global__ void __launch_bounds__(256) explicit_step_f64(PackView p, int k, int 
   Vout[j] = v + p.cdt[j] * acc;
 }
 
-// Mixed precision: gates, rates, conductances and currents in FP32; the potential is
+template <bool kGeneral>
+__global__ void __launch_bounds__(256) explicit_step_f64(PackView p, int k, int force,
+                                                         const double *__restrict__ Vin,
+                                                         double *__restrict__ Vout) {
+  chain_acquire();  // the previous launch of the time loop has finished
+  chain_release();
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.ntot) return;
+  f64_element<kGeneral>(p, k, force, j, Vin, Vout);
+}
+
+// Mixed precision (element j of step k; the body of explicit_step_mixed and of the chunk
+// kernel): gates, rates, conductances and currents in FP32; the potential is
 // accumulated in FP64.  GB300's FP64 pipe runs at 1/61 of the FP32 rate, so the stencil
 // reads an FP32 shadow of V (Vf = (float)V, refreshed from the FP64 value every step):
 // neighbour differences carry an absolute error of ~4e-9 V, while the FP64 accumulator
 // V' = V + dt-scaled current keeps long horizons free of drift.  FP64-pipe work is one
 // conversion, one add and one conversion back per element.
 template <bool kGeneral>
-__global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, int force,
-                                                           const double *__restrict__ Vin,
-                                                           double *__restrict__ Vout,
-                                                           const float *__restrict__ Fin,
-                                                           float *__restrict__ Fout) {
-  chain_acquire();  // the previous launch of the time loop has finished
-  chain_release();
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= p.ntot) return;
+__device__ __forceinline__ void mixed_element(const PackView &p, int k, int force, int64_t j,
+                                              const double *Vin, double *Vout, const float *Fin,
+                                              float *Fout) {
   const int64_t N = p.ntot;
   // Loads that do not depend on the topology record go out together with it: the
   // element's own state and its neighbours j-1 and j+1 (the mother and DR of nearly
@@ -199,6 +203,19 @@ __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, in
   const double vn = v64 + (double)(cdt * acc);
   Vout[j] = vn;
   Fout[j] = (float)vn;
+}
+
+template <bool kGeneral>
+__global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, int force,
+                                                           const double *__restrict__ Vin,
+                                                           double *__restrict__ Vout,
+                                                           const float *__restrict__ Fin,
+                                                           float *__restrict__ Fout) {
+  chain_acquire();  // the previous launch of the time loop has finished
+  chain_release();
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.ntot) return;
+  mixed_element<kGeneral>(p, k, force, j, Vin, Vout, Fin, Fout);
 }
 
 // ---- the mixed step with TMA-staged tiles
@@ -449,6 +466,106 @@ __global__ void __launch_bounds__(kTileThreads) explicit_step_mixed_tiled(
   }
 }
 
+// ---- a chunk of steps per launch (nrt_options.step_launch = 1)
+//
+// A step of a small pack (one axon; a myelinated fibre whose arrays sit in L2) is short, so
+// the time loop pays a launch per step.  This kernel runs nk steps in one cooperative launch
+// (every CTA resident) with a grid barrier after each step.  On a GB300 it is not the
+// default: with the loop's launches chained and replayed from a graph, a launch boundary
+// costs about what a grid barrier across both dies costs (1002-element FP64 axon 7.42 vs
+// 8.17 us per step; the 199k-element myelinated axon 4.63 vs 5.14-5.48 us, 7.14 vs 9.78 us
+// with its strain ramp, which needs a second barrier per step).  Every thread owns the same elements at every step (a stride over the grid),
+// so an element's gates stay with one thread.  After the barrier that ends step k:
+//  - the probes read step k's potentials (step k + 1 writes the other buffer, and step
+//    k + 2, which overwrites it, starts after the next barrier);
+//  - with a strain ramp, the strained elements take step k + 1's row of the chunk table,
+//    behind a second barrier, since a step reads its neighbours' conductances.
+// The arithmetic is the per-step kernels' element bodies, so results are theirs bit for bit.
+// Data that this kernel writes (V, its FP32 shadow, the strained coefficients) is read with
+// ordinary loads after the barrier, whose GPU-scope fences order them after the writes.
+
+// Grid barrier over a cooperative launch.  Arrivals are counted on a 64-bit word that is 0
+// when the launch starts; the b-th barrier completes when it reaches b * gridDim.x.  Thread
+// 0 of each CTA arrives after a GPU-scope fence (the CTA's writes, gathered by the CTA
+// barrier, become visible first) and polls.  It gives up after about two seconds of clock
+// (every CTA is resident, so that means a device fault) and raises the error word.
+__device__ __forceinline__ bool grid_barrier(GridBar *g, unsigned long long &target, int *err) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    target += gridDim.x;
+    __threadfence();
+    atomicAdd(&g->count, 1ull);
+    int ok = 1;
+    const volatile unsigned long long *c = &g->count;
+    if (*c < target) {
+      const long long t0 = clock64();
+      while (*c < target) {
+        if (clock64() - t0 > 4000000000ll) {
+          atomicOr(err, 1);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// The last CTA to leave puts the barrier's words back to 0 for the next launch (no CTA polls
+// them any more once every CTA has counted itself out).
+__device__ __forceinline__ void grid_barrier_exit(GridBar *g) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&g->exits, 1u) == gridDim.x - 1) {
+      atomicExch(&g->count, 0ull);
+      atomicExch(&g->exits, 0u);
+    }
+  }
+}
+
+template <bool kMixed, int kThreads>
+__global__ void __launch_bounds__(kThreads) explicit_steps_chunk(PackView p, int nk, double *V0,
+                                                                 double *V1, float *F0, float *F1,
+                                                                 RecView r, StrainView s,
+                                                                 GridBar *gb) {
+  chain_acquire();  // the previous launch of the time loop has finished
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  unsigned long long target = 0;
+  bool ok = true;
+  if (s.n > 0) {
+    for (int64_t q = tid; q < s.n; q += nth) apply_row(s, p, (int)q, 0, kMixed);
+    ok = grid_barrier(gb, target, p.err);
+  }
+  for (int k = 0; k < nk && ok; k++) {
+    const double *Vin = (k & 1) ? V1 : V0;
+    double *Vout = (k & 1) ? V0 : V1;
+    for (int64_t j = tid; j < p.ntot; j += nth) {
+      if (kMixed)
+        mixed_element<false>(p, k, -1, j, Vin, Vout, (k & 1) ? F1 : F0, (k & 1) ? F0 : F1);
+      else
+        f64_element<false>(p, k, -1, j, Vin, Vout);
+    }
+    ok = grid_barrier(gb, target, p.err);
+    if (!ok) break;
+    for (int64_t q = tid; q < r.nprobe; q += nth) {  // as record_step after step k
+      const InstDev in = p.inst[r.inst[q]];
+      const int64_t i = in.base + k;
+      if (i < in.iend) record_probe(r, (int)q, i, Vout[r.src[q]], in.dT);
+    }
+    if (s.n > 0 && k + 1 < nk) {
+      for (int64_t q = tid; q < s.n; q += nth) apply_row(s, p, (int)q, k + 1, kMixed);
+      ok = grid_barrier(gb, target, p.err);
+    }
+  }
+  grid_barrier_exit(gb);
+}
+
 // V_t = V_source(t) for every terminal (src/solverEx-cpu.cpp:155-161).
 __global__ void terminal_fixup(const Topo *__restrict__ topo, const int64_t *__restrict__ terms,
                                int64_t nterm, double *__restrict__ V, float *__restrict__ Vf) {
@@ -494,6 +611,39 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
   return NRT_OK;
 }
 
+// nk steps of the time loop in one cooperative launch (explicit_steps_chunk).  Threads per
+// CTA: step_threads when set, else up to 1024 (mixed; 256 in FP64, whose element body needs
+// more than 64 registers) while the pack fills every SM at one element per thread, and fewer
+// (down to 32) for small packs, which spreads them over more SMs (an FP64 pack over more
+// FP64 pipes).  CTAs: as many as the elements need, at most the resident limit (at most
+// per_sm_cap per SM when that is positive).
+int launch_explicit_chunk(const PackView &pv, int precision, int nk, double *V0, double *V1,
+                          float *F0, float *F1, const RecView &r, const StrainView &s,
+                          GridBar *gb, int per_sm_cap, cudaStream_t st) {
+  if (nk <= 0) return NRT_OK;
+  const bool mixed = precision == NRT_MIXED;
+  int threads = mixed ? 1024 : 256;
+  while (threads > 32 && pv.ntot < (int64_t)threads * (pv.sms > 0 ? pv.sms : 1)) threads >>= 1;
+  if (pv.step_threads > 0) threads = pv.step_threads;
+  void *fn = !mixed ? (void *)explicit_steps_chunk<false, 256>
+                    : (threads > 256 ? (void *)explicit_steps_chunk<true, 1024>
+                                     : (void *)explicit_steps_chunk<true, 256>);
+  int per_sm = 0;
+  NRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0));
+  if (per_sm_cap > 0) per_sm = std::min(per_sm, per_sm_cap);
+  if (per_sm <= 0) return NRT_EINVAL;
+  const int64_t need = (pv.ntot + threads - 1) / threads;
+  const unsigned blocks = (unsigned)std::min<int64_t>((int64_t)pv.sms * per_sm, need);
+  PackView p = pv;
+  RecView rv = r;
+  StrainView sv = s;
+  int nk_ = nk;
+  void *args[] = {&p, &nk_, &V0, &V1, &F0, &F1, &rv, &sv, &gb};
+  NRT_CUDA(cudaLaunchCooperativeKernel(fn, blocks, threads, args, 0, st));
+  count_launch_on(st);
+  return NRT_OK;
+}
+
 // Persistent CTAs for the tiled mixed step on this device (0 if it cannot run): as many
 // per SM as fit, or at most per_sm_cap when that is positive (a tuned shape; the kernel
 // strides over the tiles, so any grid gives the same results).
@@ -515,6 +665,7 @@ int launch_terminal_fixup(const Topo *topo, const int64_t *terms, int64_t nterm,
                           float *Vf, cudaStream_t st) {
   if (nterm <= 0) return NRT_OK;
   terminal_fixup<<<(unsigned)((nterm + 255) / 256), 256, 0, st>>>(topo, terms, nterm, V, Vf);
+  count_launch_on(st);
   NRT_CUDA(cudaGetLastError());
   return NRT_OK;
 }

@@ -52,6 +52,7 @@
 
 #include "hh.cuh"
 #include "nrt_solver.h"
+#include "pdl.cuh"
 #include "record.cuh"
 #include "tma.cuh"
 
@@ -87,9 +88,9 @@ struct InstStat {
   int32_t nonconv;
   double last_res;
   // passes over the rows (GMRES), for bandwidth accounting: FP64 residuals after the one
-  // fused into the assembly, preconditioner applications, solution updates, and basis
-  // vectors read by the Arnoldi steps (sum of j + 1)
-  int64_t residuals, applies, xupdates, basis;
+  // fused into the assembly, preconditioner applications, solution updates, basis
+  // vectors read by the Arnoldi steps (sum of j + 1), and Richardson refinement steps
+  int64_t residuals, applies, xupdates, basis, rich;
 };
 
 struct ImView {
@@ -102,6 +103,7 @@ struct ImView {
   double tol;
   int max_iter;      // per step per instance; 0 -> instance size; < 0 -> assembly only
   double inner_rel;  // a refinement cycle's inner target relative to its starting residual
+  int rich;          // refinement cycles start as preconditioned Richardson steps
   int ninst;
   int tile_rows;     // rows per shared-memory tile (segment preconditioner)
   const uint8_t *rowf;
@@ -1454,10 +1456,16 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
   }
   const int budget = iv.max_iter > 0 ? iv.max_iter : (iv.max_iter < 0 ? 0 : (int)inst_n);
   const double inner_rel = iv.inner_rel;
-  int iters = 0, n_res = 0, n_app = 0, n_xup = 0, n_basis = 0;
-  double res = 0;
+  int iters = 0, n_res = 0, n_app = 0, n_xup = 0, n_basis = 0, n_rich = 0;
+  double res = 0, prev_res = 0;
   bool converged = false;
   bool x0_pending = true;  // V holds V^{n-1} until the first solution update
+  // Mixed precision with the tree preconditioner: M is the FP32 factorisation of A itself,
+  // so GMRES's one Arnoldi step per cycle takes x += y M^-1 r with y within rounding of 1.
+  // A Richardson step takes x += M^-1 r without the SpMV, the products and the basis
+  // update.  The FP64 residual that opens the next cycle checks it: a cycle that does not
+  // lower the true residual tenfold hands the rest of the step to GMRES cycles.
+  bool rich = iv.rich != 0;
   for (int cycle = 0;; cycle++) {
     // ---- cycle start: true residual r = b - A x in FP64, W_0 = r, Z_0 = M^-1 r
     if (cycle == 0) {
@@ -1472,7 +1480,8 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
       converged = true;
       break;
     }
-    if (iters >= budget || !(res == res)) break;  // budget spent, or the state is not finite
+    if (iters + n_rich >= budget || !(res == res)) break;  // budget spent, or not finite
+    if (rich && cycle > 0 && res > 0.1 * prev_res) rich = false;
     if (iv.krylov == NRT_BICGSTAB) {
       if (x0_pending) {
         ph_x0(c, Vin, Vout);
@@ -1488,6 +1497,17 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
     apply_precond(c, c.w.Wb, c.w.Z);
     n_app++;
     group_sync<kGrid>(grid);  // Z_0 of every row visible before the SpMV
+    if (rich) {  // x += M^-1 r
+      if (threadIdx.x == 0) coef[0] = (T)1;
+      __syncthreads();
+      ph_xupdate(c, 1, coef, Vout, x0_pending ? Vin : (const double *)nullptr);
+      group_sync<kGrid>(grid);
+      n_xup++;
+      n_rich++;
+      x0_pending = false;
+      prev_res = res;
+      continue;
+    }
     if (threadIdx.x == 0) {
       S.g[0] = res;
       for (int i = 1; i <= m; i++) S.g[i] = 0;
@@ -1538,7 +1558,7 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
       k = j + 1;
       iters++;
       n_basis += j + 1;
-      if (S.flag[0] || iters >= budget || k >= m) break;
+      if (S.flag[0] || iters + n_rich >= budget || k >= m) break;
       // Z_{j+1} = M^-1 W_{j+1}, only when another Arnoldi step will use it
       apply_precond(c, c.w.Wb + (size_t)(j + 1) * c.pv->ntot, c.w.Z + (size_t)(j + 1) * c.pv->ntot);
       n_app++;
@@ -1570,6 +1590,7 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
     st.applies += n_app;
     st.xupdates += n_xup;
     st.basis += n_basis;
+    st.rich += n_rich;
   }
   group_sync<kGrid>(grid);  // V^{n+1} complete before the next step reads it
 }
@@ -2171,6 +2192,8 @@ int Engine::implicit_init() {
   iv.tol = opt.tol;
   iv.max_iter = opt.max_iter;
   iv.inner_rel = !mixed ? 0.0 : (opt.inner_tol > 0 ? opt.inner_tol : NRT_INNER_TOL_DEFAULT);
+  iv.rich = mixed && opt.precond == NRT_PRECOND_TREE && opt.krylov == NRT_GMRES &&
+            opt.refinement == 0;
   iv.ninst = ni;
   iv.tile_rows = S.tile_rows;
   uint8_t *pr;
@@ -2237,7 +2260,7 @@ int Engine::implicit_init() {
   TRYI(up(arena, iv.err, (const int *)nullptr, 1, st));
   NRT_CUDA(cudaMemsetAsync(iv.err, 0, sizeof(int), st));
   TRYI(up(arena, iv.partials, (const double *)nullptr, (size_t)2 * 4096 * kMaxDots, st));
-  std::vector<InstStat> zero(ni, InstStat{0, 0, 0, 0.0, 0, 0, 0, 0});
+  std::vector<InstStat> zero(ni, InstStat{0, 0, 0, 0.0, 0, 0, 0, 0, 0});
   TRYI(up(arena, iv.stats, zero.data(), ni, st));
   iv.work_lev = nullptr;
   std::vector<char> sgbuf;
@@ -2315,6 +2338,7 @@ static int implicit_launch(Engine &e, int nsteps, int force) {
     const void *k = mixed ? (const void *)implicit_steps<float, false> : (const void *)implicit_steps<double, false>;
     NRT_CUDA(cudaLaunchKernel(k, dim3(S.grid_blocks), dim3(kThreads), args, S.smem, e.stream));
   }
+  count_launch_on(e.stream);
   return NRT_OK;
 }
 
@@ -2339,7 +2363,7 @@ int implicit_advance(Engine &e, int64_t steps) {
 int instance_stats(Engine &e, int64_t *iters, int32_t *last_iters, int32_t *nonconv,
                    double *last_res) {
   const int32_t ni = e.host.ninst;
-  std::vector<InstStat> s(ni, InstStat{0, 0, 0, 0.0, 0, 0, 0, 0});
+  std::vector<InstStat> s(ni, InstStat{0, 0, 0, 0.0, 0, 0, 0, 0, 0});
   if (e.im) {
     NRT_CUDA(cudaMemcpyAsync(s.data(), e.im->iv.stats, sizeof(InstStat) * ni,
                              cudaMemcpyDeviceToHost, e.stream));
@@ -2355,9 +2379,9 @@ int instance_stats(Engine &e, int64_t *iters, int32_t *last_iters, int32_t *nonc
 }
 
 int pass_counts(Engine &e, int64_t *residuals, int64_t *applies, int64_t *xupdates,
-                int64_t *basis) {
+                int64_t *basis, int64_t *rich) {
   const int32_t ni = e.host.ninst;
-  std::vector<InstStat> s(ni, InstStat{0, 0, 0, 0.0, 0, 0, 0, 0});
+  std::vector<InstStat> s(ni, InstStat{0, 0, 0, 0.0, 0, 0, 0, 0, 0});
   if (e.im) {
     NRT_CUDA(cudaMemcpyAsync(s.data(), e.im->iv.stats, sizeof(InstStat) * ni,
                              cudaMemcpyDeviceToHost, e.stream));
@@ -2368,6 +2392,7 @@ int pass_counts(Engine &e, int64_t *residuals, int64_t *applies, int64_t *xupdat
     if (applies) applies[i] = s[i].applies;
     if (xupdates) xupdates[i] = s[i].xupdates;
     if (basis) basis[i] = s[i].basis;
+    if (rich) rich[i] = s[i].rich;
   }
   return NRT_OK;
 }

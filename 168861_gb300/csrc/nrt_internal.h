@@ -157,6 +157,13 @@ struct RecView {
   double *spk;         // [nprobe][max_spikes]
 };
 
+// The words of the explicit chunk kernel's grid barrier (explicit.cu), 0 between launches.
+struct GridBar {
+  unsigned long long count;  // arrivals in the current launch
+  unsigned int exits;        // CTAs that have left it
+  unsigned int pad;
+};
+
 struct DeviceBuffer {
   void *ptr = nullptr;
   size_t bytes = 0;
@@ -246,6 +253,13 @@ int launch_terminal_fixup(const Topo *topo, const int64_t *terms, int64_t nterm,
                           float *Vf, cudaStream_t st);
 int launch_advance_base(InstDev *inst, int32_t ninst, int64_t steps, cudaStream_t st);
 int explicit_tile_blocks(int device, int64_t ntot, int per_sm_cap);
+struct StrainView;  // strain.cuh
+// nk fused-form steps of the time loop in one cooperative launch, with the probes' reads
+// and the strained elements' rows (from the chunk table) between steps.  V0/F0 hold the
+// current state; step k writes V1/F1 when k is even and V0/F0 when it is odd.
+int launch_explicit_chunk(const PackView &pv, int precision, int nk, double *V0, double *V1,
+                          float *F0, float *F1, const RecView &r, const StrainView &s,
+                          GridBar *gb, int per_sm_cap, cudaStream_t st);
 // Recording after explicit step k (record.cu); V is that step's output.
 int launch_record_step(const RecView &r, const InstDev *inst, int k, const double *V,
                        cudaStream_t st);

@@ -35,15 +35,18 @@ struct Engine {
   bool terminals_dirty = false;
   bool general_next = false;  // explicit: the next step runs in the general form
   cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};  // one per starting buffer parity
+  int64_t graph_nodes[2] = {0, 0};                       // kernels per replay of each
   std::vector<hvec<float>> hostf;  // staging for FP32 uploads
   ImplicitState *im = nullptr;
   RecState *rec = nullptr;                // recording at probes, or null
   StrainState *strain = nullptr;          // time-varying strain of some elements, or null
+  GridBar *gbar = nullptr;                // the explicit chunk kernel's barrier words
   std::vector<void *> extra_mem;          // device tables that replaced the arena's (freed last)
 
   int init(const nrt_problem *probs, int32_t count, const nrt_options *o);
   int step(int k, int force);
   int advance(int64_t steps);
+  bool chunk_kernel() const;  // explicit time loops run a chunk of steps per launch
   int fixup();
   bool needs_general() const { return general_next || (!host.invariant && steps_done == 0); }
   int get_state(int32_t q, double *Vc, double *Vo, double *m, double *h, double *n);
@@ -78,6 +81,7 @@ int launch_strain_update(const Engine &e, int k, cudaStream_t st);
 bool strain_tabled(const Engine &e);
 int launch_strain_derive(const Engine &e, int nk, cudaStream_t st);
 int launch_strain_apply(const Engine &e, int k, cudaStream_t st);
+const StrainView *strain_view(const Engine &e);  // null without strain
 
 // implicit.cu
 int implicit_advance(Engine &e, int64_t steps);
@@ -88,6 +92,6 @@ int implicit_check(Engine &e);
 int instance_stats(Engine &e, int64_t *iters, int32_t *last_iters, int32_t *nonconv,
                    double *last_res);
 int pass_counts(Engine &e, int64_t *residuals, int64_t *applies, int64_t *xupdates,
-                int64_t *basis);
+                int64_t *basis, int64_t *rich);
 
 }  // namespace nrt

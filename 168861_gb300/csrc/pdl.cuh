@@ -29,9 +29,21 @@ __device__ __forceinline__ void chain_release() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Adds n to the count of kernels this library has launched (nrt_kernel_launches; api.cu).
+void count_launches(long long n);
+
+// Counts one launch on st unless st is being captured into a graph (a replay of the graph
+// counts its kernel nodes then).
+inline void count_launch_on(cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone)
+    count_launches(1);
+}
+
 template <typename... KArgs, typename... Args>
 cudaError_t launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
                            cudaStream_t st, Args &&...args) {
+  count_launch_on(st);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;

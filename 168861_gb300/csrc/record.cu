@@ -198,6 +198,7 @@ int Engine::upload_and_init(RecState *R, const std::vector<int64_t> &src,
   int rc = fixup();  // explicit: terminals hold their current value before the first read
   if (rc) return rc;
   record_init<<<(P + 127) / 128, 128, 0, stream>>>(v, d_raw, V[cur]);
+  count_launch_on(stream);
   NRT_CUDA(cudaGetLastError());
   NRT_CUDA(cudaStreamSynchronize(stream));  // the host vectors go out of scope after this
   return NRT_OK;

@@ -29,6 +29,7 @@
 #include <mutex>
 
 #include "nrt_internal.h"
+#include "pdl.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -364,6 +365,7 @@ extern "C" int nrt_solve_csr_static(int32_t n, const int32_t *row_ptr, const int
     void *args[] = {&a};
     cudaStream_t st = (cudaStream_t)stream;
     NRT_CUDA(cudaLaunchCooperativeKernel((const void *)static_gmres, dim3(G), dim3(kT), args, 0, st));
+    count_launch_on(st);
     double res[3];
     NRT_CUDA(cudaMemcpyAsync(res, scratch + L.result, sizeof(res), cudaMemcpyDeviceToHost, st));
     NRT_CUDA(cudaStreamSynchronize(st));

@@ -17,27 +17,9 @@
 #include "derive_elem.h"
 #include "nrt_solver.h"
 #include "pdl.cuh"
+#include "strain.cuh"
 
 namespace nrt {
-
-// The strained elements are grouped into classes of identical input columns (instance,
-// kind and the ten description values): the derivation is a pure function of those and
-// of t, so one evaluation per class gives every member bit for bit what its own would.
-// Elements are stored sorted by class, and a class's members are consecutive.
-struct StrainView {
-  int32_t n;             // strained elements
-  int32_t ncls;          // classes
-  const int64_t *elem;   // global element index, sorted by class
-  const int64_t *col;    // parameter column of an HH element (same order)
-  const int32_t *cls;    // class of each element (same order; non-decreasing)
-  const int32_t *inst;   // [ncls] instance (time and dT)
-  const int32_t *kind;   // [ncls] 1 HH / 0 cable
-  const double *spec;    // [10][ncls]: dX, diameter, ro_a, ro_m, per_m, thickness, rest, sigma_Na, sigma_K, sigma_L
-  double *tab;           // [kChunk][ncls][kStrainOut] derived ahead for a graph chunk, or null
-  int32_t *tlive;        // [kChunk][ncls]: the class's instance still runs at that step
-  int32_t myelin;
-  double e_max, eps0, eps1, t0, t1;
-};
 
 struct StrainState {
   void *mem = nullptr;
@@ -50,7 +32,6 @@ struct StrainState {
 namespace {
 
 constexpr int kStrainBlock = 32;          // strained elements (or table entries) per block
-constexpr int kStrainOut = 2 + HP_ROWS;   // dT/(c_m dX), 1/(r_a dX), then W dX, K dX or the column
 
 // Class c's coefficients for step k of the current loop range into o[kStrainOut]; false
 // when the class's instance has finished its run (nothing is written then).
@@ -101,34 +82,6 @@ __device__ bool derive_class(const StrainView &s, const PackView &p, int c, int 
   return true;
 }
 
-// Element q (class-sorted position) takes its class's coefficients o.
-__device__ void apply_element(const StrainView &s, const PackView &p, int q, const double *o,
-                              int mixed) {
-  const int64_t j = s.elem[q];
-  if (mixed) {
-    ((float *)p.cdtf)[j] = (float)o[0];
-    ((float *)p.gaxf)[j] = (float)o[1];
-  } else {
-    ((double *)p.cdt)[j] = o[0];
-    ((double *)p.gax)[j] = o[1];
-  }
-  if (s.kind[s.cls[q]] == 1) {
-    const int64_t cc = s.col[q];
-    if (mixed) {
-      float *col = (float *)(p.hpq + 3 * cc);
-      for (int r = 0; r < HP_ROWS; r++) col[r] = (float)o[2 + r];
-    } else {
-      for (int r = 0; r < HP_ROWS; r++) ((double *)p.hp)[r * p.hp_ld + cc] = o[2 + r];
-    }
-  } else if (mixed) {
-    ((float *)p.wdxf)[j] = (float)o[2];
-    ((float *)p.kdxf)[j] = (float)o[3];
-  } else {
-    ((double *)p.wdx)[j] = o[2];
-    ((double *)p.kdx)[j] = o[3];
-  }
-}
-
 // Step k, derivation and writes in one launch.  Block b owns elements [32 b, 32 b + 32)
 // of the class-sorted list, which span at most 32 consecutive classes.  Thread t derives
 // class (first class of the block) + t, if the block has it, into shared memory; then
@@ -168,8 +121,7 @@ __global__ void __launch_bounds__(256) strain_apply(StrainView s, PackView p, in
   chain_release();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= s.n) return;
-  const int64_t g = (int64_t)k * s.ncls + s.cls[q];
-  if (s.tlive[g]) apply_element(s, p, q, s.tab + g * kStrainOut, mixed);
+  apply_row(s, p, q, k, mixed);
 }
 
 }  // namespace
@@ -185,6 +137,8 @@ int launch_strain_update(const Engine &e, int k, cudaStream_t st) {
 }
 
 bool strain_tabled(const Engine &e) { return e.strain && e.strain->view.tab; }
+
+const StrainView *strain_view(const Engine &e) { return e.strain ? &e.strain->view : nullptr; }
 
 int launch_strain_derive(const Engine &e, int nk, cudaStream_t st) {
   const StrainView &v = e.strain->view;

@@ -272,12 +272,18 @@ class ProblemArrays:
                    ls_Na=hp[9], ls_K=hp[10], rest=hp[11], V0=V0, V1=V1, dT=dT)
 
 
+def kernel_launches() -> int:
+    """Kernels the library has launched in this process so far (nrt_kernel_launches)."""
+    return int(_lib.load().nrt_kernel_launches())
+
+
 def make_options(mode: int, precision: str = "fp64", krylov: str = "gmres",
                  precond: str = "tree", restart: int = 30, tol: float = 1e-14,
                  tol_mode: str = "abs", max_iter: int = 0, use_graphs: bool = True,
                  device: int = -1, schedule: int = 0, tiled: bool = True,
                  scheme: str = "be", tile_ctas_per_sm: int = 0,
-                 step_threads: int = 0, inner_tol: float = 0.0) -> _lib.Options:
+                 step_threads: int = 0, inner_tol: float = 0.0,
+                 step_launch: int = 0, refinement: str = "auto") -> _lib.Options:
     lib = _lib.load()
     o = _lib.Options()
     check(lib.nrt_options_default(ctypes.byref(o)), "nrt_options_default")
@@ -297,6 +303,8 @@ def make_options(mode: int, precision: str = "fp64", krylov: str = "gmres",
     o.tile_ctas_per_sm = int(tile_ctas_per_sm)
     o.step_threads = int(step_threads)
     o.inner_tol = float(inner_tol)
+    o.step_launch = int(step_launch)
+    o.refinement = {"auto": 0, "gmres": 1}[refinement]
     return o
 
 
@@ -532,9 +540,9 @@ class Batch(_Recorder):
 
     def pass_counts(self) -> dict:
         """Per-instance counts of the implicit kernel's passes over the rows (GMRES):
-        residuals, applies, xupdates, basis."""
+        residuals, applies, xupdates, basis, and Richardson refinement steps (richardson)."""
         out = {k: np.zeros(self.count, np.int64) for k in ("residuals", "applies", "xupdates",
-                                                          "basis")}
+                                                          "basis", "richardson")}
         check(self.lib.nrt_batch_pass_counts(self.h, *[_p(out[k], ctypes.c_int64) for k in out]),
               "nrt_batch_pass_counts")
         return out

@@ -24,7 +24,6 @@ from __future__ import annotations
 import argparse
 import importlib
 import json
-import math
 import multiprocessing as mp
 import os
 import subprocess
@@ -282,8 +281,10 @@ def algorithmic_bytes_implicit(probs, steps: int, iters, counts):
     rule: the compulsory-traffic rule for an implicit step, per compartment: assembly = HH
       state (FP32 gates r/w 24) + V r 8 + b w 8 + diagonal w 8 + the parameters that vary
       within the tree; plus, per Krylov iteration j, a CSR SpMV (36 B with FP32 values and
-      int32 indices at 3 nonzeros per row) and the orthogonalisation, 4 (2 (j + 1) + 1) B.
-      It counts no preconditioner and no refinement residual.
+      int32 indices at 3 nonzeros per row) and the orthogonalisation, 4 (2 (j + 1) + 1) B;
+      plus, per Richardson refinement step (an iteration without orthogonalisation), the
+      FP64 SpMV of the residual that checks it (56 B).  It counts no preconditioner and no
+      other refinement residual.
 
     passes: what this kernel's passes must move per row, counted per pass:
       assembly (HH 85 / passive 77 B: rowf 1, V^n 8, V^n-1 8, c_m dX/dT 8, 1/(r_a dX) 8,
@@ -303,7 +304,8 @@ def algorithmic_bytes_implicit(probs, steps: int, iters, counts):
         ph, pp = _param_bytes(p, 4)
         asm_rule = n_hh * (24 + 24 + ph) + (n - n_hh) * (24 + pp)
         I, B = float(iters[k]), float(counts["basis"][k])
-        rule += asm_rule + n * (36 * I + 4 * (2 * B + I)) / steps
+        R = float(counts["richardson"][k]) if "richardson" in counts else 0.0
+        rule += asm_rule + n * (36 * I + 4 * (2 * B + I) + 56 * R) / steps
         asm = n_hh * 85 + (n - n_hh) * 77
         per_run = (37 * counts["residuals"][k] + 38 * counts["applies"][k]
                    + (17 + 8 + 4) * I + 8 * B + 17 * counts["xupdates"][k])
@@ -421,10 +423,12 @@ def run_ours(args, rank: int, world: int, dist, wl: str, extras: bool = True, st
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
+        l0 = pkg.kernel_launches()
         ev0.record(stream)
         b.advance(K)
         ev1.record(stream)
         ev1.synchronize()
+        launches = pkg.kernel_launches() - l0  # the library's own count of its launches
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
     st = b.stats()
@@ -465,11 +469,6 @@ def run_ours(args, rank: int, world: int, dist, wl: str, extras: bool = True, st
         a2 = passes_all * K / (ms / 1e3) / 1e9 / world
         roof_passes = {"bound": "hbm", "achieved": a2, "peak": peak, "unit": "GB/s",
                        "frac": a2 / peak, "bytes_per_step": passes_all}
-    # our kernels launched in the timed region: one persistent launch + one loop-index
-    # update per 64-step chunk (implicit); 64 step launches + 1 update per graph (explicit),
-    # and with strain one coefficient write per step + one derivation per graph
-    launches = (2 * math.ceil(K / 64) if implicit
-                else (K + math.ceil(K / 64)) * (2 if strained else 1))
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms / K, "higher_is_better": True,
@@ -605,6 +604,7 @@ def run_serve(args, rank: int, world: int, dist, count: int = 0, plain: bool = T
     srv = pkg.Server(budget_bytes=64 << 30, chunk_steps=64, max_wait_us=200,
                      explicit_opts=ex, implicit_opts=im)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        l0 = pkg.kernel_launches()
         t0 = time.perf_counter()
         nxt = t0
         for gap, p, imp, run in reqs:
@@ -615,6 +615,7 @@ def run_serve(args, rank: int, world: int, dist, count: int = 0, plain: bool = T
             srv.submit(p, imp, *run)
         srv.drain()
         wall = time.perf_counter() - t0
+        launches = pkg.kernel_launches() - l0
     st = srv.stats()
     srv.close()
     work = float(st.compartment_steps)
@@ -642,7 +643,7 @@ def run_serve(args, rank: int, world: int, dist, count: int = 0, plain: bool = T
                        "sim_time": "U(10,100) ms (myelinated axons U(0.5,2) us)"},
             "p50_ms": p50, "p99_ms": p99, "max_ms": pmax,
             "batches": int(st.batches_created), "completed": int(st.completed),
-            "clocks": clk.summary(),
+            "gpu_launches": launches, "clocks": clk.summary(),
             "e2e": {"value": work / wall, "unit": "compartment-steps/s",
                     "h2d_bytes_per_step": h2d / count, "d2h_bytes_per_step": d2h / count}}
     if plain and world == 1:

@@ -136,6 +136,22 @@ typedef struct nrt_options {
                                     is below inner_tol times the cycle's starting residual
                                     (0 = the default, NRT_INNER_TOL_DEFAULT).  FP64 mode
                                     solves each cycle to the outer tolerance and ignores it */
+  int32_t step_launch;           /* explicit time loops (nrt_run, nrt_batch_advance, the
+                                    server): 0 = one launch per step (default; chained launches
+                                    replayed from a captured graph), 1 = up to 64 steps per
+                                    cooperative launch with a grid barrier between steps (on a
+                                    GB300 a barrier across both dies costs about what a chained
+                                    launch does, so this is not faster there).  Launch shapes
+                                    only: results do not depend on it */
+  int32_t refinement;            /* implicit, mixed precision, GMRES with the tree
+                                    preconditioner: 0 = auto: each FP64 refinement cycle is
+                                    one preconditioned Richardson step, x += M^-1 r (M, the
+                                    FP32 factorisation of A, solves A up to rounding, so
+                                    GMRES's single Arnoldi step would scale M^-1 r by ~1),
+                                    for as long as every cycle lowers the true residual at
+                                    least tenfold; GMRES cycles from the first that does not.
+                                    1 = GMRES cycles always.  Both stop on the same FP64
+                                    residual test */
 } nrt_options;
 
 /* One FP32 cycle cannot reduce the true residual by much more than 1e-4 on a stiff
@@ -211,6 +227,11 @@ int nrt_destroy(nrt_solver *s);
 const char *nrt_status_string(int status);
 const char *nrt_last_error(void);
 
+/* Kernels this library has launched in this process so far, over all handles and threads
+ * (a replay of a captured time-loop graph counts each of its kernel nodes; copies and
+ * memsets are not kernels).  The difference across a region is its launch count. */
+int64_t nrt_kernel_launches(void);
+
 /* ----------------------------------------------------------------------------------
  * Parameter pipeline on the host: the reference's src/init.cpp:320-333 (strain on dX),
  * :235-254 (electrical_properties), :273-298 (hhIconds), :180-198
@@ -274,11 +295,12 @@ int nrt_batch_instance_stats(nrt_batch *b, int64_t *iters, int32_t *last_iters,
                              int32_t *nonconverged, double *last_residual);
 /* Per-instance counts of the implicit kernel's passes over the rows since creation
  * (GMRES): FP64 residuals after the one fused into each step's assembly, preconditioner
- * applications, solution updates, and basis vectors read by the Arnoldi steps (the sum of
- * j + 1 over steps j).  With the iteration count they give the bytes a step moved.  Arrays
- * of `count` entries; any may be NULL.  No reference counterpart. */
+ * applications, solution updates, basis vectors read by the Arnoldi steps (the sum of
+ * j + 1 over steps j), and Richardson refinement steps (nrt_options.refinement; not
+ * counted as Krylov iterations).  With the iteration count they give the bytes a step
+ * moved.  Arrays of `count` entries; any may be NULL.  No reference counterpart. */
 int nrt_batch_pass_counts(nrt_batch *b, int64_t *residuals, int64_t *precond_applies,
-                          int64_t *xupdates, int64_t *basis_reads);
+                          int64_t *xupdates, int64_t *basis_reads, int64_t *richardson_steps);
 int nrt_batch_destroy(nrt_batch *b);
 
 /* ----------------------------------------------------------------------------------

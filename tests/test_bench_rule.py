@@ -60,6 +60,20 @@ def test_implicit_rule(axon):
     assert passes == pytest.approx(n_hh * 85 + (n - n_hh) * 77 + n * 29 + n * per_run / steps)
 
 
+def test_implicit_rule_richardson_steps(axon):
+    """Richardson refinement steps: no Krylov iteration, one FP64 SpMV (56 B) each under the
+    rule; their applications, updates and residuals are counted passes as before."""
+    n, n_hh = axon.num_elem, int(axon.struct.num_hh)
+    steps = 10
+    counts = {"basis": [0.0], "residuals": [20.0], "applies": [20.0], "xupdates": [20.0],
+              "richardson": [20.0]}
+    rule, passes = bench.algorithmic_bytes_implicit([axon], steps, [0.0], counts)
+    asm = n_hh * (24 + 24) + (n - n_hh) * 24
+    assert rule == pytest.approx(asm + n * 56 * 20 / steps)
+    per_run = 37 * 20 + 38 * 20 + 17 * 20
+    assert passes == pytest.approx(n_hh * 85 + (n - n_hh) * 77 + n * 29 + n * per_run / steps)
+
+
 def test_varied_geometry_is_charged(pkg, model):
     """A random tree (diameter set per branch level) pays for both coefficients."""
     spec = model.random_tree(seed=4, n_target=800)

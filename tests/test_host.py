@@ -82,9 +82,10 @@ def test_options_struct_matches_the_header(pkg, lib):
     o = pkg._lib.Options()
     ct.memset(ct.byref(o), 0x7f, ct.sizeof(o))
     assert lib.nrt_options_default(ct.byref(o)) == 0
-    assert ct.sizeof(o) == 4 * 6 + 8 + 4 * 8 + 8  # 6 ints, tol, 8 ints, inner_tol
+    assert ct.sizeof(o) == 4 * 6 + 8 + 4 * 8 + 8 + 4 * 2  # 6 ints, tol, 8 ints, inner_tol, 2 ints
     assert (o.tiled, o.use_graphs, o.tile_ctas_per_sm, o.step_threads) == (1, 1, 0, 0)
     assert o.inner_tol == 0.0
+    assert (o.step_launch, o.refinement) == (0, 0)
 
 
 def test_implicit_requires_reference_numbering(pkg, lib, model):

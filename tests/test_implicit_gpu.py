@@ -276,23 +276,70 @@ def test_bicgstab_unpreconditioned_reports_budget(gpu, pkg):
     s.close()
 
 
-def test_pass_counts_follow_the_gmres_structure(gpu, pkg, model):
+@pytest.mark.parametrize("refinement", ["gmres", "auto"])
+def test_pass_counts_follow_the_gmres_structure(gpu, pkg, model, refinement):
     """The kernel's pass counters (used for the bandwidth accounting): one preconditioner
-    application per Arnoldi step, one FP64 residual per solution update (every update is
-    followed by its residual check), and the basis reads of step j are j + 1."""
+    application per Arnoldi step or Richardson step, one FP64 residual per solution update
+    (every update is followed by its residual check), and the basis reads of step j are
+    j + 1.  With refinement="auto" (mixed precision, tree preconditioner) every step opens
+    with a Richardson step."""
     specs = [model.random_tree(seed=s, n_target=n, dt=2.5e-5, tspan=1e-3)
              for s, n in [(41, 3000), (42, 12000)]]
     b = pkg.Batch([pkg.ProblemArrays.from_spec(sp, pkg.derive(sp)) for sp in specs], mode=1,
-                  precision="mixed", restart=20, tol=1e-10, tol_mode="rel")
+                  precision="mixed", restart=20, tol=1e-10, tol_mode="rel",
+                  refinement=refinement)
     b.set_runs([(1, 21, sp.init_time, sp.end_input) for sp in specs])
     b.advance(20)
     it = b.instance_stats()["iters"]
     pc = b.pass_counts()
     b.close()
-    np.testing.assert_array_equal(pc["applies"], it)
+    np.testing.assert_array_equal(pc["applies"], it + pc["richardson"])
     np.testing.assert_array_equal(pc["residuals"], pc["xupdates"])
     assert (pc["xupdates"] >= 20).all()            # at least one update per step
     assert (pc["basis"] >= it).all() and (pc["basis"] <= it * (it + 1) // 2).all()
+    if refinement == "gmres":
+        assert (pc["richardson"] == 0).all() and (it >= 20).all()
+    else:
+        assert (pc["richardson"] >= 20).all()
+
+
+def test_richardson_refinement_matches_gmres_cycles(gpu, pkg, model):
+    """Mixed precision with the tree preconditioner: Richardson refinement cycles reach the
+    same FP64 residual test as GMRES cycles, so both give the backward-Euler solution to
+    the tolerance (1e-10 relative here); they differ by far less than the accuracy bar."""
+    specs = [model.random_tree(seed=s, n_target=n, dt=2.5e-5, tspan=2e-3)
+             for s, n in [(51, 1500), (52, 30000), (53, 90000)]]
+    probs = [pkg.ProblemArrays.from_spec(sp, pkg.derive(sp)) for sp in specs]
+    out = {}
+    for refinement in ("gmres", "auto"):
+        b = pkg.Batch(probs, mode=1, precision="mixed", restart=20, tol=1e-10, tol_mode="rel",
+                      refinement=refinement)
+        b.set_runs([(1, 41, sp.init_time, sp.end_input) for sp in specs])
+        b.advance(40)
+        st = b.instance_stats()
+        assert (st["nonconverged"] == 0).all()
+        out[refinement] = (b.snapshot_all(), b.pass_counts())
+        b.close()
+    for x, y in zip(out["gmres"][0], out["auto"][0]):
+        assert np.abs(x - y).max() < 1e-8  # 1e-5 mV
+    assert (out["auto"][1]["basis"] == 0).all()  # every cycle took the Richardson step
+
+
+def test_richardson_hands_over_to_gmres_when_it_stalls(gpu, pkg, model):
+    """A tolerance below what FP64 rounding of the residual allows: the Richardson steps
+    stop lowering the residual tenfold, the rest of each step runs GMRES cycles, and the
+    budget ends the step (reported as non-converged)."""
+    spec = model.random_tree(seed=54, n_target=5000, dt=2.5e-5, tspan=1e-3)
+    b = pkg.Batch([pkg.ProblemArrays.from_spec(spec, pkg.derive(spec))], mode=1,
+                  precision="mixed", restart=20, tol=1e-19, tol_mode="rel", max_iter=8)
+    b.set_runs([(1, 4, spec.init_time, spec.end_input)])
+    b.advance(3)
+    st = b.instance_stats()
+    pc = b.pass_counts()
+    b.close()
+    assert pc["richardson"][0] >= 3 and pc["basis"][0] > 0
+    assert st["nonconverged"][0] == 3
+    assert pc["richardson"][0] + st["iters"][0] == 3 * 8  # the budget counts both kinds
 
 
 @pytest.mark.parametrize("name", golden_names("i"))
