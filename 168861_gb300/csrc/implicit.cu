@@ -249,16 +249,21 @@ __device__ __forceinline__ void group_sync(cg::grid_group &grid) {
 
 // ---------------------------------------------------------------- row kernels
 
-// (A x)_r for the kN rows r = rb + u * stride (rows >= r1 give 0, flag R_IDENT).  D / G:
-// diagonal and conductance arrays (FP32 or FP64), x the vector.  All independent loads of
-// the kN rows are issued before any use.
-template <int kN, typename C, typename X>
-__device__ __forceinline__ void apply_rows(const PackView &pv, const ImView &iv,
-                                           const C *__restrict__ D, const C *__restrict__ G,
-                                           const X *x, int64_t rb, int64_t stride, int64_t r1,
-                                           X (&out)[kN], uint8_t (&fl)[kN]) {
+// b_r - (A x)_r for the kN rows r = rb + u * stride (rows >= r1 give 0, flag R_IDENT), in
+// FP64 as fused multiply-adds: b - d x first (one rounding for the two terms that nearly
+// cancel), then + g x_q for each neighbour.  D / G: diagonal and conductance arrays, x the
+// vector.  All independent loads of the kN rows are issued before any use.
+template <int kN>
+__device__ __forceinline__ void residual_rows(const PackView &pv, const ImView &iv,
+                                              const double *__restrict__ B,
+                                              const double *__restrict__ D,
+                                              const double *__restrict__ G, const double *x,
+                                              int64_t rb, int64_t stride, int64_t r1,
+                                              double (&out)[kN], uint8_t (&fl)[kN]) {
+  using C = double;
+  using X = double;
   const int64_t N = pv.ntot;
-  C dg[kN], gm[kN], gp[kN];
+  C dg[kN], gm[kN], gp[kN], bb[kN];
   X xs[kN], xm[kN], xp[kN];
 #pragma unroll
   for (int u = 0; u < kN; u++) {
@@ -266,6 +271,7 @@ __device__ __forceinline__ void apply_rows(const PackView &pv, const ImView &iv,
     const bool ok = r < r1;
     const int64_t rm = r > 0 ? r - 1 : r, rp = r + 1 < N ? r + 1 : r;
     fl[u] = ok ? iv.rowf[r] : (uint8_t)R_IDENT;
+    bb[u] = ok ? B[r] : (C)0;
     dg[u] = ok ? D[r] : (C)0;
     gm[u] = ok ? G[r] : (C)0;
     gp[u] = ok ? G[rp] : (C)0;
@@ -288,10 +294,10 @@ __device__ __forceinline__ void apply_rows(const PackView &pv, const ImView &iv,
           xl = x[t.dl];
         }
       }
-      s = dg[u] * xs[u];
-      if (f & R_UP) s -= gm[u] * mo;
-      if (f & R_DOWNR) s -= gp[u] * xp[u];
-      if (f & R_DOWNL) s -= gl * xl;
+      s = fma(-dg[u], xs[u], bb[u]);
+      if (f & R_UP) s = fma(gm[u], mo, s);
+      if (f & R_DOWNR) s = fma(gp[u], xp[u], s);
+      if (f & R_DOWNL) s = fma(gl, xl, s);
     }
     out[u] = s;
   }
@@ -1044,12 +1050,11 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
       }
       iv.rhs[r] = b;
       bacc += (T)b * (T)b;
-      // r = b - A x0, in the order of row_apply: diagonal, mother, DR, DL
-      double ax = d * (2.0 * v[u] - vo[u]);
-      if (f[u] & R_UP) ax -= gj[u] * xmo;
-      if (f[u] & R_DOWNR) ax -= gn[u] * xp[u];
-      if (f[u] & R_DOWNL) ax -= gl * xl;
-      const double rr = b - ax;
+      // r = b - A x0 as residual_rows forms it: b - d x0, then mother, DR, DL
+      double rr = fma(-d, 2.0 * v[u] - vo[u], b);
+      if (f[u] & R_UP) rr = fma(gj[u], xmo, rr);
+      if (f[u] & R_DOWNR) rr = fma(gn[u], xp[u], rr);
+      if (f[u] & R_DOWNL) rr = fma(gl, xl, rr);
       c.w.Wb[r] = (T)rr;
       racc += rr * rr;
     }
@@ -1066,22 +1071,22 @@ __device__ __noinline__ void ph_x0(Ctx<T, kGrid> c, const double *Vin, double *V
 }
 
 // True residual r = b - A x in FP64 into W_0 (identity rows 0); returns the thread's
-// part of ||r||^2.
+// part of ||r||^2, or with scale > 0 of ||scale r||^2 summed in FP32.  That form is for
+// the mixed GMRES and Richardson cycles, where the norm only decides convergence and scales
+// an FP32 basis: it keeps the sum off the FP64 pipe, and the caller passes a power of two
+// near 1 / (the previous residual norm), which keeps the entries in FP32's range.  FP64
+// solves and BiCGSTAB (whose rho_0 is this norm squared) take the FP64 sum.
 template <typename T, bool kGrid>
-__device__ __noinline__ double ph_residual(Ctx<T, kGrid> c, const double *x) {
+__device__ __noinline__ double ph_residual(Ctx<T, kGrid> c, const double *x, float scale) {
   const PackView &pv = *c.pv;
   const ImView &iv = *c.iv;
   const int64_t stride = blockDim.x;
-  double acc = 0;
+  float acc = 0;
+  double acc64 = 0;
   for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kR * stride) {
-    double rh[kR], ax[kR];
+    double rr[kR];
     uint8_t fl[kR];
-#pragma unroll
-    for (int u = 0; u < kR; u++) {
-      const int64_t r = rb + u * stride;
-      rh[u] = r < c.r1 ? iv.rhs[r] : 0.0;
-    }
-    apply_rows<kR>(pv, iv, iv.diag, iv.g64, x, rb, stride, c.r1, ax, fl);
+    residual_rows<kR>(pv, iv, iv.rhs, iv.diag, iv.g64, x, rb, stride, c.r1, rr, fl);
 #pragma unroll
     for (int u = 0; u < kR; u++) {
       const int64_t r = rb + u * stride;
@@ -1090,12 +1095,16 @@ __device__ __noinline__ double ph_residual(Ctx<T, kGrid> c, const double *x) {
         c.w.Wb[r] = 0;
         continue;
       }
-      const double rr = rh[u] - ax[u];
-      c.w.Wb[r] = (T)rr;
-      acc += rr * rr;
+      c.w.Wb[r] = (T)rr[u];
+      if (scale > 0) {
+        const float e = (float)rr[u] * scale;
+        acc = fmaf(e, e, acc);
+      } else {
+        acc64 += rr[u] * rr[u];
+      }
     }
   }
-  return acc;
+  return scale > 0 ? (double)acc : acc64;
 }
 
 // y = s_j A Z_j, fused with the thread's parts of <y, W_i> for i < g1.
@@ -1238,6 +1247,36 @@ __device__ __noinline__ void ph_xupdate(Ctx<T, kGrid> c, int k, const T *coef, d
         const double base = Vin ? x0_of(Vin, Vout, r) : Vout[r];
         Vout[r] = base + (double)a[u];
       }
+    }
+  }
+}
+
+// A Richardson step's update V += Z_0 (identity rows keep their value), with every load of
+// a thread's kV rows issued before any use.  With Vin non-null this is the step's first
+// update and V starts from x0 = 2 Vin - V.  Equal bit for bit to ph_xupdate with k = 1 and
+// coefficient 1.
+template <typename T, bool kGrid>
+__device__ __noinline__ void ph_rich_update(Ctx<T, kGrid> c, double *Vout, const double *Vin) {
+  const int64_t stride = blockDim.x;
+  const uint8_t *rowf = c.iv->rowf;
+  const T *Z = c.w.Z;
+  for (int64_t rb = c.r0 + threadIdx.x; rb < c.r1; rb += kV * stride) {
+    uint8_t fl[kV];
+    T z[kV];
+    double v[kV], w[kV];
+#pragma unroll
+    for (int u = 0; u < kV; u++) {
+      const int64_t r = rb + u * stride;
+      const bool ok = r < c.r1;
+      fl[u] = ok ? rowf[r] : (uint8_t)R_IDENT;
+      z[u] = ok ? Z[r] : (T)0;
+      v[u] = ok ? Vout[r] : 0.0;
+      w[u] = ok && Vin ? Vin[r] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kV; u++) {
+      const int64_t r = rb + u * stride;
+      if (!(fl[u] & R_IDENT)) Vout[r] = (Vin ? 2.0 * w[u] - v[u] : v[u]) + (double)z[u];
     }
   }
 }
@@ -1471,9 +1510,12 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
     if (cycle == 0) {
       res = res0;
     } else {
-      double acc[1] = {ph_residual(c, Vout)};
+      // res > 0 here (a zero residual has converged); the scale stays a normal FP32 number
+      const bool f32 = sizeof(T) == 4 && iv.krylov == NRT_GMRES;
+      const int e = f32 ? max(-126, min(126, ilogb(res))) : 0;
+      double acc[1] = {ph_residual(c, Vout, f32 ? exp2f((float)-e) : 0.0f)};
       group_reduce<kGrid>(grid, acc, 1, S, iv.partials, parity);
-      res = sqrt(S.red[0]);
+      res = sqrt(S.red[0]) * exp2((double)e);
       n_res++;
     }
     if (res <= target) {
@@ -1498,9 +1540,7 @@ __device__ __forceinline__ void implicit_one_step(Ctx<T, kGrid> &c, cg::grid_gro
     n_app++;
     group_sync<kGrid>(grid);  // Z_0 of every row visible before the SpMV
     if (rich) {  // x += M^-1 r
-      if (threadIdx.x == 0) coef[0] = (T)1;
-      __syncthreads();
-      ph_xupdate(c, 1, coef, Vout, x0_pending ? Vin : (const double *)nullptr);
+      ph_rich_update(c, Vout, x0_pending ? Vin : (const double *)nullptr);
       group_sync<kGrid>(grid);
       n_xup++;
       n_rich++;
