@@ -41,11 +41,11 @@ METRIC = "compartment-steps/s"
 
 # DRAM bytes (read + write) per compartment-step of the dominant kernel, from ncu captures
 # above L2 (profiles/ gives the commands): the explicit step on 1024 trees (21.9M elements)
-# moved 1.394 GB per launch; the implicit launch on 256 trees of 20k elements (5.12M)
-# moved 5.418 GB over 3 steps.  The traffic of a full-size step is scaled from these by the
+# moved 1.394 GB per launch; the implicit launch on 608 trees of 10k elements (6.08M)
+# moved 6.124 GB over 3 steps.  The traffic of a full-size step is scaled from these by the
 # compartments it processes.
 TRAFFIC_PER_ELEMENT_STEP = {"batch-explicit-mixed": 1.394e9 / 21910344,
-                            "batch-implicit-mixed": 5.418e9 / (3 * 5120180)}
+                            "batch-implicit-mixed": 6.124348e9 / (3 * 6081291)}
 WORKLOADS = ("batch-implicit-mixed", "batch-explicit-mixed", "batch-explicit-fp64",
              "axon-explicit-fp64", "myelin-explicit-mixed", "serve")
 DEFAULT_WORKLOAD = "batch-implicit-mixed"
@@ -459,7 +459,7 @@ def run_ours(args, rank: int, world: int, dist, wl: str, extras: bool = True, st
             "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
             "algorithmic_bytes_per_step": alg_all,
             "traffic_note": "DRAM bytes per step from an ncu capture above L2 (1024 trees "
-                            "explicit, 256 trees of 20k elements implicit), scaled by compartments"
+                            "explicit, 608 trees of 10k elements implicit), scaled by compartments"
                             if per_el else None}
     roof_passes = None
     if passes is not None:
