@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(256) explicit_step_f64(PackView p, int k, int 
 
 // Mixed precision (element j of step k; the body of explicit_step_mixed and of the chunk
 // kernel): gates, rates, conductances and currents in FP32; the potential is
-// accumulated in FP64.  GB300's FP64 pipe runs at 1/61 of the FP32 rate, so the stencil
+// accumulated in FP64.  GB300's FP64 pipe runs at 1/70 of the FP32 rate, so the stencil
 // reads an FP32 shadow of V (Vf = (float)V, refreshed from the FP64 value every step):
 // neighbour differences carry an absolute error of ~4e-9 V, while the FP64 accumulator
 // V' = V + dt-scaled current keeps long horizons free of drift.  FP64-pipe work is one

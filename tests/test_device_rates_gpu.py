@@ -123,3 +123,61 @@ def test_device_rates(tmp_path):
           f"{issue:.0f} cycles per copy")
     assert r32 > 20 * r64       # FP64 arithmetic is far below FP32 on this part
     assert 50 < issue < 5000    # a bulk copy keeps its issuing thread for hundreds of cycles
+
+
+COOP_SRC = r"""
+#include <cstdio>
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+namespace cg = cooperative_groups;
+// spins for a fixed number of clock cycles (waits on nothing else), then one grid sync
+__global__ void spin(long long cycles, int *out) {
+  cg::grid_group g = cg::this_grid();
+  const long long t0 = clock64();
+  while (clock64() - t0 < cycles) {}
+  g.sync();
+  if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(out, 1);
+}
+int main() {
+  int *out; cudaMalloc(&out, 4); cudaMemset(out, 0, 4);
+  cudaStream_t s[4];
+  for (int i = 0; i < 4; i++) cudaStreamCreateWithFlags(&s[i], cudaStreamNonBlocking);
+  long long cyc = 20000000;  // ~10 ms at 2 GHz
+  cudaEvent_t e0, e1; cudaEventCreate(&e0); cudaEventCreate(&e1);
+  float t[2];
+  for (int k = 0; k < 2; k++) {
+    const int n = k == 0 ? 1 : 4;
+    cudaDeviceSynchronize();
+    cudaEventRecord(e0, 0);
+    cudaDeviceSynchronize();
+    for (int i = 0; i < n; i++) {
+      void *args[] = {&cyc, &out};
+      cudaLaunchCooperativeKernel((void *)spin, 20, 256, args, 0, s[i]);
+    }
+    cudaDeviceSynchronize();
+    cudaEventRecord(e1, 0);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&t[k], e0, e1);
+  }
+  const cudaError_t err = cudaDeviceSynchronize();
+  printf("%.3f %.3f %s\n", t[0], t[1], err == cudaSuccess ? "ok" : cudaGetErrorString(err));
+  return err == cudaSuccess ? 0 : 1;
+}
+"""
+
+
+def test_cooperative_launches_overlap(tmp_path):
+    """Cooperative launches on different streams run at the same time (the server steps
+    each wide implicit request as a cooperative launch on its batch's own stream): four
+    20-CTA kernels that each spin ~10 ms take about as long as one."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    src = tmp_path / "coop.cu"
+    src.write_text(COOP_SRC)
+    exe = tmp_path / "coop"
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", str(src), "-o",
+                    str(exe)], check=True, capture_output=True, text=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    one, four = float(out[0]), float(out[1])
+    assert out[2] == "ok"
+    print(f"\none cooperative kernel {one:.2f} ms; four on four streams {four:.2f} ms")
+    assert four < 1.5 * one
