@@ -496,7 +496,8 @@ int nrt_server_destroy(nrt_server *s);
  * n * (2*restart + 6) + 2*1024*(NRT_STATIC_MAX_RESTART + 1) + 4 doubles (about 109,000 rows
  * at restart 16, 189,000 at restart 8); larger systems are refused with NRT_EBUDGET.
  * The first call on a device also looks up the array's device address (a one-time set-up
- * with that device current), so make that first call before any stream capture.
+ * with that device current).  No call can be captured into a CUDA graph: each one reads
+ * the iteration count back to the host and synchronises `stream` before it returns.
  * A system, right-hand side or initial guess holding NaN or Inf ends the solve with
  * NRT_EINVAL (x keeps its last finite iterate).  In relative mode a right-hand side that is
  * zero on every coupled row is measured over all rows, and one that is zero everywhere
