@@ -177,7 +177,7 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
   // sets in order of first appearance and each HH element's index among them.
   std::vector<char> fusable(count, 1), invariant(count, 1);
   std::vector<std::vector<HHKey>> local_keys(count);
-  std::vector<uint32_t> cls(N, 0);
+  hvec<uint32_t> cls(N);  // written per instance below (no serial zero fill)
   parallel_for(count, [&](int32_t i) {
     const nrt_problem &p = probs[i];
     const int64_t o = hp.off[i];
@@ -216,6 +216,7 @@ int build_host_pack(const nrt_problem *probs, int32_t count, HostPack &hp) {
       }
       t.flags = f | ((uint32_t)i << INST_SHIFT);
       hp.topo[o + j] = t;
+      cls[o + j] = 0;  // HH elements get their class below
       const double dx = p.dx[j], c_m = p.c_m[j], r_a = p.r_a[j];
       hp.cdt[o + j] = p.dT / (c_m * dx);     // dT/(c_m dX), src/solverEx-cpu.cpp:141
       hp.gax[o + j] = 1.0 / (r_a * dx);      // 1/(r_a dX)
@@ -378,12 +379,14 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   size_t bytes = 2 * al(8 * N) + al(sizeof(Topo) * N) + al(sizeof(InstDev) * count) +
                  al(8 * host.terms.size() + 8) + al(16);
   const size_t hpn = (size_t)HP_ROWS * host.hp_ld;
+  // the explicit step's coefficient rows (the implicit kernel reads its own FP64 rows)
+  const bool explicit_rows = opt.mode == NRT_EXPLICIT;
   if (!host.hp_cls.empty()) bytes += al(4 * N);
-  if (mixed && opt.mode == NRT_EXPLICIT) bytes += al(4 * N);  // flags of the compact step
+  if (mixed && explicit_rows) bytes += al(4 * N);  // flags of the compact step
   if (mixed)
-    bytes += 7 * al(4 * N) + al(4 * 3 * N) + al(4 * 12 * (size_t)host.hp_ld);
+    bytes += (explicit_rows ? 7 * al(4 * N) : 0) + al(4 * 3 * N) + al(4 * 12 * (size_t)host.hp_ld);
   else
-    bytes += 5 * al(8 * N) + al(8 * 3 * N) + al(8 * hpn);
+    bytes += (explicit_rows ? 5 * al(8 * N) : 0) + al(8 * 3 * N) + al(8 * hpn);
   if (opt.mode == NRT_IMPLICIT_BE) {
     size_t ib = 0;
     TRY(implicit_plan(ib));
@@ -400,8 +403,8 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
     hostf.emplace_back(host.V1.begin(), host.V1.end());
     TRY(upload(arena, Vf[1], hostf.back().data(), N, st));
   }
-  Topo *topo = nullptr;
-  TRY(upload(arena, topo, host.topo.data(), N, st));
+  Topo *topo = nullptr;  // the implicit set-up uploads it once it has set the row flags
+  TRY(upload(arena, topo, explicit_rows ? host.topo.data() : nullptr, N, st));
   InstDev *inst = nullptr;
   TRY(upload(arena, inst, host.inst.data(), count, st));
   TRY(upload(arena, terms, host.terms.data(), host.terms.size(), st));
@@ -413,7 +416,7 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
   pv.hh_dense = 2 * (int64_t)host.hh_local.size() >= N ? 1 : 0;
   pv.eflags = nullptr;
   if (mixed && opt.mode == NRT_EXPLICIT) {
-    std::vector<uint32_t> fl(N);
+    hvec<uint32_t> fl(N);  // every entry written below
     parallel_ranges(N, [&](int64_t a, int64_t b) {
       for (int64_t j = a; j < b; j++) fl[j] = host.topo[j].flags;
     });
@@ -451,11 +454,13 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
     };
     hostf.reserve(8);
     float *p;
-    TRY(upload(arena, p, f32(host.cdt), N, st)); pv.cdtf = p;
-    TRY(upload(arena, p, f32(host.gax), N, st)); pv.gaxf = p;
-    TRY(upload(arena, p, f32(host.wdx), N, st)); pv.wdxf = p;
-    TRY(upload(arena, p, f32(host.kdx), N, st)); pv.kdxf = p;
-    TRY(upload(arena, p, f32(host.inp), N, st)); pv.inpf = p;
+    if (explicit_rows) {
+      TRY(upload(arena, p, f32(host.cdt), N, st)); pv.cdtf = p;
+      TRY(upload(arena, p, f32(host.gax), N, st)); pv.gaxf = p;
+      TRY(upload(arena, p, f32(host.wdx), N, st)); pv.wdxf = p;
+      TRY(upload(arena, p, f32(host.kdx), N, st)); pv.kdxf = p;
+      TRY(upload(arena, p, f32(host.inp), N, st)); pv.inpf = p;
+    }
     TRY(upload(arena, p, f32(host.gate), 3 * N, st)); pv.gatef = p;
     {  // the parameter table by column: 12 floats (HP_* rows and a pad) per column
       const int64_t L = host.hp_ld;
@@ -469,11 +474,13 @@ int Engine::init(const nrt_problem *probs, int32_t count, const nrt_options *o) 
     }
   } else {
     double *p;
-    TRY(upload(arena, p, host.cdt.data(), N, st)); pv.cdt = p;
-    TRY(upload(arena, p, host.gax.data(), N, st)); pv.gax = p;
-    TRY(upload(arena, p, host.wdx.data(), N, st)); pv.wdx = p;
-    TRY(upload(arena, p, host.kdx.data(), N, st)); pv.kdx = p;
-    TRY(upload(arena, p, host.inp.data(), N, st)); pv.inp = p;
+    if (explicit_rows) {
+      TRY(upload(arena, p, host.cdt.data(), N, st)); pv.cdt = p;
+      TRY(upload(arena, p, host.gax.data(), N, st)); pv.gax = p;
+      TRY(upload(arena, p, host.wdx.data(), N, st)); pv.wdx = p;
+      TRY(upload(arena, p, host.kdx.data(), N, st)); pv.kdx = p;
+      TRY(upload(arena, p, host.inp.data(), N, st)); pv.inp = p;
+    }
     TRY(upload(arena, p, host.gate.data(), 3 * N, st)); pv.gate = p;
     TRY(upload(arena, p, host.hp.data(), hpn, st)); pv.hp = p;
   }

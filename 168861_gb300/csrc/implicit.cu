@@ -1735,18 +1735,18 @@ __global__ void __launch_bounds__(kThreads, 4) implicit_steps(const PackView *pv
 // CTA of the cooperative launch, or one instance of a batch) gets, per level (deepest
 // first), tiles of whole segments whose slots fit the shared-memory staging area; every
 // tile starts on a multiple of 16 slots (padding slots in between have row -1).
-struct TreeSchedule {
-  std::vector<int> seg_len, seg_c1, seg_c2, seg_prow, seg_soff;  // tile order
-  std::vector<int> tile_seg, tile_slot, slot_row, lev_tile, work_lev;
-  std::vector<uint8_t> slot_flag;
+struct TreeSchedule {  // sized without a fill: every entry is written by the builders
+  hvec<int> seg_len, seg_c1, seg_c2, seg_prow, seg_soff;  // tile order
+  hvec<int> tile_seg, tile_slot, slot_row, lev_tile, work_lev;
+  hvec<uint8_t> slot_flag;
 };
 
 struct ImplicitState {
   ImView iv{};
   PackView *d_pv = nullptr;  // device copies the kernel reads
   ImView *d_iv = nullptr;
-  std::vector<uint8_t> rowf;
-  std::vector<int2> pieces;
+  hvec<uint8_t> rowf;  // sized without a fill: implicit_plan writes every row
+  hvec<int2> pieces;
   std::vector<int> tiles, cta_row, cta_tile, inst_tile, order;
   std::vector<int64_t> inst_row;
   TreeSchedule tree;
@@ -2024,7 +2024,7 @@ static void build_tree_schedule_batch(const HostPack &host, int cap, TreeSchedul
 }
 
 // Groups pieces [pa, pb) into tiles whose row span fits the shared-memory staging area.
-static void make_tiles(const std::vector<int2> &pieces, int pa, int pb, int tile_rows,
+static void make_tiles(const hvec<int2> &pieces, int pa, int pb, int tile_rows,
                        std::vector<int> &tiles) {
   int64_t start_row = -1;
   for (int p = pa; p < pb; p++) {
@@ -2047,9 +2047,7 @@ int Engine::implicit_plan(size_t &bytes) {
   const int32_t ni = host.ninst;
   // Row structure (flags) per element.  The validator guaranteed the reference
   // numbering: mother < j, DR == j + 1 off terminals, terminals follow their mother.
-  std::vector<char> is_term(N, 0);
-  for (int64_t t : host.terms) is_term[t] = 1;
-  S.rowf.assign(N, R_IDENT);
+  S.rowf.resize(N);
   parallel_for(ni, [&](int64_t i) {
     const int64_t o = host.off[i], n = host.num_elem[i];
     for (int64_t jl = 0; jl < n; jl++) {
@@ -2058,7 +2056,7 @@ int Engine::implicit_plan(size_t &bytes) {
       t.flags &= ~(uint32_t)(F_UP | F_DOWNR | F_DOWNL | F_IDENT);
       uint8_t rf = (t.flags & F_HH) ? R_HH : 0;
       if (host.inp[j] != 0.0) rf |= R_INP;
-      const bool ident = jl == 0 || jl == n - 1 || is_term[j];
+      const bool ident = jl == 0 || jl == n - 1 || (t.flags & F_TERM);
       if (ident) {
         t.flags |= F_IDENT;
         S.rowf[j] = rf | R_IDENT;
@@ -2069,7 +2067,7 @@ int Engine::implicit_plan(size_t &bytes) {
         rf |= R_UP;
         if (t.mother != j - 1) rf |= R_FAR;
       }
-      if (!is_term[j + 1]) {
+      if (!(host.topo[j + 1].flags & F_TERM)) {  // j + 1 is in this instance (j < o + n - 1)
         t.flags |= F_DOWNR;
         rf |= R_DOWNR;
       }
@@ -2238,29 +2236,24 @@ int Engine::implicit_init() {
   iv.tile_rows = S.tile_rows;
   uint8_t *pr;
   TRYI(up(arena, pr, S.rowf.data(), N, st)); iv.rowf = pr;
-  // staging buffers filled in parallel (no zero fill first)
-  std::unique_ptr<double[]> cmdt_b(new double[N]), g64_b(new double[N]), w64_b(new double[N]),
-      k64_b(new double[N]), inp_b(new double[N]);
+  // c_m dX / dT and the FP32 conductances are staged (filled in parallel, no zero fill
+  // first); the other FP64 rows go up straight from the host pack
+  std::unique_ptr<double[]> cmdt_b(new double[N]);
   std::unique_ptr<float[]> gf_b(new float[N]);
-  double *cmdt = cmdt_b.get(), *g64 = g64_b.get(), *w64 = w64_b.get(), *k64 = k64_b.get(),
-         *inp = inp_b.get();
+  double *cmdt = cmdt_b.get();
   float *gf = gf_b.get();
   parallel_ranges(N, [&](int64_t a, int64_t b) {
     for (int64_t j = a; j < b; j++) {
       cmdt[j] = host.c_m_dx[j] / host.inst[host.topo[j].flags >> INST_SHIFT].dT;
-      g64[j] = host.gax[j];
       gf[j] = (float)host.gax[j];
-      w64[j] = host.wdx[j];
-      k64[j] = host.kdx[j];
-      inp[j] = host.inp[j];
     }
   });
   double *p;
   TRYI(up(arena, p, cmdt, N, st)); iv.cmdt = p;
-  TRYI(up(arena, p, g64, N, st)); iv.g64 = p;
-  TRYI(up(arena, p, w64, N, st)); iv.wdx64 = p;
-  TRYI(up(arena, p, k64, N, st)); iv.kdx64 = p;
-  TRYI(up(arena, p, inp, N, st)); iv.inp64 = p;
+  TRYI(up(arena, p, host.gax.data(), N, st)); iv.g64 = p;
+  TRYI(up(arena, p, host.wdx.data(), N, st)); iv.wdx64 = p;
+  TRYI(up(arena, p, host.kdx.data(), N, st)); iv.kdx64 = p;
+  TRYI(up(arena, p, host.inp.data(), N, st)); iv.inp64 = p;
   TRYI(up(arena, iv.diag, (const double *)nullptr, N, st));
   TRYI(up(arena, iv.rhs, (const double *)nullptr, N, st));
   float *pf;

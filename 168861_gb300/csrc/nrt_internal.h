@@ -211,7 +211,7 @@ struct HostPack {
   hvec<double> gate;                // [3][ntot]
   std::vector<double> hp;           // [HP_ROWS][hp_ld]
   bool hp_inst = false;             // one HH parameter column per instance
-  std::vector<uint32_t> hp_cls;     // column per element when classes are used
+  hvec<uint32_t> hp_cls;            // column per element when classes are used
   int64_t hp_ld = 0;
   hvec<double> c_m_dx, radx;        // c_m dX and r_a dX per element (implicit assembly)
   hvec<double> Wfull, Kfull;        // W, K per element as given

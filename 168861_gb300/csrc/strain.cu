@@ -222,7 +222,7 @@ int Engine::strain_config(const nrt_strain_config *c) {
     std::vector<double> hp((size_t)HP_ROWS * L1);
     for (int r = 0; r < HP_ROWS; r++)
       for (int64_t cc = 0; cc < L0; cc++) hp[(size_t)r * L1 + cc] = host.hp[(size_t)r * L0 + cc];
-    std::vector<uint32_t> cls(N);
+    hvec<uint32_t> cls(N);  // every entry written below
     for (int32_t i = 0; i < host.ninst; i++)
       for (int64_t j = host.off[i]; j < host.off[i + 1]; j++)
         cls[j] = host.hp_cls.empty() ? (uint32_t)i : host.hp_cls[j];
