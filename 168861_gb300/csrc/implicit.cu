@@ -140,6 +140,8 @@ struct ImView {
   void *sinv, *se, *sy;           // T per slot: 1 / pivot, g / pivot, eliminated right side
   void *exp_d, *exp_b;            // T per segment: what it passes to its parent row
   int tree_cap;                   // staging slots per tree tile (multiple of 16)
+  int local_top;                  // one tree: levels 0 .. local_top all belong to CTA 0, which
+                                  // passes between them with CTA barriers only (-1: none)
 };
 
 template <typename T>
@@ -733,7 +735,9 @@ __device__ __noinline__ void tree_factor(Ctx<T, kGrid> c) {
       fence_proxy_async();  // the solves read sinv / se back with bulk copies
       __syncthreads();
     }
-    level_sync<kGrid>(grid);
+    // entry e is level c.l1 - 1 - e; the next (shallower) one is CTA 0's alone when this
+    // one is (every CTA evaluates the same test, so all take the same grid syncs)
+    if (c.l1 - 1 - e > iv.local_top) level_sync<kGrid>(grid);
   }
 }
 
@@ -773,7 +777,8 @@ __device__ __noinline__ void tree_apply(Ctx<T, kGrid> c, const T *v, T *z) {
       fence_proxy_async();  // the substitution reads sy back with bulk copies
       __syncthreads();
     }
-    level_sync<kGrid>(grid);
+    // as in tree_factor; after level 0 the substitution starts at level 0, in CTA 0
+    if (c.l1 - 1 - e > iv.local_top) level_sync<kGrid>(grid);
   }
   // substitution, root level first: x_k = inv_k y_k + e_k x_{k-1} (x_mother on a first row)
   for (int e = c.l1 - 1; e >= c.l0; e--) {
@@ -798,7 +803,8 @@ __device__ __noinline__ void tree_apply(Ctx<T, kGrid> c, const T *v, T *z) {
       tile_scatter(z, t.r, t.a, cnt);
       __syncthreads();
     }
-    level_sync<kGrid>(grid);
+    // the next (deeper) level is CTA 0's alone when it is within the top levels
+    if (c.l1 - 1 - e >= iv.local_top) level_sync<kGrid>(grid);
   }
 }
 
@@ -1739,6 +1745,7 @@ struct TreeSchedule {  // sized without a fill: every entry is written by the bu
   hvec<int> seg_len, seg_c1, seg_c2, seg_prow, seg_soff;  // tile order
   hvec<int> tile_seg, tile_slot, slot_row, lev_tile, work_lev;
   hvec<uint8_t> slot_flag;
+  int local_top = -1;  // ImView::local_top
 };
 
 struct ImplicitState {
@@ -1826,12 +1833,23 @@ static void build_tree_schedule(const HostPack &host, int cap, bool grid_mode, i
     std::vector<std::vector<int>> by_level(max_level + 1);
     for (int s = 0; s < (int)segs.size(); s++) by_level[segs[s].level].push_back(s);
     for (int w = 0; w < nwork; w++) lists[w].resize(max_level + 1);
+    std::vector<int64_t> level_rows(max_level + 1, 0);
+    for (int L = 0; L <= max_level; L++)
+      for (int s : by_level[L]) level_rows[L] += segs[s].len;
+    // The top levels, while together they fit one tile, all go to CTA 0: a grid-wide sync
+    // between two of them would wait on CTAs that have nothing to do there.
+    int64_t top_rows = 0;
+    T.local_top = -1;
+    for (int L = 0; L <= max_level && top_rows + level_rows[L] <= cap; L++) {
+      top_rows += level_rows[L];
+      T.local_top = L;
+    }
     for (int L = 0; L <= max_level; L++) {
-      int64_t rows = 0;
-      for (int s : by_level[L]) rows += segs[s].len;
       int64_t acc = 0;
       for (int s : by_level[L]) {
-        const int w = (int)std::min<int64_t>(nwork - 1, acc * nwork / std::max<int64_t>(rows, 1));
+        const int w = L <= T.local_top ? 0
+                                       : (int)std::min<int64_t>(nwork - 1, acc * nwork /
+                                                                std::max<int64_t>(level_rows[L], 1));
         lists[w][L].push_back(s);
         acc += segs[s].len;
       }
@@ -2174,6 +2192,7 @@ int Engine::implicit_plan(size_t &bytes) {
   }
   S.tiles.push_back(np);  // sentinel: end piece of the last tile
   const bool tree = opt.precond == NRT_PRECOND_TREE;
+  S.iv.local_top = -1;
   if (tree) {
     // staging slots: three T rows, the slot row and the slot flag per slot
     S.iv.tree_cap = (int)(kTileBytes / (3 * tb + 5)) & ~15;
@@ -2181,6 +2200,7 @@ int Engine::implicit_plan(size_t &bytes) {
       build_tree_schedule(host, S.iv.tree_cap, true, S.grid_blocks, S.tree);
     else
       build_tree_schedule_batch(host, S.iv.tree_cap, S.tree);
+    S.iv.local_top = S.tree.local_top;
   }
   // device bytes, in the order implicit_init takes them
   const int m = opt.restart;
