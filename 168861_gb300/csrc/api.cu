@@ -660,14 +660,35 @@ int Engine::advance(int64_t steps) {
       NRT_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
       int rc = NRT_OK;
       const bool tabled = strain_tabled(*this);
+      // mixed steps write the strained rows of the step after them (StrainFold): one row
+      // write per chunk instead of one launch per step; the coefficient rows and the
+      // parameter table alternate between two copies by the step's parity
+      const StrainView *sv = strain_view(*this);
+      const bool fold = tabled && opt.precision == NRT_MIXED && sv && sv->alt_gaxf;
+      PackView alt = pv;
+      if (fold) {
+        alt.cdtf = sv->alt_cdtf;
+        alt.gaxf = sv->alt_gaxf;
+        alt.wdxf = sv->alt_wdxf;
+        alt.kdxf = sv->alt_kdxf;
+        alt.hpq = sv->alt_hpq;
+      }
       if (tabled) rc = launch_strain_derive(*this, kChunk, stream);
       for (int k = 0; k < kChunk && rc == NRT_OK; k++) {
-        if (strain)
+        if (strain && (!fold || k == 0))
           rc = tabled ? launch_strain_apply(*this, k, stream) : launch_strain_update(*this, k, stream);
         if (rc != NRT_OK) break;
-        rc = launch_explicit_step(pv, opt.precision, false, k, -1, V[(cur + k) & 1],
+        const PackView &pk = fold && (k & 1) ? alt : pv;
+        StrainFold f{};
+        f.row = -1;
+        if (fold && k + 1 < kChunk) {
+          f.s = *sv;
+          f.next = (k + 1) & 1 ? alt : pv;
+          f.row = k + 1;
+        }
+        rc = launch_explicit_step(pk, opt.precision, false, k, -1, V[(cur + k) & 1],
                                   V[(cur + k + 1) & 1], Vf[(cur + k) & 1], Vf[(cur + k + 1) & 1],
-                                  stream);
+                                  stream, fold ? &f : nullptr);
         if (rc == NRT_OK && rec)
           rc = launch_record_step(rec_view_host(), pv.inst, k, V[(cur + k + 1) & 1], stream);
       }

@@ -210,9 +210,14 @@ __global__ void __launch_bounds__(256) explicit_step_mixed(PackView p, int k, in
                                                            const double *__restrict__ Vin,
                                                            double *__restrict__ Vout,
                                                            const float *__restrict__ Fin,
-                                                           float *__restrict__ Fout) {
+                                                           float *__restrict__ Fout,
+                                                           StrainFold fold) {
   chain_acquire();  // the previous launch of the time loop has finished
   chain_release();
+  if (fold.row >= 0 && (int)blockIdx.x >= fold.first_block) {
+    fold_rows(fold);  // the next step's strained rows, into the other copy
+    return;
+  }
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= p.ntot) return;
   mixed_element<kGeneral>(p, k, force, j, Vin, Vout, Fin, Fout);
@@ -399,9 +404,15 @@ constexpr int kTileWarps = kTileThreads / 32;
 
 __global__ void __launch_bounds__(kTileThreads) explicit_step_mixed_tiled(
     PackView p, int k, int force, const double *__restrict__ Vin, double *__restrict__ Vout,
-    const float *__restrict__ Fin, float *__restrict__ Fout) {
+    const float *__restrict__ Fin, float *__restrict__ Fout, StrainFold fold) {
   chain_acquire();  // the previous launch of the time loop has finished
   chain_release();
+  if (fold.row >= 0 && (int)blockIdx.x >= fold.first_block) {
+    fold_rows(fold);  // the next step's strained rows, into the other copy
+    return;
+  }
+  // the CTAs that walk tiles (the others write strain rows)
+  const int nblk = fold.row >= 0 ? fold.first_block : (int)gridDim.x;
   extern __shared__ __align__(16) unsigned char tsm[];
   uint64_t *full = (uint64_t *)(tsm + 2 * kTileBufBytes);
   uint64_t *empty = full + 2;
@@ -426,8 +437,8 @@ __global__ void __launch_bounds__(kTileThreads) explicit_step_mixed_tiled(
   }
   int b = 0;
   bool first = true;
-  for (; t < ntiles; t += gridDim.x) {
-    const int64_t tn = t + gridDim.x;
+  for (; t < ntiles; t += nblk) {
+    const int64_t tn = t + nblk;
     bool ok = true;
     if (issuer && tn < ntiles) {
       const int nb = b ^ 1;
@@ -590,7 +601,13 @@ __global__ void advance_base(InstDev *inst, int32_t ninst, int64_t steps) {
 
 int launch_explicit_step(const PackView &pv, int precision, bool general, int k, int force,
                          const double *Vin, double *Vout, const float *Fin, float *Fout,
-                         cudaStream_t st) {
+                         cudaStream_t st, const StrainFold *fold) {
+  StrainFold f{};
+  f.row = -1;
+  if (fold && precision == NRT_MIXED && !general) f = *fold;
+  // CTAs that write the next step's strained rows, after the ones that step
+  const unsigned fold_blocks =
+      f.row >= 0 ? (unsigned)std::min(64, (f.s.n + kTileThreads - 1) / kTileThreads) : 0u;
   // Small trees: spread the elements over as many SMs as possible (the FP64 pipe of one
   // SM, not memory, bounds a small block); large packs: 256-thread blocks.
   int threads = 256;
@@ -598,12 +615,19 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
   if (pv.step_threads > 0) threads = pv.step_threads;  // a tuned shape (same results)
   const unsigned blocks = (unsigned)((pv.ntot + threads - 1) / threads);
   if (precision == NRT_MIXED) {
-    if (!general && pv.tile_blocks > 0 && pv.eflags && pv.err)
-      NRT_CUDA(launch_chained(explicit_step_mixed_tiled, pv.tile_blocks, kTileThreads,
-                              2 * kTileBufBytes + 32, st, pv, k, force, Vin, Vout, Fin, Fout));
-    else
+    if (!general && pv.tile_blocks > 0 && pv.eflags && pv.err) {
+      f.first_block = pv.tile_blocks;
+      NRT_CUDA(launch_chained(explicit_step_mixed_tiled, pv.tile_blocks + fold_blocks,
+                              kTileThreads, 2 * kTileBufBytes + 32, st, pv, k, force, Vin, Vout,
+                              Fin, Fout, f));
+    } else {
+      f.first_block = (int)blocks;
       NRT_CUDA(launch_chained(general ? explicit_step_mixed<true> : explicit_step_mixed<false>,
-                              blocks, threads, 0, st, pv, k, force, Vin, Vout, Fin, Fout));
+                              blocks + (f.row >= 0 ? (unsigned)std::min(64, (f.s.n + threads - 1) /
+                                                                                   threads)
+                                                   : 0u),
+                              threads, 0, st, pv, k, force, Vin, Vout, Fin, Fout, f));
+    }
   } else {
     NRT_CUDA(launch_chained(general ? explicit_step_f64<true> : explicit_step_f64<false>, blocks,
                             threads, 0, st, pv, k, force, Vin, Vout));

@@ -245,10 +245,12 @@ __host__ __device__ inline int64_t hp_col(const PackView &p, int64_t j, uint32_t
   return p.hp_cls ? (int64_t)p.hp_cls[j] : (p.hp_inst ? (int64_t)inst : j);
 }
 
-// Kernel launchers (explicit.cu).
+// Kernel launchers (explicit.cu).  fold (mixed, fused form; strain.cuh): the step also
+// writes the strained elements' coefficients of the next step.
+struct StrainFold;
 int launch_explicit_step(const PackView &pv, int precision, bool general, int k, int force,
                          const double *Vin, double *Vout, const float *Fin, float *Fout,
-                         cudaStream_t st);
+                         cudaStream_t st, const StrainFold *fold = nullptr);
 int launch_terminal_fixup(const Topo *topo, const int64_t *terms, int64_t nterm, double *V,
                           float *Vf, cudaStream_t st);
 int launch_advance_base(InstDev *inst, int32_t ninst, int64_t steps, cudaStream_t st);

@@ -303,9 +303,14 @@ int Engine::strain_config(const nrt_strain_config *c) {
   // step derives its own coefficients
   const size_t tab_entries = (size_t)kChunk * ncls;
   const bool tabled = tab_entries * (8 * kStrainOut + 4) <= ((size_t)64 << 20);
+  // mixed, with the table: a second copy of the coefficient rows and of the parameter
+  // table, for the steps of a graph chunk that write the next step's rows (StrainFold)
+  const bool alt = tabled && mixed;
+  auto rnd = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t fold_bytes = alt ? 4 * rnd(4 * (size_t)N) + rnd(48 * (size_t)pv.hp_ld) : 0;
   const size_t bytes = 8 * (size_t)n * 2 + 4 * (size_t)n + 4 * (size_t)ncls * 2 +
                        8 * c_spec.size() +
-                       (tabled ? tab_entries * (8 * kStrainOut + 4) : 0) + 256 * 8;
+                       (tabled ? tab_entries * (8 * kStrainOut + 4) : 0) + fold_bytes + 256 * 8;
   if (cudaMalloc(&S->mem, bytes) != cudaSuccess) {
     cudaGetLastError();
     set_error("device allocation for the strain");
@@ -324,6 +329,11 @@ int Engine::strain_config(const nrt_strain_config *c) {
   double *d_spec = (double *)take(8 * c_spec.size());
   v.tab = tabled ? (double *)take(8 * kStrainOut * tab_entries) : nullptr;
   v.tlive = tabled ? (int32_t *)take(4 * tab_entries) : nullptr;
+  v.alt_cdtf = alt ? (float *)take(4 * (size_t)N) : nullptr;
+  v.alt_gaxf = alt ? (float *)take(4 * (size_t)N) : nullptr;
+  v.alt_wdxf = alt ? (float *)take(4 * (size_t)N) : nullptr;
+  v.alt_kdxf = alt ? (float *)take(4 * (size_t)N) : nullptr;
+  v.alt_hpq = alt ? (float4 *)take(48 * (size_t)pv.hp_ld) : nullptr;
   NRT_CUDA(cudaMemcpyAsync(d_elem, s_elem.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, stream));
   NRT_CUDA(cudaMemcpyAsync(d_col, s_col.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, stream));
   NRT_CUDA(cudaMemcpyAsync(d_cls, s_cls.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, stream));
@@ -348,6 +358,15 @@ int Engine::strain_config(const nrt_strain_config *c) {
   v.eps1 = c->eps1;
   v.t0 = c->t0;
   v.t1 = c->t1;
+  if (alt) {  // unstrained elements keep the same coefficients in both copies for good
+    const auto d2d = cudaMemcpyDeviceToDevice;
+    NRT_CUDA(cudaMemcpyAsync(v.alt_cdtf, pv.cdtf, 4 * (size_t)N, d2d, stream));
+    NRT_CUDA(cudaMemcpyAsync(v.alt_gaxf, pv.gaxf, 4 * (size_t)N, d2d, stream));
+    NRT_CUDA(cudaMemcpyAsync(v.alt_wdxf, pv.wdxf, 4 * (size_t)N, d2d, stream));
+    NRT_CUDA(cudaMemcpyAsync(v.alt_kdxf, pv.kdxf, 4 * (size_t)N, d2d, stream));
+    NRT_CUDA(cudaMemcpyAsync(v.alt_hpq, pv.hpq, 48 * (size_t)pv.hp_ld, d2d, stream));
+  }
+  NRT_CUDA(cudaStreamSynchronize(stream));
   strain = S.release();
   return NRT_OK;
 }

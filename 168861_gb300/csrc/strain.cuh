@@ -21,8 +21,23 @@ struct StrainView {
   const double *spec;    // [10][ncls]: dX, diameter, ro_a, ro_m, per_m, thickness, rest, sigma_Na, sigma_K, sigma_L
   double *tab;           // [kChunk][ncls][kStrainOut] derived ahead for a chunk of steps, or null
   int32_t *tlive;        // [kChunk][ncls]: the class's instance still runs at that step
+  // mixed, with the table: the second copy of the coefficient rows and parameter table
+  // that a graph chunk's odd steps read (the even steps read the pack's own)
+  float *alt_cdtf, *alt_gaxf, *alt_wdxf, *alt_kdxf;
+  float4 *alt_hpq;
   int32_t myelin;
   double e_max, eps0, eps1, t0, t1;
+};
+
+// A step that also writes the strained elements' coefficients of the next step (mixed
+// explicit steps of a graph chunk).  The step's CTAs from first_block on do that instead of
+// elements, at the same time as the others step.  Step k reads the copy of its parity and
+// writes row k + 1 into the other (`next`), so no element of a step sees a value of the next.
+struct StrainFold {
+  StrainView s;
+  PackView next;     // the pack with the coefficient copy step k + 1 reads
+  int row;           // table row written (k + 1 of the chunk), or -1: none
+  int first_block;   // the first CTA that writes rows
 };
 
 constexpr int kStrainOut = 2 + HP_ROWS;  // dT/(c_m dX), 1/(r_a dX), then W dX, K dX or the column
@@ -60,6 +75,14 @@ __device__ __forceinline__ void apply_row(const StrainView &s, const PackView &p
                                           int mixed) {
   const int64_t g = (int64_t)k * s.ncls + s.cls[q];
   if (s.tlive[g]) apply_element(s, p, q, s.tab + g * kStrainOut, mixed);
+}
+
+// The row-writing CTAs of a folded step: every strained element's row for the next step.
+__device__ __forceinline__ void fold_rows(const StrainFold &f) {
+  const int nb = gridDim.x - f.first_block;
+  for (int q = (blockIdx.x - f.first_block) * blockDim.x + threadIdx.x; q < f.s.n;
+       q += nb * blockDim.x)
+    apply_row(f.s, f.next, q, f.row, 1);
 }
 
 }  // namespace nrt

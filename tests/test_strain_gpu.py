@@ -144,3 +144,32 @@ def test_strain_needs_the_explicit_stepper(gpu, pkg, model):
     with pytest.raises(pkg.NeuriteError):
         s.set_strain(spec, [5, 6], 0.0, 0.1, 0.0, 1e-3)
     s.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("tree", ["myelin", "tree"])
+def test_strain_graph_chunks_equal_single_steps(gpu, pkg, model, precision, tree):
+    """The captured time loop (a row table derived per 64-step chunk; in mixed precision each
+    step also writes the strained rows of the next step, with 1/(r_a dX) alternating between
+    two buffers) gives bit for bit what one launch per step with its own derivation gives,
+    over ranges that end inside a chunk and several whole chunks."""
+    build, pick = TREES[tree]
+    spec = build(model)
+    seg = pick(spec)
+    dT = step_size(pkg, spec, seg, 0.2)
+    t0, t1 = 50 * dT, 700 * dT
+    out = []
+    for graphs in (True, False):
+        s = pkg.SolverEx(pkg.ProblemArrays.from_spec(spec, pkg.derive(spec), dT),
+                         precision=precision, use_graphs=graphs)
+        s.set_strain(spec, seg, 0.0, 0.2, t0, t1)
+        s.record([1, spec.n // 2], interval=3, capacity=400)
+        s.run(1, 1 + 101, spec.init_time, spec.end_input)
+        s.run(102, 102 + 900, spec.init_time, spec.end_input)
+        out.append((s.get_state(), s.recording()))
+        s.close()
+    (a, ra), (b, rb) = out
+    np.testing.assert_array_equal(a.V, b.V)
+    np.testing.assert_array_equal(a.m, b.m)
+    for c in range(2):
+        np.testing.assert_array_equal(ra.values[c], rb.values[c])
