@@ -66,9 +66,9 @@ constexpr int kMaxPiece = 256;                 // longest segment piece one swee
 constexpr int kMaxDots = kMaxRestart + 1;
 constexpr int kTileBytes = 44 * 1024;          // shared-memory staging for the sweeps
 constexpr int kU = 4;                          // rows per thread in flight: SpMV + products
-constexpr int kV = 8;                          // rows per thread in flight: streaming passes
+constexpr int kV = 4;                          // rows per thread in flight: streaming passes
 constexpr int kA = 1;                          // rows per thread in flight: assembly
-constexpr int kR = 4;                          // rows per thread in flight: FP64 residual
+constexpr int kR = 2;                          // rows per thread in flight: FP64 residual
 constexpr int kG = 8;                          // Gram-Schmidt products per pass over the rows
 
 // Per-row flags of the implicit system (ImView::rowf).
