@@ -9,8 +9,11 @@ arithmetic is the same whatever the grid):
 
 Which one is fastest depends on the tree sizes, the share of HH compartments and the
 device, so `tune` times every candidate on the workload itself. It uses a sample of the
-trees (the first ones, up to `sample_elements` compartments) in a batch of its own, so the
-caller's state is never touched. It keeps the fastest. Results are cached in a JSON file
+trees in a batch of its own, so the caller's state is never touched: every k-th tree, which
+keeps the workload's mix of sizes, about `sample_elements` compartments but (implicit) at
+least `min_trees` trees, enough one-tree CTAs to fill every SM at the largest CTA count
+searched (a sample of a few large trees leaves most SMs idle, and then every CTA count times
+the same). It keeps the fastest. Results are cached in a JSON file
 per device, mode, precision and workload size, so a workload is tuned once per machine.
 
 The implicit block-per-instance kernel (batches) has one shape-only knob: how many of its
@@ -58,15 +61,14 @@ def choose(times: list[float]) -> int:
     return best
 
 
-def sample(problems, sample_elements: float) -> list:
-    """The first trees, up to sample_elements compartments (at least one tree)."""
-    out, total = [], 0
-    for p in problems:
-        if out and total + p.num_elem > sample_elements:
-            break
-        out.append(p)
-        total += p.num_elem
-    return out
+def sample(problems, sample_elements: float, min_trees: int = 1) -> list:
+    """Every k-th tree from the first: about sample_elements compartments, and at least
+    min_trees trees (all of them when there are no more)."""
+    n = len(problems)
+    total = sum(p.num_elem for p in problems)
+    k = max(1, math.ceil(total / max(sample_elements, 1)))
+    k = min(k, max(1, n // max(min_trees, 1)))
+    return list(problems[::k])
 
 
 def workload_key(device: str, mode: int, precision: str, problems, restarts=None) -> str:
@@ -132,16 +134,19 @@ def _store(path: str, cache: dict) -> None:
 
 
 def tune(problems, mode: int = _lib.NRT_EXPLICIT, precision: str = "fp64", *,
-         steps: int = 64, warmup: int = 3, sample_elements: float = 4e6, restarts=None,
-         cache: str | None = None, timer=None, device_key: str | None = None,
+         steps: int = 64, warmup: int = 3, sample_elements: float = 4e6, min_trees: int = 0,
+         restarts=None, cache: str | None = None, timer=None, device_key: str | None = None,
          **opts) -> dict:
     """The fastest launch shape for `problems`: {"options": overrides, "key": cache key,
     "times": seconds per step of each candidate (None when served from the cache),
     "candidates": the shapes searched}.
 
     timer(problems, mode, precision, overrides) -> seconds per step replaces the device
-    timing (tests use it); device_key replaces the device's name in the cache key.  `opts`
-    are the caller's other options (make_options keywords), kept fixed."""
+    timing (tests use it); device_key replaces the device's name in the cache key.
+    min_trees: the sample's fewest trees (0: 1024 for the implicit kernel, whose CTAs each
+    take one tree -- 4 CTAs on each of up to 256 SMs; 1 for the explicit steps, which tile
+    the elements).  `opts` are the caller's other options (make_options keywords), kept
+    fixed."""
     cands = candidates(mode, precision, restarts)
     dev = device_key if device_key is not None else device_name(int(opts.get("device", -1)))
     key = workload_key(dev, mode, precision, problems, restarts)
@@ -152,7 +157,9 @@ def tune(problems, mode: int = _lib.NRT_EXPLICIT, precision: str = "fp64", *,
         return {"options": dict(hit["options"]), "key": key, "times": None, "candidates": cands}
     if len(cands) == 1:
         return {"options": dict(cands[0]), "key": key, "times": [None], "candidates": cands}
-    part = sample(problems, sample_elements)
+    if min_trees <= 0:
+        min_trees = 1 if mode == _lib.NRT_EXPLICIT else 1024
+    part = sample(problems, sample_elements, min_trees)
     if timer is None:
         def timer(ps, m, prec, ov):
             return time_candidate(ps, m, prec, ov, steps, warmup, **opts)

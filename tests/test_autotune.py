@@ -33,10 +33,18 @@ def test_choose():
 
 
 def test_sample():
+    """A stride through the trees (the size mix kept), about sample_elements compartments,
+    at least min_trees trees."""
     trees = [Tree(n) for n in (1000, 3000, 5000, 100)]
-    assert [t.num_elem for t in at.sample(trees, 4000)] == [1000, 3000]
+    assert [t.num_elem for t in at.sample(trees, 4600)] == [1000, 5000]  # every 2nd
     assert [t.num_elem for t in at.sample(trees, 10)] == [1000]  # at least one tree
     assert len(at.sample(trees, 1e9)) == 4
+    assert len(at.sample(trees, 10, min_trees=2)) == 2
+    many = [Tree(n) for n in range(1000, 5096)]  # 4096 trees of rising size
+    part = at.sample(many, 4e6 / 22)
+    sizes = [t.num_elem for t in part]
+    assert sizes[0] == 1000 and sizes[-1] > 5000 and len(part) < 100  # small to large
+    assert len(at.sample(many, 4e6 / 22, min_trees=1024)) >= 1024
 
 
 def test_key_separates_devices_modes_and_sizes():
