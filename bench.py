@@ -42,10 +42,10 @@ METRIC = "compartment-steps/s"
 # DRAM bytes (read + write) per compartment-step of the dominant kernel, from ncu captures
 # above L2 (profiles/ gives the commands): the explicit step on 1024 trees (21.9M elements)
 # moved 1.394 GB per launch; the implicit launch on 608 trees of 10k elements (6.08M)
-# moved 6.124 GB over 3 steps.  The traffic of a full-size step is scaled from these by the
+# moved 3.720 GB over 3 steps.  The traffic of a full-size step is scaled from these by the
 # compartments it processes.
 TRAFFIC_PER_ELEMENT_STEP = {"batch-explicit-mixed": 1.394e9 / 21910344,
-                            "batch-implicit-mixed": 6.124348e9 / (3 * 6081291)}
+                            "batch-implicit-mixed": 3.720006e9 / (3 * 6081291)}
 WORKLOADS = ("batch-implicit-mixed", "batch-explicit-mixed", "batch-explicit-fp64",
              "axon-explicit-fp64", "myelin-explicit-mixed", "serve")
 DEFAULT_WORKLOAD = "batch-implicit-mixed"
