@@ -8,12 +8,14 @@ arithmetic is the same whatever the grid):
 - the FP64 step: 32 .. 256 threads per block.
 
 Which one is fastest depends on the tree sizes, the share of HH compartments and the
-device, so `tune` times every candidate on the workload itself. It uses a sample of the
-trees in a batch of its own, so the caller's state is never touched: every k-th tree, which
-keeps the workload's mix of sizes, about `sample_elements` compartments but (implicit) at
-least `min_trees` trees, enough one-tree CTAs to fill every SM at the largest CTA count
-searched (a sample of a few large trees leaves most SMs idle, and then every CTA count times
-the same). It keeps the fastest. Results are cached in a JSON file
+device, so `tune` times every candidate on the workload itself, in a batch of its own, so
+the caller's state is never touched. The explicit steps tile the elements, and a sample
+stands for the workload: every k-th tree (the workload's mix of sizes), about
+`sample_elements` compartments. The implicit kernel gives each tree to one CTA, and its best
+CTA count depends on the whole population: on a quarter of the 4096-tree batch, 2 CTAs per
+SM ran fastest (the largest trees, which set a sample's time, share their SMs less), while on
+the whole batch 4 per SM beat 2 by a third (throughput over all trees). So the implicit
+kernel is timed on the whole workload, over fewer steps. It keeps the fastest. Results are cached in a JSON file
 per device, mode, precision and workload size, so a workload is tuned once per machine.
 
 The implicit block-per-instance kernel (batches) has one shape-only knob: how many of its
@@ -134,7 +136,7 @@ def _store(path: str, cache: dict) -> None:
 
 
 def tune(problems, mode: int = _lib.NRT_EXPLICIT, precision: str = "fp64", *,
-         steps: int = 64, warmup: int = 3, sample_elements: float = 4e6, min_trees: int = 0,
+         steps: int = 0, warmup: int = 3, sample_elements: float = 0, min_trees: int = 1,
          restarts=None, cache: str | None = None, timer=None, device_key: str | None = None,
          **opts) -> dict:
     """The fastest launch shape for `problems`: {"options": overrides, "key": cache key,
@@ -143,9 +145,9 @@ def tune(problems, mode: int = _lib.NRT_EXPLICIT, precision: str = "fp64", *,
 
     timer(problems, mode, precision, overrides) -> seconds per step replaces the device
     timing (tests use it); device_key replaces the device's name in the cache key.
-    min_trees: the sample's fewest trees (0: 1024 for the implicit kernel, whose CTAs each
-    take one tree -- 4 CTAs on each of up to 256 SMs; 1 for the explicit steps, which tile
-    the elements).  `opts` are the caller's other options (make_options keywords), kept
+    steps: timed steps per repeat (0: 64 explicit, 16 implicit); sample_elements: the sample's
+    size (0: 4e6 compartments explicit, the whole workload implicit); min_trees: the sample's
+    fewest trees.  `opts` are the caller's other options (make_options keywords), kept
     fixed."""
     cands = candidates(mode, precision, restarts)
     dev = device_key if device_key is not None else device_name(int(opts.get("device", -1)))
@@ -157,8 +159,9 @@ def tune(problems, mode: int = _lib.NRT_EXPLICIT, precision: str = "fp64", *,
         return {"options": dict(hit["options"]), "key": key, "times": None, "candidates": cands}
     if len(cands) == 1:
         return {"options": dict(cands[0]), "key": key, "times": [None], "candidates": cands}
-    if min_trees <= 0:
-        min_trees = 1 if mode == _lib.NRT_EXPLICIT else 1024
+    explicit = mode == _lib.NRT_EXPLICIT
+    steps = steps or (64 if explicit else 16)
+    sample_elements = sample_elements or (4e6 if explicit else math.inf)
     part = sample(problems, sample_elements, min_trees)
     if timer is None:
         def timer(ps, m, prec, ov):

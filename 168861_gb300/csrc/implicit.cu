@@ -1045,14 +1045,14 @@ __device__ __noinline__ double2 ph_assemble(Ctx<T, kGrid> c, const double *Vin,
       double b;
       if (!cn) {
         b = cm[u] * v[u] + kdx;
-        if (active) b += inp[u];
+        if (active && (f[u] & R_INP)) b += inp[u];  // other rows would add an exact 0
       } else {  // (2 c_m dX/dT + W dX) V^n - sum g (V^n - V^n_q) + 2 (K dX + I)
         b = (2.0 * cm[u] + wdx) * v[u];
         if (f[u] & R_UP) b -= gj[u] * (v[u] - vmo);
         if (f[u] & R_DOWNR) b -= gn[u] * (v[u] - vp[u]);
         if (f[u] & R_DOWNL) b -= gl * (v[u] - vl);
         b += 2.0 * kdx;
-        if (active) b += 2.0 * inp[u];
+        if (active && (f[u] & R_INP)) b += 2.0 * inp[u];
       }
       iv.rhs[r] = b;
       bacc += (T)b * (T)b;
