@@ -63,14 +63,19 @@ def choose(times: list[float]) -> int:
     return best
 
 
-def sample(problems, sample_elements: float, min_trees: int = 1) -> list:
-    """Every k-th tree from the first: about sample_elements compartments, and at least
-    min_trees trees (all of them when there are no more)."""
+def sample_indices(problems, sample_elements: float, min_trees: int = 1) -> list:
+    """Every k-th tree's index from the first: about sample_elements compartments, and at
+    least min_trees trees (all of them when there are no more)."""
     n = len(problems)
     total = sum(p.num_elem for p in problems)
     k = max(1, math.ceil(total / max(sample_elements, 1)))
     k = min(k, max(1, n // max(min_trees, 1)))
-    return list(problems[::k])
+    return list(range(0, n, k))
+
+
+def sample(problems, sample_elements: float, min_trees: int = 1) -> list:
+    """The trees of sample_indices."""
+    return [problems[i] for i in sample_indices(problems, sample_elements, min_trees)]
 
 
 def workload_key(device: str, mode: int, precision: str, problems, restarts=None) -> str:
@@ -93,15 +98,20 @@ def device_name(device: int = -1) -> str:
 
 
 def time_candidate(problems, mode: int, precision: str, overrides: dict, steps: int,
-                   warmup: int, repeats: int = 2, **opts) -> float:
+                   warmup: int, repeats: int = 2, runs=None, **opts) -> float:
     """Seconds per step of a batch of `problems` built with `overrides`: the best of
     `repeats` timings of `steps` steps after `warmup` steps, with the device idle on both
-    sides of each timing."""
+    sides of each timing.  runs: each tree's (i_begin, i_end, init_time, end_input), whose
+    stimulus windows the timed steps use (the loop ranges are lengthened to cover them);
+    None: no stimulus."""
     from .solver import Batch
     b = Batch(problems, mode, precision=precision, **{**opts, **overrides})
     try:
         total = warmup + repeats * steps
-        b.set_runs([(1, 1 + total, 0.0, -1.0)] * len(problems))
+        if runs is None:
+            b.set_runs([(1, 1 + total, 0.0, -1.0)] * len(problems))
+        else:
+            b.set_runs([(a, max(e, a + total), t0, t1) for a, e, t0, t1 in runs])
         b.advance(warmup)
         b.synchronize()
         best = math.inf
@@ -138,7 +148,7 @@ def _store(path: str, cache: dict) -> None:
 def tune(problems, mode: int = _lib.NRT_EXPLICIT, precision: str = "fp64", *,
          steps: int = 0, warmup: int = 3, sample_elements: float = 0, min_trees: int = 1,
          restarts=None, cache: str | None = None, timer=None, device_key: str | None = None,
-         **opts) -> dict:
+         runs=None, **opts) -> dict:
     """The fastest launch shape for `problems`: {"options": overrides, "key": cache key,
     "times": seconds per step of each candidate (None when served from the cache),
     "candidates": the shapes searched}.
@@ -147,8 +157,9 @@ def tune(problems, mode: int = _lib.NRT_EXPLICIT, precision: str = "fp64", *,
     timing (tests use it); device_key replaces the device's name in the cache key.
     steps: timed steps per repeat (0: 64 explicit, 16 implicit); sample_elements: the sample's
     size (0: 4e6 compartments explicit, the whole workload implicit); min_trees: the sample's
-    fewest trees.  `opts` are the caller's other options (make_options keywords), kept
-    fixed."""
+    fewest trees.  runs: the trees' loop ranges and stimulus windows (as Batch.set_runs), so
+    the timed steps see the workload's stimulus (None: none).  `opts` are the caller's other
+    options (make_options keywords), kept fixed."""
     cands = candidates(mode, precision, restarts)
     dev = device_key if device_key is not None else device_name(int(opts.get("device", -1)))
     key = workload_key(dev, mode, precision, problems, restarts)
@@ -162,10 +173,12 @@ def tune(problems, mode: int = _lib.NRT_EXPLICIT, precision: str = "fp64", *,
     explicit = mode == _lib.NRT_EXPLICIT
     steps = steps or (64 if explicit else 16)
     sample_elements = sample_elements or (4e6 if explicit else math.inf)
-    part = sample(problems, sample_elements, min_trees)
+    idx = sample_indices(problems, sample_elements, min_trees)
+    part = [problems[i] for i in idx]
+    part_runs = [runs[i] for i in idx] if runs is not None else None
     if timer is None:
         def timer(ps, m, prec, ov):
-            return time_candidate(ps, m, prec, ov, steps, warmup, **opts)
+            return time_candidate(ps, m, prec, ov, steps, warmup, runs=part_runs, **opts)
     times = []
     for ov in cands:
         try:

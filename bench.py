@@ -382,7 +382,7 @@ def run_ours(args, rank: int, world: int, dist, wl: str, extras: bool = True, st
     if (args.autotune if autotune is None else autotune):  # outside every timed region
         rest = {k: v for k, v in opts.items() if k != "precision"}
         tuned = importlib.import_module(pkg.__name__ + ".autotune").tune(probs, mode, precision,
-                                                                         **rest)
+                                                                         runs=runs, **rest)
         opts.update(tuned["options"])
         launch_shape = {"tuned": tuned["options"], "candidates": tuned["candidates"],
                         "seconds_per_step": tuned["times"]}

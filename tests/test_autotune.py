@@ -103,3 +103,24 @@ def test_implicit_tunes_its_cta_count(tmp_path):
                 timer=lambda ps, m, p, ov: ov["restart"] + ov["tile_ctas_per_sm"] / 10,
                 device_key="dev", restarts=[16, 20])
     assert r["options"] == {"restart": 16, "tile_ctas_per_sm": 2}
+
+
+def test_timer_gets_the_sampled_trees_runs(tmp_path):
+    """With runs, each sampled tree is timed with its own loop range and stimulus window."""
+    trees = [Tree(1000 + i) for i in range(40)]
+    runs = [(1, 100 + i, 0.0, 1e-3 * i) for i in range(40)]
+    got = []
+
+    def fake_time(ps, m, prec, ov, steps, warmup, runs=None, **opts):
+        got.append(([p.num_elem for p in ps], runs))
+        return 1.0
+
+    orig = at.time_candidate
+    at.time_candidate = fake_time
+    try:
+        at.tune(trees, lib.NRT_EXPLICIT, "fp64", cache="", sample_elements=10000, runs=runs,
+                device_key="dev")
+    finally:
+        at.time_candidate = orig
+    sizes, rs = got[0]
+    assert len(sizes) < 40 and rs == [runs[s - 1000] for s in sizes]
