@@ -4,8 +4,9 @@ A small CUDA program (compiled here with nvcc for sm_103a) times, over all SMs:
   - FP64 and FP32 fused multiply-adds (four independent chains per thread);
   - FP64 -> FP32 conversions;
   - the cycles a thread spends issuing one cp.async.bulk copy into shared memory.
-The test prints the figures (run with -s) and checks what the design relies on: FP64 arithmetic runs at a small fraction of the FP32 rate on this
-part, and a bulk copy keeps its issuing thread for hundreds of cycles.
+The test prints the figures (run with -s) and checks what the design relies on: FP64
+arithmetic runs at a small fraction of the FP32 rate on this part, and a bulk copy keeps its
+issuing thread for hundreds of cycles.
 """
 import shutil
 import subprocess
