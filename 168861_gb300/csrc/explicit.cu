@@ -484,9 +484,9 @@ __global__ void __launch_bounds__(kTileThreads) explicit_step_mixed_tiled(
 // (every CTA resident) with a grid barrier after each step.  On a GB300 it is not the
 // default: with the loop's launches chained and replayed from a graph, a launch boundary
 // costs about what a grid barrier across both dies costs (1002-element FP64 axon 7.42 vs
-// 8.17 us per step; the 199k-element myelinated axon 4.63 vs 5.14-5.48 us, 7.14 vs 9.78 us
-// with its strain ramp, which needs a second barrier per step).  Every thread owns the same elements at every step (a stride over the grid),
-// so an element's gates stay with one thread.  After the barrier that ends step k:
+// 8.17 us per step; the 199k-element myelinated axon without strain 4.63 vs 5.14-5.48 us).
+// Every thread owns the same elements at every step (a stride over the grid), so an
+// element's gates stay with one thread.  After the barrier that ends step k:
 //  - the probes read step k's potentials (step k + 1 writes the other buffer, and step
 //    k + 2, which overwrites it, starts after the next barrier);
 //  - with a strain ramp, the strained elements take step k + 1's row of the chunk table,
