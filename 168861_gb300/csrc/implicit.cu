@@ -24,7 +24,9 @@
 // step of iterative refinement.  Inner products and norms: per-thread partial sums in the
 // basis precision over the thread's rows, then FP64 across threads and CTAs in a fixed
 // order (deterministic, identical in every CTA).  Initial guess: V^n extrapolated
-// linearly from V^{n-1}.
+// linearly from V^{n-1}.  In mixed precision with the tree preconditioner a refinement
+// cycle is one preconditioned Richardson step, x += M^-1 r (see implicit_one_step), with
+// GMRES cycles taking over when a cycle lowers the true residual less than tenfold.
 //
 // Preconditioners: the exact tree factorisation (Hines order, see tree_factor), an exact
 // tridiagonal solve of every unbranched segment piece, Jacobi, or none.
