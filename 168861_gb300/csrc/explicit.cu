@@ -48,10 +48,13 @@ __device__ __forceinline__ int64_t ghost_source(const Topo &t, int64_t j) {
   return (t.flags & F_ROOT) ? j + 1 : (int64_t)t.mother;
 }
 
-// Element j of step k in FP64 (the body of explicit_step_f64 and of the chunk kernel).
+// Element j of step k in FP64 (the body of explicit_step_f64, of explicit_step_f64_lanes'
+// lane 0 and of the chunk kernel).  rates: the element's six HH rates when its lanes have
+// evaluated them (hh_rate64), else null (this thread evaluates them).
 template <bool kGeneral>
 __device__ __forceinline__ void f64_element(const PackView &p, int k, int force, int64_t j,
-                                            const double *Vin, double *Vout) {
+                                            const double *Vin, double *Vout,
+                                            const double *rates = nullptr) {
   const Topo tj = p.topo[j];
   const InstDev in = p.inst[tj.flags >> INST_SHIFT];
   const int64_t i = in.base + k;
@@ -67,11 +70,15 @@ __device__ __forceinline__ void f64_element(const PackView &p, int k, int force,
   if (tj.flags & F_HH) {
     const int64_t L = p.hp_ld;
     const double *hp = p.hp + hp_col(p, j, tj.flags >> INST_SHIFT);
-    GateStep64 g = hh_step64(v, p.gate[j], p.gate[N + j], p.gate[2 * N + j],
-                             hp[HP_LSNA * L], hp[HP_LSK * L], hp[HP_REST * L],
-                             hp[HP_DTMS * L], hp[HP_GNA * L], hp[HP_GK * L],
-                             hp[HP_GL * L], hp[HP_ENA * L], hp[HP_EK * L],
-                             hp[HP_EL * L]);
+    GateStep64 g =
+        rates ? hh_gates64(rates[0], rates[1], rates[2], rates[3], rates[4], rates[5],
+                           p.gate[j], p.gate[N + j], p.gate[2 * N + j], hp[HP_DTMS * L],
+                           hp[HP_GNA * L], hp[HP_GK * L], hp[HP_GL * L], hp[HP_ENA * L],
+                           hp[HP_EK * L], hp[HP_EL * L])
+              : hh_step64(v, p.gate[j], p.gate[N + j], p.gate[2 * N + j], hp[HP_LSNA * L],
+                          hp[HP_LSK * L], hp[HP_REST * L], hp[HP_DTMS * L], hp[HP_GNA * L],
+                          hp[HP_GK * L], hp[HP_GL * L], hp[HP_ENA * L], hp[HP_EK * L],
+                          hp[HP_EL * L]);
     p.gate[j] = g.m;
     p.gate[N + j] = g.h;
     p.gate[2 * N + j] = g.n;
@@ -107,6 +114,45 @@ __global__ void __launch_bounds__(256) explicit_step_f64(PackView p, int k, int 
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= p.ntot) return;
   f64_element<kGeneral>(p, k, force, j, Vin, Vout);
+}
+
+// Small FP64 packs: eight lanes per element.  One warp's FP64 work per element is the
+// step's floor when each warp holds 32 elements (six exponentials and three divisions each
+// on a pipe at 1/70 of FP32), so lanes 0-5 of an element's group evaluate one rate each with
+// the same code (hh_rate64: no divergence), lane 0 gathers them by shuffles and finishes the
+// element as explicit_step_f64 does.  Every lane of a warp takes part in the shuffles; lanes
+// of elements that are out of range, finished, passive or sealed-end ghosts evaluate rates
+// of a placeholder potential that nobody reads.  The same values as explicit_step_f64, bit
+// for bit.
+constexpr int kRateLanes = 8;
+
+template <bool kGeneral>
+__global__ void __launch_bounds__(256) explicit_step_f64_lanes(PackView p, int k, int force,
+                                                               const double *__restrict__ Vin,
+                                                               double *__restrict__ Vout) {
+  chain_acquire();  // the previous launch of the time loop has finished
+  chain_release();
+  const int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kRateLanes;
+  const int q = (int)(threadIdx.x % kRateLanes);
+  double vna = 0.0, vk = 0.0;
+  if (j < p.ntot) {  // the element's potential and shifts, as f64_element reads them
+    const Topo tj = p.topo[j];
+    const InstDev in = p.inst[tj.flags >> INST_SHIFT];
+    const bool term = (tj.flags & F_TERM) != 0;
+    if (in.base + k < in.iend && (tj.flags & F_HH)) {
+      const double v = Vin[(kGeneral || !term) ? j : ghost_source(tj, j)];
+      const int64_t L = p.hp_ld;
+      const double *hp = p.hp + hp_col(p, j, tj.flags >> INST_SHIFT);
+      vna = ((v + hp[HP_LSNA * L]) - hp[HP_REST * L]) * 1000.0;
+      vk = ((v + hp[HP_LSK * L]) - hp[HP_REST * L]) * 1000.0;
+    }
+  }
+  const double r = hh_rate64(q < 6 ? q : 5, vna, vk);
+  double rates[6];
+  const int base = (int)(threadIdx.x & 31) & ~(kRateLanes - 1);
+#pragma unroll
+  for (int s = 0; s < 6; s++) rates[s] = __shfl_sync(0xffffffffu, r, base + s);
+  if (q == 0 && j < p.ntot) f64_element<kGeneral>(p, k, force, j, Vin, Vout, rates);
 }
 
 // Mixed precision (element j of step k; the body of explicit_step_mixed and of the chunk
@@ -628,6 +674,11 @@ int launch_explicit_step(const PackView &pv, int precision, bool general, int k,
                                                    : 0u),
                               threads, 0, st, pv, k, force, Vin, Vout, Fin, Fout, f));
     }
+  } else if (pv.step_threads == 0 && pv.ntot * kRateLanes <= (int64_t)64 * 1024) {
+    // small packs (up to 8192 elements): eight lanes per element, 128-thread blocks
+    const unsigned lb = (unsigned)((pv.ntot * kRateLanes + 127) / 128);
+    NRT_CUDA(launch_chained(general ? explicit_step_f64_lanes<true> : explicit_step_f64_lanes<false>,
+                            lb, 128, 0, st, pv, k, force, Vin, Vout));
   } else {
     NRT_CUDA(launch_chained(general ? explicit_step_f64<true> : explicit_step_f64<false>, blocks,
                             threads, 0, st, pv, k, force, Vin, Vout));

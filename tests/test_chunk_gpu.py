@@ -169,3 +169,27 @@ def test_kernel_launch_counter(gpu, pkg, model):
     b.synchronize()
     assert pkg.kernel_launches() - l0 == 2  # the persistent kernel + loop-index update
     b.close()
+
+
+def test_fp64_rate_lanes_equal_one_thread_per_element(gpu, pkg, model):
+    """Small FP64 packs step with eight lanes per element (six evaluate one HH rate each,
+    lane 0 finishes the element); the result is bit for bit that of one thread per element
+    (step_threads set), over the exact first step and graph chunks, single trees and a
+    batch."""
+    axon = golden_axon(pkg)
+    tree = model.random_tree(seed=12, n_target=3000, depth_lo=5, depth_hi=8, tspan=2e-3)
+    cases = [[axon[1]], [built(pkg, tree)[0]],
+             [built(pkg, model.random_tree(seed=s, n_target=1500, depth_lo=4, depth_hi=7,
+                                           tspan=2e-3))[0] for s in (30, 31, 32)]]
+    for probs in cases:
+        assert sum(p.num_elem for p in probs) <= 8192  # the lanes kernel's range
+        states = []
+        for shape in ({}, {"step_threads": 64}):
+            b = pkg.Batch(probs, precision="fp64", **shape)
+            b.set_runs([(1, 1 + 300, 0.0, 3e-4)] * len(probs))
+            b.advance(37)
+            b.advance(200)
+            states.append([b.get_state(q) for q in range(len(probs))])
+            b.close()
+        for a, c in zip(*states):
+            assert_same_state(a, c)
