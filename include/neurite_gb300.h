@@ -129,8 +129,10 @@ typedef struct nrt_options {
                                     as fit, the default): of the mixed explicit tiled step,
                                     and of the implicit block-per-instance kernel (batches) */
   int32_t step_threads;          /* explicit, one thread per element: threads per block, a
-                                    multiple of 32 up to 256 (0 = chosen from the tree size).
-                                    Launch shapes only: results do not depend on them */
+                                    multiple of 32 up to 256 (0 = chosen from the tree size;
+                                    FP64 packs of up to 8192 elements then take eight lanes
+                                    per element).  Launch shapes only: results do not depend
+                                    on them */
   double inner_tol;              /* implicit, mixed precision: each FP64 refinement cycle's
                                     inner FP32 Krylov solve stops once its residual estimate
                                     is below inner_tol times the cycle's starting residual
