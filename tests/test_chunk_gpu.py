@@ -1,9 +1,13 @@
-"""The explicit time loop's chunk kernel (nrt_options.step_launch = 1: up to 64 steps per
-cooperative launch, grid barrier between steps) against one launch per step (the default,
-step_launch = 0): the potentials, the gates, the probes' samples and spike times, and the
-strained coefficients must come out bit for bit the same, over loop ranges that end inside
-a chunk, in FP64 and mixed precision, for single trees and for batches whose instances
-finish at different steps.
+"""Launch shapes of the explicit time loop that must not change a bit of the results:
+
+- the chunk kernel (nrt_options.step_launch = 1: up to 64 steps per cooperative launch,
+  grid barrier between steps) against one launch per step (the default): potentials, gates,
+  the probes' samples and spike times and the strained coefficients, over loop ranges that
+  end inside a chunk, FP64 and mixed, single trees and batches whose instances finish at
+  different steps;
+- small FP64 packs' eight lanes per element against one thread per element;
+
+and the library's count of its own kernel launches (nrt_kernel_launches).
 """
 import numpy as np
 import pytest
